@@ -1,0 +1,348 @@
+"""Benchmark: Lanczos ground state of the periodic XXZ chain, L = 24, Sz = 0.
+
+Workload (the reference's headline case): H = sum_i [Jxy/2 (S+_i S-_{i+1} + h.c.)
++ Jz S^z_i S^z_{i+1}], Jxy = Jz = 1, dim 2,704,156, nnz 36,564,892 (explicit
+zeros kept), FP64 Lanczos with krylov_dim = 100 from a seeded uniform[-1, 1]
+start vector.  One step = one getGroundState solve (100 sparse products and
+the fused dot / axpy / norm kernels, the tridiagonal solve and the Ritz
+vector) with the Hamiltonian and start vector already in HBM.
+
+  value    matvecs/s over the timed steps (CUDA events on the engine stream)
+  e2e      the same metric through the public API with host buffers: each step
+           uploads the start vector from pinned memory, solves, evaluates
+           psi.eval and downloads the Ritz vector
+  roofline achieved HBM GB/s of the CSR product kernel: algorithmic bytes
+           nnz*(8+4) + (dim+1)*8 + 2*dim*8 per launch / CUDA-event time
+  cpu_baseline  the CPU oracle port (the reference's CSC column-push product,
+           complex128, one core like the reference) on a bounded sample
+
+--impl reference times that CPU port alone on the same workload.
+Multi-GPU: each rank solves its own copy (replicas; no data-path collective).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L = 24
+KRY = 100
+SEED = 12345
+METRIC = "matvecs/s (Lanczos ground state, XXZ L=24 Sz=0, FP64)"
+UNIT = "matvecs/s"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    def __init__(self, world, local):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch
+            import torch.distributed as dist
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+            self.dist = dist
+            self.torch = torch
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device="cuda")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device="cuda")
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                p = [x.strip() for x in line.split(",")]
+                if len(p) < 9:
+                    continue
+                try:
+                    sms.append(float(p[1]))
+                    mx = float(p[2])
+                except ValueError:
+                    continue
+                for n, v in zip(names, p[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        os.unlink(self.path)
+        if not sms:
+            return None
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sms)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(kernel_key: str):
+    """dram bytes per launch recorded from an ncu capture in profiles/ (line
+    `traffic_bytes_per_launch: <n>` in the summary named for the kernel)."""
+    path = os.path.join(ROOT, "profiles", f"{kernel_key}.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if line.strip().startswith("traffic_bytes_per_launch:"):
+                try:
+                    return float(line.split(":", 1)[1].strip().split()[0])
+                except ValueError:
+                    return None
+    return None
+
+
+# ----------------------------------------------------------------- CPU legs
+def cpu_sample(kry: int, budget_s: float):
+    """The oracle port on one core: repeated Lanczos solves of kry steps at L=24."""
+    import oracle as O
+    from qudrip_gb300 import chains
+    spec, ham = chains.xxz_chain(L)
+    sec = O.Sector(spec)
+    H = O.Ham(sec, ham)
+    v0 = np.random.Generator(np.random.PCG64(SEED)).uniform(-1.0, 1.0, sec.dim)
+    return H, v0
+
+
+def run_cpu_steps(H, v0, kry, steps):
+    mv = 0
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        r = H.lanczos_ground(v0, kry)
+        mv += r["matvecs"]
+    dt = time.perf_counter() - t0
+    return mv, dt
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return 0
+    H, v0 = cpu_sample(4, 0)
+    kry = 4  # bounded sample: 2*4 products per solve (first pass + getState pass)
+    run_cpu_steps(H, v0, kry, args.warmup)
+    mv, dt = run_cpu_steps(H, v0, kry, args.steps)
+    value = mv / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic (seeded uniform[-1,1] start vector)",
+        "config": {"workload": "xxz_chain_L24_periodic_Sz0_lanczos", "L": L, "dim": H.dim, "nnz": H.nnz,
+                   "krylov_dim_sample": kry, "spmv": "csc_column_push_complex128"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"{args.steps} Lanczos solves with krylov_dim={kry} at L=24 "
+                                   "(CPU restatement of the reference; the reference is single-threaded)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ----------------------------------------------------------------- GPU arm
+def gpu_arm(args, rank, world, local):
+    import qudrip_gb300 as q
+    from qudrip_gb300 import _capi as A
+    from qudrip_gb300 import chains
+
+    dist = Dist(world, local)
+    ctx = q.Context(local)
+    spec, ham = chains.xxz_chain(L)
+    sec = q.Sector(spec.index, spec.constraints, ctx=ctx)
+    H = sec.lower(ham)
+    dim = sec.dim
+    v0 = q.start_vector(dim, SEED).astype(np.complex128)
+    psi = q.getState(sec, 2)
+    psi.set(1, v0)  # resident start vector
+    solver = q.Arnoldi.getLanczosSolver(sec, KRY)
+
+    def solve_resident():
+        A.call("qd_state_copy", psi.handle, 1, psi.handle, 0)
+        return solver.getGroundState(H, psi(0), 0)
+
+    for _ in range(args.warmup):
+        solve_resident()
+    ctx.sync()
+    clocks = ClockSampler(local)
+    clocks.start()
+    dist.barrier()
+    ctx.sync()
+    l0 = ctx.launches()
+    A.call("qd_ctx_record", ctx.handle, 0)
+    mv = 0
+    ritz = None
+    for _ in range(args.steps):
+        r = solve_resident()
+        mv += r.matvecs
+        ritz = r.ritz_value
+    A.call("qd_ctx_record", ctx.handle, 1)
+    ms = C.c_float(0)
+    A.call("qd_ctx_elapsed", ctx.handle, 0, 1, C.byref(ms))
+    ctx.sync()
+    launches = ctx.launches() - l0
+    dist.barrier()
+    clk = clocks.stop()
+    t_max = dist.max(ms.value / 1e3)
+    mv_all = dist.sum(float(mv))
+    value = mv_all / t_max
+
+    # roofline of the product kernel, timed live on the engine stream
+    avg_ms = C.c_double(0)
+    nbytes = C.c_double(0)
+    A.call("qd_ham_time_spmv", H.handle, A.QD_SPMV_CSR, 50, C.byref(avg_ms), C.byref(nbytes))
+    hbm_peak, peak_kind = peaks()
+    achieved = nbytes.value / (avg_ms.value * 1e-3) / 1e9
+    traffic = profile_traffic("spmv_csr_f64_xxz_L24")
+
+    # end to end through the public API with pinned host buffers
+    hb = C.c_void_p()
+    A.call("qd_host_alloc", dim * 16, C.byref(hb))
+    hv = np.ctypeslib.as_array((C.c_double * (2 * dim)).from_address(hb.value)).view(np.complex128)
+    hv[:] = v0
+    ho = C.c_void_p()
+    A.call("qd_host_alloc", dim * 16, C.byref(ho))
+    dptr = C.cast(hb, C.POINTER(C.c_double))
+    optr = C.cast(ho, C.POINTER(C.c_double))
+    e_steps = max(1, min(args.steps, 5))
+
+    def e2e_step():
+        A.call("qd_state_upload", psi.handle, 0, dptr)
+        r = solver.getGroundState(H, psi(0), 0)
+        E = psi.eval(0, H)
+        A.call("qd_state_download", psi.handle, 0, optr)
+        return r, E
+
+    e2e_step()
+    dist.barrier()
+    t0 = time.perf_counter()
+    e_mv = 0
+    energy = None
+    for _ in range(e_steps):
+        r, energy = e2e_step()
+        e_mv += r.matvecs + 1
+    ctx.sync()
+    t_e2e = dist.max(time.perf_counter() - t0)
+    e2e_value = dist.sum(float(e_mv)) / t_e2e
+    A.call("qd_host_free", hb)
+    A.call("qd_host_free", ho)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        Ho, ov0 = cpu_sample(4, 0)
+        mv_c, dt_c = run_cpu_steps(Ho, ov0, 4, 6)
+        cpu = {"value": mv_c / dt_c, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": "6 Lanczos solves with krylov_dim=4 at L=24 (48 complex128 CSC products plus "
+                         "vector work, CPU restatement of the reference, single-threaded like it)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * t_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded uniform[-1,1] start vector; Hamiltonian built from the operator tree)",
+            "config": {"workload": "xxz_chain_L24_periodic_Sz0_lanczos_k100", "L": L, "Jxy": 1.0, "Jz": 1.0,
+                       "dim": dim, "nnz": H.nnz, "krylov_dim": KRY, "spmv": "csr_warp_tile_fp64",
+                       "ritz": "stored_basis", "parallelism": f"replicas{world}",
+                       "l2": "inputs larger than L2 (CSR 493 MB); no flush",
+                       "ritz_value": ritz, "psi_eval": energy.real if energy is not None else None},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": dim * 16,
+                    "d2h_bytes_per_step": dim * 16 + 16},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "traffic": traffic,
+                         "kernel": "spmv_tile_kernel<double,double>", "peak_kind": peak_kind,
+                         "bytes_per_launch": nbytes.value, "launch_ms": avg_ms.value},
+            "cpu_baseline": cpu,
+            "clocks": clk,
+        }
+        print(json.dumps(line))
+    dist.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return reference_arm(args, rank, world)
+    return gpu_arm(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,238 @@
+/*
+ * qudrip_gb300.h -- C ABI of the GB300 (sm_103a) exact-diagonalization engine.
+ *
+ * This is the drop-in boundary for QuDrip's exact-diagonalization path.  The
+ * reference has no FFI: its boundary is the C++ template API of
+ * include/{index,conservation,operator,operator_abel,state,sparse_algorithm}.hpp.
+ * Every entry point below names the reference interface it replaces
+ * (file:line inside the QuDrip project).  The C++ drop-in header
+ * include/qudrip_gpu.hpp rebuilds the reference's own names on top of these.
+ *
+ * Conventions
+ *   - Every function returns a qd_status; QD_OK is 0.  Nothing aborts.
+ *   - Host arrays belong to the caller; device memory belongs to the handles.
+ *   - Complex numbers are interleaved (re, im) doubles, i.e. C99 double
+ *     complex / std::complex<double> layout.
+ *   - A qd_ctx owns one CUDA stream; handles made from one context must not be
+ *     used from two host threads at once.  Contexts are independent.
+ */
+#ifndef QUDRIP_GB300_H
+#define QUDRIP_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QD_API_VERSION 1
+
+typedef int qd_status;
+enum {
+  QD_OK = 0,
+  QD_ERR_INVALID = 1,     /* bad argument, size or handle */
+  QD_ERR_OOM = 2,         /* device allocation failed */
+  QD_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  QD_ERR_BREAKDOWN = 4,   /* Krylov breakdown (norm < 1e-10); reported, not fatal */
+  QD_ERR_TIMEOUT = 5,     /* a bounded device-side wait gave up */
+  QD_ERR_UNSUPPORTED = 6, /* valid request the engine does not implement */
+  QD_ERR_OVERFLOW = 7,    /* a per-column leaf table or an index type overflowed */
+  QD_ERR_NOT_HERMITIAN = 8,
+  QD_ERR_BUSY = 9         /* server slot / admission refused for now */
+};
+
+typedef struct qd_ctx qd_ctx;
+typedef struct qd_sector qd_sector;
+typedef struct qd_ham qd_ham;
+typedef struct qd_state qd_state;
+
+/* ------------------------------------------------------------------ */
+/* Context                                                            */
+/* ------------------------------------------------------------------ */
+qd_status qd_ctx_create(int device, qd_ctx **out);
+qd_status qd_ctx_destroy(qd_ctx *ctx);
+qd_status qd_ctx_sync(qd_ctx *ctx);
+/* The CUDA stream (cudaStream_t) all work of this context is issued on. */
+qd_status qd_ctx_stream(qd_ctx *ctx, void **stream_out);
+/* Number of kernels this context launched since creation (diagnostics). */
+qd_status qd_ctx_launch_count(qd_ctx *ctx, int64_t *count);
+/* Timing on the context's stream: record event `slot` (0..15); elapsed ms
+ * between two recorded slots (waits for the later one). */
+qd_status qd_ctx_record(qd_ctx *ctx, int slot);
+qd_status qd_ctx_elapsed(qd_ctx *ctx, int slot_a, int slot_b, float *ms);
+/* Page-locked host memory for fast host<->device copies. */
+qd_status qd_host_alloc(int64_t bytes, void **out);
+qd_status qd_host_free(void *p);
+const char *qd_status_string(qd_status s);
+/* Last error message recorded on this host thread (empty if none). */
+const char *qd_last_error(void);
+int qd_api_version(void);
+
+/* ------------------------------------------------------------------ */
+/* Conserved quantities and sectors                                   */
+/*   replaces getQbits (index.hpp:80-94,300), getNset/getNup/getNdo   */
+/*   (conservation.hpp:89-115,233-246), getNd/getNh (117-157,248-256),*/
+/*   Constrain/LooseConstrain/Evaluate (conservation.hpp:200-231) and */
+/*   SubIndex (index.hpp:187-261)                                     */
+/* ------------------------------------------------------------------ */
+enum { QD_CQ_NSET = 0, QD_CQ_ND = 1 };
+
+typedef struct {
+  int32_t kind;  /* QD_CQ_NSET: popcount(state & mask)                       */
+                 /* QD_CQ_ND:   popcount(((s>>nsite)^m) & (s^m)), m = hole ?  */
+                 /*             low nsite bits : 0 (doublons / holons)       */
+  int32_t nsite; /* QD_CQ_ND only */
+  int32_t hole;  /* QD_CQ_ND only: 0 = doublon count, 1 = holon count */
+  int32_t coef;  /* integer weight of this quantity in the constraint sum */
+  uint64_t mask; /* QD_CQ_NSET only */
+} qd_cq_term;
+
+/* One `cq = target` argument of Constrain: sum_k coef_k * Q_k == target
+ * (|difference| <= tight). */
+typedef struct {
+  int32_t nterms; /* 1..4 */
+  int32_t reserved;
+  int64_t target;
+  qd_cq_term term[4];
+} qd_constraint;
+
+/* Sector of an nbits-qubit register (nbits <= 62).  The basis is every
+ * state that satisfies all constraints, in ascending integer order; ncons == 0
+ * gives the full 2^nbits space (dim must fit in int32). tight is
+ * LooseConstrain's tolerance (0 for Constrain). */
+qd_status qd_sector_create(qd_ctx *ctx, int nbits, const qd_constraint *cons,
+                           int ncons, int tight, qd_sector **out);
+qd_status qd_sector_destroy(qd_sector *sec);
+qd_status qd_sector_dim(const qd_sector *sec, int64_t *dim);
+/* 1 if ranks come from the combinatorial number system (product of
+ * popcount constraints on disjoint contiguous bit fields), 0 if from a search
+ * of the sorted basis. */
+qd_status qd_sector_rank_kind(const qd_sector *sec, int *kind);
+/* Copy the basis (dim states, ascending) to host memory. */
+qd_status qd_sector_basis(qd_sector *sec, uint64_t *host_states);
+/* rank of each state; states outside the sector get dim (the reference's
+ * SubIndex returns range(), index.hpp:234-240). */
+qd_status qd_sector_rank(qd_sector *sec, const uint64_t *host_states, int64_t n,
+                         int64_t *host_ranks);
+
+/* ------------------------------------------------------------------ */
+/* Operator trees                                                     */
+/*   replaces bitOp / getBoseGate / getFermiGate (operators/bit.hpp), */
+/*   hopBitOp / getHopFermiGate / getHopBoseGate (operators/hopbit.hpp)*/
+/*   Operator products (operator.hpp:68-132) and OperatorSum          */
+/*   (operator_abel.hpp:9-158)                                        */
+/* ------------------------------------------------------------------ */
+enum { QD_GATE_BIT = 0, QD_GATE_HOP = 1 };
+
+typedef struct {
+  int32_t kind;   /* QD_GATE_BIT or QD_GATE_HOP */
+  int32_t site;   /* BIT: the site; HOP: creation site a of gate(a, b) */
+  int32_t site_b; /* HOP: annihilation site b of gate(a, b); a == b is n_a */
+  int32_t string; /* +1 bosonic gate, -1 fermionic (Jordan-Wigner) gate */
+  /* BIT only: the 2x2 matrix given with `gate << U`, row-major,
+   * u[2*(2*i+j)] + i*u[2*(2*i+j)+1] = U(i, j).  The amplitude from input bit
+   * b to output bit o is U(b, o), i.e. the gate applies U transposed, exactly
+   * as elOpBase::operator<< (operator.hpp:24-29) with bitOp::branch
+   * (operators/bit.hpp:62-63). */
+  double u[8];
+} qd_gate;
+
+typedef struct {
+  double coeff_re, coeff_im;
+  int32_t gate_offset; /* first gate of this product in the gate array */
+  int32_t ngates;      /* gates g[off] * g[off+1] * ...; applied right to left */
+} qd_term;
+
+/* ------------------------------------------------------------------ */
+/* Lowering `OperatorSum >> index`                                     */
+/*   replaces Operator::operator>> / full_branch (operator.hpp:135-267) */
+/*   and OperatorSum::operator>> (operator_abel.hpp:25-34)            */
+/* The result is bit-identical to the reference's Eigen CSC matrix:    */
+/* same sparsity pattern (explicit zeros from cross-term cancellation   */
+/* kept, leaves with |value| <= 1e-10 dropped before duplicate sums)    */
+/* and the same complex128 values.  It is held on the device as CSR.   */
+/* ------------------------------------------------------------------ */
+enum { QD_HAM_REAL = 1, QD_HAM_HERMITIAN = 2 };
+
+typedef struct {
+  int64_t dim;
+  int64_t nnz;
+  int32_t flags;       /* QD_HAM_REAL | QD_HAM_HERMITIAN */
+  int32_t max_row_nnz;
+  int32_t has_matrix_free; /* 1 if qd_ham_build_matrix_free succeeded */
+  int32_t reserved;
+} qd_ham_info;
+
+qd_status qd_ham_lower(qd_sector *sec, const qd_term *terms, int nterms,
+                       const qd_gate *gates, int ngates, qd_ham **out);
+qd_status qd_ham_destroy(qd_ham *ham);
+qd_status qd_ham_get_info(qd_ham *ham, qd_ham_info *info);
+/* Reference layout: column pointers (dim+1), row indices sorted within each
+ * column, complex values (2*nnz doubles). */
+qd_status qd_ham_download_csc(qd_ham *ham, int64_t *colptr, int32_t *rowidx,
+                              double *vals);
+qd_status qd_ham_download_csr(qd_ham *ham, int64_t *rowptr, int32_t *colidx,
+                              double *vals);
+
+/* ------------------------------------------------------------------ */
+/* States                                                             */
+/*   replaces State / getState / operator() / eval (state.hpp:9-104)  */
+/* A state is nt complex128 columns of length dim on the device.       */
+/* ------------------------------------------------------------------ */
+qd_status qd_state_create(qd_ctx *ctx, int64_t dim, int nt, qd_state **out);
+qd_status qd_state_destroy(qd_state *st);
+qd_status qd_state_upload(qd_state *st, int t, const double *host_complex);
+qd_status qd_state_download(qd_state *st, int t, double *host_complex);
+/* dst(:, t_dst) = src(:, t_src) on the device (same dim). */
+qd_status qd_state_copy(qd_state *src, int t_src, qd_state *dst, int t_dst);
+/* Device address of column t (complex128, dim entries). */
+qd_status qd_state_device_ptr(qd_state *st, int t, void **dptr);
+/* y(:, t_out) = H * x(:, t_in)   (Eigen `H * psi`) */
+qd_status qd_ham_apply(qd_ham *ham, qd_state *x, int t_in, qd_state *y,
+                       int t_out);
+/* psi(:,t)^dagger * H * psi(:,t), unnormalised, as State::eval
+ * (state.hpp:33-45). */
+qd_status qd_state_eval(qd_state *psi, int t, qd_ham *ham, double *re_im);
+
+/* ------------------------------------------------------------------ */
+/* Lanczos ground state                                               */
+/*   replaces Arnoldi::getLanczosSolver(...).getGroundState            */
+/*   (sparse_algorithm.hpp:395-425, 458-473, 475-604)                  */
+/* ------------------------------------------------------------------ */
+enum { QD_SPMV_CSR = 0, QD_SPMV_MATRIX_FREE = 1 };
+enum { QD_RITZ_STORED_BASIS = 0, QD_RITZ_SECOND_PASS = 1 };
+
+typedef struct {
+  int32_t krylov_dim; /* kry_dim of getLanczosSolver(index, kry_dim) */
+  int32_t spmv;       /* QD_SPMV_CSR or QD_SPMV_MATRIX_FREE */
+  int32_t ritz;       /* QD_RITZ_STORED_BASIS (default) or QD_RITZ_SECOND_PASS */
+  int32_t reserved;
+} qd_lanczos_opts;
+
+typedef struct {
+  int32_t act_dim;    /* Krylov dimension reached (act_dim() of the solver) */
+  int32_t breakdown;  /* 1 if the recurrence stopped at norm < 1e-10 */
+  int32_t matvecs;    /* sparse matrix-vector products performed */
+  int32_t reserved;
+  double ritz_value;  /* lowest eigenvalue of the Krylov matrix */
+  double err;         /* error(): norm of eigenvalue change (first call: |lambda_0|) */
+} qd_lanczos_result;
+
+/* psi(:, t) is the start vector on entry and the (unnormalised) Ritz vector on
+ * exit, exactly as getGroundState overwrites psi(tstp).  evals_out (may be
+ * NULL) receives act_dim ascending Krylov eigenvalues. */
+qd_status qd_lanczos_ground(qd_ham *ham, qd_state *psi, int t,
+                            const qd_lanczos_opts *opts, double *evals_out,
+                            qd_lanczos_result *res);
+
+/* Average device time of the sparse product kernel the solvers use on this
+ * Hamiltonian (iters back-to-back launches on the context stream, timed with
+ * CUDA events), and the kernel's algorithmic HBM bytes per launch:
+ * CSR: nnz*(value + 4) + (dim+1)*8 + dim*(x + y) bytes. */
+qd_status qd_ham_time_spmv(qd_ham *ham, int spmv, int iters, double *avg_ms,
+                           double *bytes_per_launch);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QUDRIP_GB300_H */

@@ -1,0 +1,165 @@
+"""ctypes view of the C ABI declared in include/qudrip_gb300.h.
+
+The structures are defined without loading the shared library so that host
+logic (operator algebra, argument packing) works on machines without a GPU.
+`lib()` loads the in-tree library and fails loudly when it is missing: the
+engine has no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libqudrip_gb300.so")
+
+# status codes (qudrip_gb300.h)
+QD_OK = 0
+QD_ERR_INVALID = 1
+QD_ERR_OOM = 2
+QD_ERR_CUDA = 3
+QD_ERR_BREAKDOWN = 4
+QD_ERR_TIMEOUT = 5
+QD_ERR_UNSUPPORTED = 6
+QD_ERR_OVERFLOW = 7
+QD_ERR_NOT_HERMITIAN = 8
+QD_ERR_BUSY = 9
+
+QD_CQ_NSET = 0
+QD_CQ_ND = 1
+QD_GATE_BIT = 0
+QD_GATE_HOP = 1
+QD_HAM_REAL = 1
+QD_HAM_HERMITIAN = 2
+QD_SPMV_CSR = 0
+QD_SPMV_MATRIX_FREE = 1
+QD_RITZ_STORED_BASIS = 0
+QD_RITZ_SECOND_PASS = 1
+
+
+class qd_cq_term(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("nsite", C.c_int32), ("hole", C.c_int32),
+                ("coef", C.c_int32), ("mask", C.c_uint64)]
+
+
+class qd_constraint(C.Structure):
+    _fields_ = [("nterms", C.c_int32), ("reserved", C.c_int32), ("target", C.c_int64),
+                ("term", qd_cq_term * 4)]
+
+
+class qd_gate(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("site", C.c_int32), ("site_b", C.c_int32),
+                ("string", C.c_int32), ("u", C.c_double * 8)]
+
+
+class qd_term(C.Structure):
+    _fields_ = [("coeff_re", C.c_double), ("coeff_im", C.c_double),
+                ("gate_offset", C.c_int32), ("ngates", C.c_int32)]
+
+
+class qd_ham_info(C.Structure):
+    _fields_ = [("dim", C.c_int64), ("nnz", C.c_int64), ("flags", C.c_int32),
+                ("max_row_nnz", C.c_int32), ("has_matrix_free", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class qd_lanczos_opts(C.Structure):
+    _fields_ = [("krylov_dim", C.c_int32), ("spmv", C.c_int32), ("ritz", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class qd_lanczos_result(C.Structure):
+    _fields_ = [("act_dim", C.c_int32), ("breakdown", C.c_int32), ("matvecs", C.c_int32),
+                ("reserved", C.c_int32), ("ritz_value", C.c_double), ("err", C.c_double)]
+
+
+class QDError(RuntimeError):
+    def __init__(self, code: int, where: str, msg: str):
+        super().__init__(f"{where}: status {code} ({msg})")
+        self.code = code
+
+
+_P = C.c_void_p
+_PP = C.POINTER(C.c_void_p)
+_I64P = C.POINTER(C.c_int64)
+_DP = C.POINTER(C.c_double)
+
+# name -> (argtypes); every function returns qd_status (int) unless listed in _RESTYPES
+_SIGNATURES = {
+    "qd_ctx_create": [C.c_int, _PP],
+    "qd_ctx_destroy": [_P],
+    "qd_ctx_sync": [_P],
+    "qd_ctx_stream": [_P, _PP],
+    "qd_ctx_launch_count": [_P, _I64P],
+    "qd_ctx_record": [_P, C.c_int],
+    "qd_ctx_elapsed": [_P, C.c_int, C.c_int, C.POINTER(C.c_float)],
+    "qd_host_alloc": [C.c_int64, _PP],
+    "qd_host_free": [_P],
+    "qd_ham_time_spmv": [_P, C.c_int, C.c_int, _DP, _DP],
+    "qd_status_string": [C.c_int],
+    "qd_last_error": [],
+    "qd_api_version": [],
+    "qd_sector_create": [_P, C.c_int, C.POINTER(qd_constraint), C.c_int, C.c_int, _PP],
+    "qd_sector_destroy": [_P],
+    "qd_sector_dim": [_P, _I64P],
+    "qd_sector_rank_kind": [_P, C.POINTER(C.c_int)],
+    "qd_sector_basis": [_P, C.POINTER(C.c_uint64)],
+    "qd_sector_rank": [_P, C.POINTER(C.c_uint64), C.c_int64, _I64P],
+    "qd_ham_lower": [_P, C.POINTER(qd_term), C.c_int, C.POINTER(qd_gate), C.c_int, _PP],
+    "qd_ham_destroy": [_P],
+    "qd_ham_get_info": [_P, C.POINTER(qd_ham_info)],
+    "qd_ham_download_csc": [_P, _I64P, C.POINTER(C.c_int32), _DP],
+    "qd_ham_download_csr": [_P, _I64P, C.POINTER(C.c_int32), _DP],
+    "qd_state_create": [_P, C.c_int64, C.c_int, _PP],
+    "qd_state_destroy": [_P],
+    "qd_state_upload": [_P, C.c_int, _DP],
+    "qd_state_download": [_P, C.c_int, _DP],
+    "qd_state_device_ptr": [_P, C.c_int, _PP],
+    "qd_state_copy": [_P, C.c_int, _P, C.c_int],
+    "qd_ham_apply": [_P, _P, C.c_int, _P, C.c_int],
+    "qd_state_eval": [_P, C.c_int, _P, _DP],
+    "qd_lanczos_ground": [_P, _P, C.c_int, C.POINTER(qd_lanczos_opts), _DP,
+                          C.POINTER(qd_lanczos_result)],
+}
+_RESTYPES = {"qd_status_string": C.c_char_p, "qd_last_error": C.c_char_p,
+             "qd_api_version": C.c_int}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def declared_symbols():
+    """Names of every entry point this module binds (all declared in the header)."""
+    return sorted(_SIGNATURES)
+
+
+def lib():
+    """Load libqudrip_gb300.so (built in-tree by __graft_entry__.build())."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise ImportError(
+                    f"qudrip_gb300 CUDA library not found at {LIB_PATH}; "
+                    "run `python -c 'import __graft_entry__ as g; g.build()'` first "
+                    "(there is no CPU fallback)")
+            L = C.CDLL(LIB_PATH)
+            for name, args in _SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.argtypes = args
+                fn.restype = _RESTYPES.get(name, C.c_int)
+            _lib = L
+    return _lib
+
+
+def check(code: int, where: str):
+    if code != QD_OK:
+        L = lib()
+        msg = (L.qd_last_error() or b"").decode() or (L.qd_status_string(code) or b"").decode()
+        raise QDError(code, where, msg)
+
+
+def call(name: str, *args):
+    fn = getattr(lib(), name)
+    check(fn(*args), name)

@@ -1,0 +1,158 @@
+// common.cuh -- shared infrastructure of the GB300 engine: status handling,
+// device allocation bookkeeping, exact (non-contracted) complex arithmetic.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/qudrip_gb300.h"
+
+namespace qd {
+
+// ---------------------------------------------------------------- errors
+void set_error(const char* fmt, ...);
+void clear_error();
+
+struct Error {
+  qd_status code;
+};
+
+#define QD_CUDA(call)                                                                  \
+  do {                                                                                 \
+    cudaError_t e__ = (call);                                                          \
+    if (e__ != cudaSuccess) {                                                          \
+      ::qd::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e__)); \
+      throw ::qd::Error{e__ == cudaErrorMemoryAllocation ? QD_ERR_OOM : QD_ERR_CUDA};  \
+    }                                                                                  \
+  } while (0)
+
+#define QD_REQUIRE(cond, code, ...)   \
+  do {                                \
+    if (!(cond)) {                    \
+      ::qd::set_error(__VA_ARGS__);   \
+      throw ::qd::Error{code};        \
+    }                                 \
+  } while (0)
+
+#define QD_LAUNCHED(ctx) ((ctx)->launches++)
+
+#define QD_CHECK_LAUNCH()                                                              \
+  do {                                                                                 \
+    cudaError_t e__ = cudaGetLastError();                                              \
+    if (e__ != cudaSuccess) {                                                          \
+      ::qd::set_error("%s:%d kernel launch: %s", __FILE__, __LINE__, cudaGetErrorString(e__)); \
+      throw ::qd::Error{QD_ERR_CUDA};                                                  \
+    }                                                                                  \
+  } while (0)
+
+// Wrap a C-ABI body: converts thrown qd::Error into a status code.
+template <typename F>
+qd_status guard(F&& f) {
+  try {
+    clear_error();
+    f();
+    return QD_OK;
+  } catch (const Error& e) {
+    return e.code;
+  } catch (...) {
+    set_error("unexpected host exception");
+    return QD_ERR_INVALID;
+  }
+}
+
+// ---------------------------------------------------------------- device buffers
+// Owning device buffer (cudaMalloc / cudaFree); never copied.
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DBuf() = default;
+  explicit DBuf(size_t count) { alloc(count); }
+  DBuf(const DBuf&) = delete;
+  DBuf& operator=(const DBuf&) = delete;
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) {
+    o.p = nullptr;
+    o.n = 0;
+  }
+  DBuf& operator=(DBuf&& o) noexcept {
+    if (this != &o) {
+      release();
+      p = o.p;
+      n = o.n;
+      o.p = nullptr;
+      o.n = 0;
+    }
+    return *this;
+  }
+  ~DBuf() { release(); }
+  void alloc(size_t count) {
+    release();
+    if (count == 0) count = 1;
+    QD_CUDA(cudaMalloc((void**)&p, count * sizeof(T)));
+    n = count;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  size_t bytes() const { return n * sizeof(T); }
+};
+
+// ---------------------------------------------------------------- context
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  int64_t launches = 0;
+  cudaEvent_t events[16] = {};
+};
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+}  // namespace qd
+
+// ---------------------------------------------------------------- device math
+// Complex arithmetic with one rounding per product and per sum (the
+// __d*_rn intrinsics are never contracted into FMA).  This reproduces the
+// reference's std::complex<double> results bit for bit.
+struct __align__(16) cplx {
+  double re, im;
+};
+
+__host__ __device__ inline cplx mkc(double r, double i) {
+  cplx c;
+  c.re = r;
+  c.im = i;
+  return c;
+}
+
+#ifdef __CUDACC__
+__device__ __forceinline__ cplx cmul_rn(cplx a, cplx b) {
+  return mkc(__dsub_rn(__dmul_rn(a.re, b.re), __dmul_rn(a.im, b.im)),
+             __dadd_rn(__dmul_rn(a.re, b.im), __dmul_rn(a.im, b.re)));
+}
+__device__ __forceinline__ cplx cadd_rn(cplx a, cplx b) {
+  return mkc(__dadd_rn(a.re, b.re), __dadd_rn(a.im, b.im));
+}
+__device__ __forceinline__ cplx rmul_rn(double r, cplx b) {
+  return mkc(__dmul_rn(r, b.re), __dmul_rn(r, b.im));
+}
+#endif

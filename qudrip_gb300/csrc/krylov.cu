@@ -1,0 +1,362 @@
+// krylov.cu -- SpMV entry points, psi.eval, and the Lanczos ground state.
+//
+// Lanczos (Arnoldi::ArnoldiSolver<T, herm=1>, sparse_algorithm.hpp:395-425,
+// 458-473, 514-585).  Step k = 1..kry_dim, with v1 = v_{k-1}, v2 = v_{k-2}:
+//   K1  w = H v1                  fused with  beta'_k = <v2, w>   (k >= 2)
+//   K2  w -= beta'_k v2           fused with  alpha_k = <v1, w>
+//   K3  w -= alpha_k v1           fused with  n_k = ||w||, stop if n_k < 1e-10
+//   K4  v_k = w / n_k   (stored: the basis is kept in HBM)
+// This is the reference's order of operations (local orthogonalisation
+// against the two previous vectors, no full reorthogonalisation).  The
+// scalars stay on the device, so the whole recurrence is one CUDA graph with
+// no host round trip; a breakdown sets a device flag that turns the remaining
+// steps into no-ops.  The tridiagonal matrix tridiag(Re alpha, n) is solved on
+// the host and the Ritz vector psi = sum_k y_k v_k is formed from the stored
+// basis -- the values the reference's second Lanczos pass (getState<1>)
+// regenerates, obtained without repeating the kry_dim products.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "krylov.cuh"
+#include "spmv.cuh"
+#include "tridiag.cuh"
+
+namespace qd {
+
+constexpr int kVecThreads = 256;
+
+static int vec_grid(Ctx* ctx, int64_t n) {
+  const int64_t want = ceil_div(n, kVecThreads);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->num_sms * 8));
+}
+
+static int spmv_grid(Ctx* ctx, int64_t dim) {
+  const int64_t tiles = (dim + 31) / 32;
+  const int64_t want = ceil_div(tiles, kSpmvWarps);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->num_sms * 16));
+}
+
+// ---------------------------------------------------------------- kernels
+__device__ __forceinline__ bool stopped(const int* stop, int step) {
+  if (!stop) return false;
+  const int st = *stop;
+  return st != 0 && st < step;
+}
+
+template <typename VV>
+__global__ void __launch_bounds__(kVecThreads) lz_k2_kernel(int64_t n, const int* stop, int step, VV* w,
+                                                            const VV* v1, const VV* v2, const VV* beta,
+                                                            VV* alpha, GridRed<VV> red) {
+  if (stopped(stop, step)) return;
+  const VV b = v2 ? *beta : vzero(VV{});
+  VV acc = vzero(VV{});
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    VV wi = w[i];
+    if (v2) wi = vsubmul(wi, b, v2[i]);
+    w[i] = wi;
+    acc = vdotfma(v1[i], wi, acc);
+  }
+  grid_sum(acc, red, alpha);
+}
+
+template <typename VV>
+__global__ void __launch_bounds__(kVecThreads) lz_k3_kernel(int64_t n, int* stop, int step, VV* w,
+                                                            const VV* v1, const VV* alpha, double* nrm2,
+                                                            double* nrm, GridRed<double> red) {
+  if (stopped(stop, step)) return;
+  const VV a = *alpha;
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const VV wi = vsubmul(w[i], a, v1[i]);
+    w[i] = wi;
+    acc += vnorm2(wi);
+  }
+  if (grid_sum(acc, red, nrm2) && threadIdx.x == 0) {
+    const double nr = sqrt(*nrm2);
+    *nrm = nr;
+    if (nr < 1e-10 && *stop == 0) *stop = step;  // sparse_algorithm.hpp:421
+  }
+}
+
+template <typename VV>
+__global__ void __launch_bounds__(kVecThreads) lz_k4_kernel(int64_t n, const int* stop, int step, const VV* w,
+                                                            const double* nrm, VV* vout) {
+  if (stopped(stop, step)) return;
+  const double inv = 1.0 / *nrm;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    vout[i] = vscale(inv, w[i]);
+}
+
+// ||psi||^2 of a complex column, and whether its imaginary part vanishes.
+__global__ void __launch_bounds__(kVecThreads) colnorm_kernel(int64_t n, const cplx* psi, double* nrm2,
+                                                              GridRed<double> red, int* has_imag) {
+  double acc = 0.0;
+  bool im = false;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const cplx p = psi[i];
+    acc = fma(p.re, p.re, fma(p.im, p.im, acc));
+    im |= (p.im != 0.0);
+  }
+  if (im) atomicOr(has_imag, 1);
+  grid_sum(acc, red, nrm2);
+}
+
+__device__ __forceinline__ void store_from(double& dst, cplx v) { dst = v.re; }
+__device__ __forceinline__ void store_from(cplx& dst, cplx v) { dst = v; }
+
+// v0 = psi / ||psi||  (initKrylov, sparse_algorithm.hpp:514-519)
+template <typename VV>
+__global__ void __launch_bounds__(kVecThreads) init_v0_kernel(int64_t n, const cplx* psi, const double* nrm2,
+                                                              VV* v0) {
+  const double inv = 1.0 / sqrt(*nrm2);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const cplx p = psi[i];
+    store_from(v0[i], mkc(p.re * inv, p.im * inv));
+  }
+}
+
+__device__ __forceinline__ cplx to_c(double v) { return mkc(v, 0.0); }
+__device__ __forceinline__ cplx to_c(cplx v) { return v; }
+
+// psi = sum_{k < act} y_k V[k], accumulated in k order per element.
+template <typename VV>
+__global__ void __launch_bounds__(kVecThreads) ritz_kernel(int64_t n, const VV* V, int64_t ld, const double* y,
+                                                           int act, cplx* psi) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    VV acc = vscale(y[0], V[i]);
+    for (int k = 1; k < act; ++k) acc = vfma(y[k], V[(int64_t)k * ld + i], acc);
+    psi[i] = to_c(acc);
+  }
+}
+
+// <a, b> over complex columns (a^dagger b).
+__global__ void __launch_bounds__(kVecThreads) cdot_kernel(int64_t n, const cplx* a, const cplx* b, cplx* out,
+                                                           GridRed<cplx> red) {
+  cplx acc = mkc(0.0, 0.0);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc = vdotfma(a[i], b[i], acc);
+  grid_sum(acc, red, out);
+}
+
+// ---------------------------------------------------------------- launches
+template <typename MV, typename VV>
+void launch_spmv(Ctx* ctx, const qd_ham* H, const MV* vals, const VV* x, VV* y, double scale, const VV* dotv,
+                 GridRed<VV> red, VV* dot_out, const int* stop, int step) {
+  SpmvArgs<MV, VV> A;
+  A.dim = H->dim;
+  A.rowptr = H->rowptr.p;
+  A.colidx = H->colidx.p;
+  A.vals = vals;
+  A.x = x;
+  A.y = y;
+  A.scale = scale;
+  A.dotv = dotv;
+  A.red = red;
+  A.dot_out = dot_out;
+  A.stop = stop;
+  A.step = step;
+  spmv_tile_kernel<MV, VV><<<spmv_grid(ctx, H->dim), kSpmvThreads, 0, ctx->stream>>>(A);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+}
+
+Workspace::Workspace(Ctx* c) : ctx(c) {
+  partials_d.alloc(kMaxGrid);
+  partials_c.alloc(kMaxGrid);
+  tickets.alloc(8);
+  QD_CUDA(cudaMemsetAsync(tickets.p, 0, 8 * sizeof(unsigned), c->stream));
+}
+
+GridRed<double> Workspace::red_d(int slot) { return GridRed<double>{partials_d.p, tickets.p + slot}; }
+GridRed<cplx> Workspace::red_c(int slot) { return GridRed<cplx>{partials_c.p, tickets.p + slot}; }
+
+Workspace& ham_workspace(qd_ham* H) {
+  if (!H->ws) H->ws.reset(new Workspace(H->ctx));
+  return *H->ws;
+}
+
+// y = H x on complex columns.
+void ham_apply_c(qd_ham* H, const cplx* x, cplx* y) {
+  Workspace& W = ham_workspace(H);
+  if (H->flags & QD_HAM_REAL)
+    launch_spmv<double, cplx>(H->ctx, H, H->vals_r.p, x, y, 1.0, nullptr, W.red_c(0), nullptr, nullptr, 0);
+  else
+    launch_spmv<cplx, cplx>(H->ctx, H, H->vals_c.p, x, y, 1.0, nullptr, W.red_c(0), nullptr, nullptr, 0);
+}
+
+cplx state_eval(qd_ham* H, const cplx* psi) {
+  Ctx* ctx = H->ctx;
+  Workspace& W = ham_workspace(H);
+  DBuf<cplx> tmp(H->dim + 1);
+  DBuf<cplx> out(1);
+  // psi^dagger (H psi): the product and the dot in one pass
+  if (H->flags & QD_HAM_REAL)
+    launch_spmv<double, cplx>(ctx, H, H->vals_r.p, psi, tmp.p, 1.0, psi, W.red_c(0), out.p, nullptr, 0);
+  else
+    launch_spmv<cplx, cplx>(ctx, H, H->vals_c.p, psi, tmp.p, 1.0, psi, W.red_c(0), out.p, nullptr, 0);
+  cplx h;
+  QD_CUDA(cudaMemcpyAsync(&h, out.p, sizeof(cplx), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  return h;
+}
+
+// The product the real Lanczos path launches, timed back to back.
+void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per_launch) {
+  Ctx* ctx = H->ctx;
+  Workspace& W = ham_workspace(H);
+  const int64_t n = H->dim;
+  const bool real = (H->flags & QD_HAM_REAL) != 0;
+  const size_t vb = real ? sizeof(double) : sizeof(cplx);
+  DBuf<char> x((n + 32) * vb), y((n + 32) * vb);
+  QD_CUDA(cudaMemsetAsync(x.p, 0, x.bytes(), ctx->stream));
+  auto launch = [&]() {
+    if (real)
+      launch_spmv<double, double>(ctx, H, H->vals_r.p, (const double*)x.p, (double*)y.p, 1.0, nullptr,
+                                  W.red_d(0), nullptr, nullptr, 0);
+    else
+      launch_spmv<cplx, cplx>(ctx, H, H->vals_c.p, (const cplx*)x.p, (cplx*)y.p, 1.0, nullptr, W.red_c(0),
+                              nullptr, nullptr, 0);
+  };
+  for (int i = 0; i < 3; ++i) launch();
+  QD_CUDA(cudaEventRecord(ctx->events[14], ctx->stream));
+  for (int i = 0; i < iters; ++i) launch();
+  QD_CUDA(cudaEventRecord(ctx->events[15], ctx->stream));
+  QD_CUDA(cudaEventSynchronize(ctx->events[15]));
+  float ms = 0.f;
+  QD_CUDA(cudaEventElapsedTime(&ms, ctx->events[14], ctx->events[15]));
+  *avg_ms = (double)ms / iters;
+  const double mvb = real ? 8.0 : 16.0;
+  *bytes_per_launch = (double)H->nnz * (mvb + 4.0) + (double)(n + 1) * 8.0 + (double)n * 2.0 * (double)vb;
+}
+
+// ---------------------------------------------------------------- Lanczos
+template <typename MV, typename VV>
+static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int kdim, Workspace& W) {
+  Ctx* ctx = H->ctx;
+  const int64_t n = H->dim;
+  const int vg = vec_grid(ctx, n);
+  for (int k = 1; k <= kdim; ++k) {
+    const VV* v1 = B.V.p + (int64_t)(k - 1) * B.ld;
+    const VV* v2 = (k >= 2) ? B.V.p + (int64_t)(k - 2) * B.ld : nullptr;
+    VV* vout = B.V.p + (int64_t)k * B.ld;
+    launch_spmv<MV, VV>(ctx, H, vals, v1, B.w.p, 1.0, v2, W.red_c_or_d<VV>(1), B.beta.p + k, B.stop.p, k);
+    lz_k2_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.stop.p, k, B.w.p, v1, v2, B.beta.p + k,
+                                                           B.alpha.p + k, W.red_c_or_d<VV>(2));
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+    lz_k3_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.stop.p, k, B.w.p, v1, B.alpha.p + k,
+                                                           B.nrm2.p + k, B.nrm.p + k, W.red_d(3));
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+    lz_k4_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.stop.p, k, B.w.p, B.nrm.p + k, vout);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+  }
+}
+
+template <typename VV>
+static LanczosBuffers<VV>& buffers_for(Workspace& W, int64_t n, int kdim);
+
+template <>
+LanczosBuffers<double>& buffers_for<double>(Workspace& W, int64_t n, int kdim) {
+  W.lz_d.ensure(n, kdim);
+  return W.lz_d;
+}
+template <>
+LanczosBuffers<cplx>& buffers_for<cplx>(Workspace& W, int64_t n, int kdim) {
+  W.lz_c.ensure(n, kdim);
+  return W.lz_c;
+}
+
+template <typename MV, typename VV>
+static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, const qd_lanczos_opts& o,
+                                double* evals_out, qd_lanczos_result* res) {
+  Ctx* ctx = H->ctx;
+  const int64_t n = H->dim;
+  const int kdim = o.krylov_dim;
+  Workspace& W = ham_workspace(H);
+  LanczosBuffers<VV>& B = buffers_for<VV>(W, n, kdim);
+  const MV* vals = nullptr;
+  if constexpr (std::is_same<MV, double>::value) vals = H->vals_r.p;
+  else vals = H->vals_c.p;
+  const int vg = vec_grid(ctx, n);
+  QD_CUDA(cudaMemsetAsync(B.stop.p, 0, sizeof(int), ctx->stream));
+  init_v0_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, psi, psi_nrm2, B.V.p);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+
+  B.run_graph(ctx, [&]() { lanczos_run<MV, VV>(H, vals, B, kdim, W); });
+  int matvecs = kdim;
+
+  std::vector<VV> alpha(kdim + 1);
+  std::vector<double> nrm(kdim + 1);
+  int stop = 0;
+  QD_CUDA(cudaMemcpyAsync(alpha.data(), B.alpha.p, (kdim + 1) * sizeof(VV), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(nrm.data(), B.nrm.p, (kdim + 1) * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(&stop, B.stop.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (stop) matvecs = stop;
+  const int act = stop ? stop - 1 : kdim;  // expandBasis<1> return value
+  QD_REQUIRE(act >= 1, QD_ERR_BREAKDOWN, "Lanczos broke down at the first step (start vector in an "
+             "invariant subspace of dimension 1)");
+  std::vector<double> d(act), e(act), z((size_t)act * act, 0.0);
+  for (int i = 0; i < act; ++i) {
+    d[i] = real_part(alpha[i + 1]);
+    e[i] = (i + 1 < act) ? nrm[i + 1] : 0.0;
+    z[(size_t)i * act + i] = 1.0;
+  }
+  QD_REQUIRE(tridiag_ql<double>(act, d.data(), e.data(), z.data(), act) == 0, QD_ERR_INVALID,
+             "tridiagonal eigensolver did not converge");
+  if (o.ritz == QD_RITZ_SECOND_PASS) {
+    // getState<1> regenerates v_1..v_act with the same kernels (same bits);
+    // run it for the reference's work pattern (act more products).
+    init_v0_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, psi, psi_nrm2, B.V.p);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+    QD_CUDA(cudaMemsetAsync(B.stop.p, 0, sizeof(int), ctx->stream));
+    lanczos_run<MV, VV>(H, vals, B, act, W);
+    matvecs += act;
+  }
+  QD_CUDA(cudaMemcpyAsync(B.y.p, z.data(), act * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  ritz_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, B.y.p, act, psi);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (evals_out) std::memcpy(evals_out, d.data(), act * sizeof(double));
+  res->act_dim = act;
+  res->breakdown = stop ? 1 : 0;
+  res->matvecs = matvecs;
+  res->ritz_value = d[0];
+  res->err = std::fabs(d[0]);
+}
+
+void lanczos_ground(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, double* evals_out, qd_lanczos_result* res) {
+  Ctx* ctx = H->ctx;
+  const int64_t n = H->dim;
+  QD_REQUIRE(o.krylov_dim >= 1 && o.krylov_dim <= 4096, QD_ERR_INVALID, "krylov_dim must be in 1..4096");
+  QD_REQUIRE(n >= 1, QD_ERR_INVALID, "empty sector");
+  Workspace& W = ham_workspace(H);
+  // ||psi||^2 and whether the start vector is real
+  DBuf<double> nrm2(1);
+  DBuf<int> has_im(1);
+  QD_CUDA(cudaMemsetAsync(has_im.p, 0, sizeof(int), ctx->stream));
+  colnorm_kernel<<<vec_grid(ctx, n), kVecThreads, 0, ctx->stream>>>(n, psi, nrm2.p, W.red_d(0), has_im.p);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  int him = 0;
+  double hn = 0.0;
+  QD_CUDA(cudaMemcpyAsync(&him, has_im.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(&hn, nrm2.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  QD_REQUIRE(hn > 0.0 && std::isfinite(hn), QD_ERR_INVALID, "start vector has zero or non-finite norm");
+  const bool real_h = (H->flags & QD_HAM_REAL) != 0;
+  if (real_h && !him)
+    lanczos_ground_impl<double, double>(H, psi, nrm2.p, o, evals_out, res);
+  else if (real_h)
+    lanczos_ground_impl<double, cplx>(H, psi, nrm2.p, o, evals_out, res);
+  else
+    lanczos_ground_impl<cplx, cplx>(H, psi, nrm2.p, o, evals_out, res);
+}
+
+}  // namespace qd

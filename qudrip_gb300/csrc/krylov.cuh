@@ -1,0 +1,100 @@
+// krylov.cuh -- solver workspaces (reused across calls on one Hamiltonian).
+#pragma once
+
+#include <type_traits>
+
+#include "ham.cuh"
+#include "vec.cuh"
+
+namespace qd {
+
+constexpr int kMaxGrid = 8192;  // upper bound on blocks of any reduction kernel
+
+inline double real_part(double v) { return v; }
+inline double real_part(cplx v) { return v.re; }
+
+// Device buffers of one Lanczos recurrence and its captured CUDA graph.
+template <typename VV>
+struct LanczosBuffers {
+  int64_t n = 0;
+  int kdim = 0;
+  int64_t ld = 0;  // leading dimension of the stored basis
+  DBuf<VV> V;      // (kdim + 1) x ld basis vectors
+  DBuf<VV> w;
+  DBuf<VV> alpha, beta;
+  DBuf<double> nrm, nrm2, y;
+  DBuf<int> stop;
+  cudaGraphExec_t exec = nullptr;
+  int64_t graph_kernels = 0;
+
+  void ensure(int64_t n_, int kdim_) {
+    if (n_ == n && kdim_ == kdim) return;
+    drop_graph();
+    n = n_;
+    kdim = kdim_;
+    ld = (n + 31) / 32 * 32;
+    V.alloc((size_t)(kdim + 1) * ld);
+    w.alloc(ld);
+    alpha.alloc(kdim + 2);
+    beta.alloc(kdim + 2);
+    nrm.alloc(kdim + 2);
+    nrm2.alloc(kdim + 2);
+    y.alloc(kdim + 2);
+    stop.alloc(1);
+  }
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    exec = nullptr;
+  }
+  // Capture `body` (a fixed launch sequence) once, replay it afterwards.
+  template <typename F>
+  void run_graph(Ctx* ctx, F&& body) {
+    if (!exec) {
+      cudaGraph_t g = nullptr;
+      const int64_t before = ctx->launches;
+      QD_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      try {
+        body();
+      } catch (...) {
+        cudaStreamEndCapture(ctx->stream, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      QD_CUDA(cudaStreamEndCapture(ctx->stream, &g));
+      graph_kernels = ctx->launches - before;
+      ctx->launches = before;
+      const cudaError_t e = cudaGraphInstantiate(&exec, g, 0);
+      cudaGraphDestroy(g);
+      QD_CUDA(e);
+    }
+    QD_CUDA(cudaGraphLaunch(exec, ctx->stream));
+    ctx->launches += graph_kernels;
+  }
+  ~LanczosBuffers() { drop_graph(); }
+};
+
+struct Workspace {
+  Ctx* ctx;
+  DBuf<double> partials_d;
+  DBuf<cplx> partials_c;
+  DBuf<unsigned> tickets;
+  LanczosBuffers<double> lz_d;
+  LanczosBuffers<cplx> lz_c;
+
+  explicit Workspace(Ctx* c);
+  GridRed<double> red_d(int slot);
+  GridRed<cplx> red_c(int slot);
+  template <typename VV>
+  GridRed<VV> red_c_or_d(int slot) {
+    if constexpr (std::is_same<VV, double>::value) return red_d(slot);
+    else return red_c(slot);
+  }
+};
+
+Workspace& ham_workspace(qd_ham* H);
+void ham_apply_c(qd_ham* H, const cplx* x, cplx* y);
+cplx state_eval(qd_ham* H, const cplx* psi);
+void lanczos_ground(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, double* evals_out, qd_lanczos_result* res);
+void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per_launch);
+
+}  // namespace qd

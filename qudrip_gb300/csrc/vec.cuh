@@ -1,0 +1,123 @@
+// vec.cuh -- value-type traits and deterministic grid reductions.
+//
+// Real Hamiltonians with real vectors run in `double`; everything else in
+// `cplx` (complex128).  Reductions are deterministic: every thread sums its
+// grid-stride slice in index order, blocks combine by a fixed shuffle tree,
+// and the last block to finish adds the block partials in a fixed order.
+#pragma once
+
+#include "common.cuh"
+
+namespace qd {
+
+// ---------------------------------------------------------------- scalar traits
+__device__ __forceinline__ double vzero(double) { return 0.0; }
+__device__ __forceinline__ cplx vzero(cplx) { return mkc(0.0, 0.0); }
+
+// acc + a * x
+__device__ __forceinline__ double vfma(double a, double x, double acc) { return fma(a, x, acc); }
+__device__ __forceinline__ cplx vfma(double a, cplx x, cplx acc) {
+  return mkc(fma(a, x.re, acc.re), fma(a, x.im, acc.im));
+}
+__device__ __forceinline__ cplx vfma(cplx a, cplx x, cplx acc) {
+  return mkc(fma(-a.im, x.im, fma(a.re, x.re, acc.re)), fma(a.im, x.re, fma(a.re, x.im, acc.im)));
+}
+__device__ __forceinline__ cplx vfma(cplx a, double x, cplx acc) {
+  return mkc(fma(a.re, x, acc.re), fma(a.im, x, acc.im));
+}
+
+// acc + conj(a) * b
+__device__ __forceinline__ double vdotfma(double a, double b, double acc) { return fma(a, b, acc); }
+__device__ __forceinline__ cplx vdotfma(cplx a, cplx b, cplx acc) {
+  return mkc(fma(a.im, b.im, fma(a.re, b.re, acc.re)), fma(-a.im, b.re, fma(a.re, b.im, acc.im)));
+}
+
+__device__ __forceinline__ double vadd(double a, double b) { return a + b; }
+__device__ __forceinline__ cplx vadd(cplx a, cplx b) { return mkc(a.re + b.re, a.im + b.im); }
+__device__ __forceinline__ double vscale(double s, double x) { return s * x; }
+__device__ __forceinline__ cplx vscale(double s, cplx x) { return mkc(s * x.re, s * x.im); }
+__device__ __forceinline__ double vnorm2(double x) { return x * x; }
+__device__ __forceinline__ double vnorm2(cplx x) { return fma(x.re, x.re, x.im * x.im); }
+// x - a * y
+__device__ __forceinline__ double vsubmul(double x, double a, double y) { return fma(-a, y, x); }
+__device__ __forceinline__ cplx vsubmul(cplx x, cplx a, cplx y) {
+  return mkc(fma(a.im, y.im, fma(-a.re, y.re, x.re)), fma(-a.im, y.re, fma(-a.re, y.im, x.im)));
+}
+
+__device__ __forceinline__ double shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ cplx shfl_xor(cplx v, int o) {
+  return mkc(__shfl_xor_sync(0xffffffffu, v.re, o), __shfl_xor_sync(0xffffffffu, v.im, o));
+}
+
+__device__ __forceinline__ double ld_cg(const double* p) { return __ldcg(p); }
+__device__ __forceinline__ cplx ld_cg(const cplx* p) {
+  const double2 d = __ldcg(reinterpret_cast<const double2*>(p));
+  return mkc(d.x, d.y);
+}
+
+// read-only (non-coherent) loads
+__device__ __forceinline__ double ld_ro(const double* p) { return __ldg(p); }
+__device__ __forceinline__ float ld_ro(const float* p) { return __ldg(p); }
+__device__ __forceinline__ cplx ld_ro(const cplx* p) {
+  const double2 d = __ldg(reinterpret_cast<const double2*>(p));
+  return mkc(d.x, d.y);
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = vadd(v, shfl_xor(v, o));
+  return v;
+}
+
+// Sum over the block; the result is valid in thread 0.  smem >= 32 entries.
+template <typename T>
+__device__ __forceinline__ T block_sum(T v, T* smem) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) smem[warp] = v;
+  __syncthreads();
+  T r = vzero(v);
+  if (warp == 0) {
+    r = (lane < nw) ? smem[lane] : vzero(v);
+    r = warp_sum(r);
+  }
+  return r;
+}
+
+// Grid reduction slot: per-block partials and a ticket counter (zero at rest).
+template <typename T>
+struct GridRed {
+  T* partials;
+  unsigned int* ticket;
+};
+
+// Every thread of every block calls this with its value; the last block to
+// arrive returns true in all its threads and thread 0 of it writes *total.
+template <typename T>
+__device__ __forceinline__ bool grid_sum(T v, GridRed<T> R, T* total) {
+  __shared__ T smem[32];
+  __shared__ bool last;
+  const T b = block_sum(v, smem);
+  if (threadIdx.x == 0) {
+    R.partials[blockIdx.x] = b;
+    __threadfence();
+    const unsigned t = atomicAdd(R.ticket, 1u);
+    last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  T acc = vzero(v);
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) acc = vadd(acc, ld_cg(R.partials + i));
+  const T tot = block_sum(acc, smem);
+  if (threadIdx.x == 0) {
+    *total = tot;
+    *R.ticket = 0u;
+  }
+  return true;
+}
+
+}  // namespace qd

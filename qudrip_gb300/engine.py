@@ -1,0 +1,312 @@
+"""Device objects behind QuDrip's API: sectors, lowered Hamiltonians, states, solvers.
+
+Every call goes through the C ABI (include/qudrip_gb300.h) into the CUDA
+library; nothing here computes on the CPU.  Names follow the reference:
+`Constrain` (conservation.hpp:234-239), `ham >> chain` (operator_abel.hpp:25-34),
+`getState` / `psi(t)` / `psi.eval` (state.hpp:67-102, 33-45),
+`Arnoldi.getLanczosSolver(...).getGroundState` (sparse_algorithm.hpp:564-604).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from typing import Optional
+
+import numpy as np
+
+from . import _capi as A
+from .operators import OperatorSum, Operator, QbitsIndex, SectorSpec, Constraint
+
+
+class Context:
+    """One CUDA stream on one device (qd_ctx)."""
+
+    def __init__(self, device: int = 0):
+        self.handle = C.c_void_p()
+        A.call("qd_ctx_create", device, C.byref(self.handle))
+        self.device = device
+
+    def sync(self):
+        A.call("qd_ctx_sync", self.handle)
+
+    def launches(self) -> int:
+        n = C.c_int64(0)
+        A.call("qd_ctx_launch_count", self.handle, C.byref(n))
+        return n.value
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        A.call("qd_ctx_stream", self.handle, C.byref(s))
+        return s.value or 0
+
+    def close(self):
+        if self.handle:
+            A.lib().qd_ctx_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default = None
+_default_lock = threading.Lock()
+
+
+def default_context() -> Context:
+    global _default
+    with _default_lock:
+        if _default is None:
+            _default = Context(0)
+    return _default
+
+
+class Sector(SectorSpec):
+    """Constrained sector (SubIndex) built on the device."""
+
+    def __init__(self, index: QbitsIndex, constraints, tight: int = 0, ctx: Optional[Context] = None):
+        super().__init__(index, constraints, tight)
+        self.ctx = ctx or default_context()
+        arr, n = self.constraint_array()
+        self.handle = C.c_void_p()
+        A.call("qd_sector_create", self.ctx.handle, self.nbits, arr, n, self.tight, C.byref(self.handle))
+        d = C.c_int64(0)
+        A.call("qd_sector_dim", self.handle, C.byref(d))
+        self.dim = d.value
+
+    def range(self) -> int:
+        return self.dim
+
+    def rank_kind(self) -> int:
+        k = C.c_int(0)
+        A.call("qd_sector_rank_kind", self.handle, C.byref(k))
+        return k.value
+
+    def basis(self) -> np.ndarray:
+        out = np.empty(self.dim, dtype=np.uint64)
+        A.call("qd_sector_basis", self.handle, out.ctypes.data_as(C.POINTER(C.c_uint64)))
+        return out
+
+    def rank(self, states) -> np.ndarray:
+        s = np.ascontiguousarray(states, dtype=np.uint64)
+        r = np.empty(len(s), dtype=np.int64)
+        A.call("qd_sector_rank", self.handle, s.ctypes.data_as(C.POINTER(C.c_uint64)), len(s),
+               r.ctypes.data_as(C.POINTER(C.c_int64)))
+        return r
+
+    def lower(self, opsum) -> "Hamiltonian":
+        if isinstance(opsum, Operator):
+            opsum = OperatorSum([(opsum, 1.0 + 0j)])
+        return Hamiltonian(self, opsum)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            A.lib().qd_sector_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def Constrain(index: QbitsIndex, *constraints: Constraint, ctx: Optional[Context] = None) -> Sector:
+    return Sector(index, constraints, 0, ctx)
+
+
+def LooseConstrain(index: QbitsIndex, tight: int, *constraints: Constraint,
+                   ctx: Optional[Context] = None) -> Sector:
+    return Sector(index, constraints, tight, ctx)
+
+
+class Hamiltonian:
+    """A lowered OperatorSum (qd_ham): CSR on the device, reference CSC on demand."""
+
+    def __init__(self, sector: Sector, opsum: OperatorSum):
+        self.sector = sector
+        self.ctx = sector.ctx
+        terms, nt, gates, ng = opsum.pack()
+        self.handle = C.c_void_p()
+        A.call("qd_ham_lower", sector.handle, terms, nt, gates, ng, C.byref(self.handle))
+        info = A.qd_ham_info()
+        A.call("qd_ham_get_info", self.handle, C.byref(info))
+        self.dim = info.dim
+        self.nnz = info.nnz
+        self.flags = info.flags
+        self.max_row_nnz = info.max_row_nnz
+
+    @property
+    def is_real(self) -> bool:
+        return bool(self.flags & A.QD_HAM_REAL)
+
+    @property
+    def is_hermitian(self) -> bool:
+        return bool(self.flags & A.QD_HAM_HERMITIAN)
+
+    def rows(self) -> int:
+        return self.dim
+
+    def cols(self) -> int:
+        return self.dim
+
+    def _download(self, name):
+        ptr = np.empty(self.dim + 1, dtype=np.int64)
+        idx = np.empty(max(self.nnz, 1), dtype=np.int32)
+        vals = np.empty(max(self.nnz, 1), dtype=np.complex128)
+        A.call(name, self.handle, ptr.ctypes.data_as(C.POINTER(C.c_int64)),
+               idx.ctypes.data_as(C.POINTER(C.c_int32)), vals.ctypes.data_as(C.POINTER(C.c_double)))
+        return ptr, idx[:self.nnz], vals[:self.nnz]
+
+    def csr(self):
+        return self._download("qd_ham_download_csr")
+
+    def csc(self):
+        return self._download("qd_ham_download_csc")
+
+    def scipy(self):
+        import scipy.sparse as sp
+        ptr, idx, vals = self.csr()
+        return sp.csr_matrix((vals, idx, ptr), shape=(self.dim, self.dim))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            A.lib().qd_ham_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class State:
+    """getState(index, nt): nt complex128 columns on the device (state.hpp:9-104)."""
+
+    def __init__(self, sector: Sector, nt: int):
+        self.sector = sector
+        self.ctx = sector.ctx
+        self.dim = sector.dim
+        self._nt = nt
+        self.t = 0
+        self.handle = C.c_void_p()
+        A.call("qd_state_create", self.ctx.handle, self.dim, nt, C.byref(self.handle))
+
+    def nt(self) -> int:
+        return self._nt
+
+    def ndim(self) -> int:
+        return self.dim
+
+    def __call__(self, t: int) -> "State":  # psi(t) selects the column, returns the state
+        if not 0 <= t < self._nt:
+            raise IndexError("time slot out of range")
+        self.t = t
+        return self
+
+    def set(self, t: int, values) -> None:
+        v = np.ascontiguousarray(np.asarray(values, dtype=np.complex128))
+        if v.shape != (self.dim,):
+            raise ValueError("state column has the wrong length")
+        A.call("qd_state_upload", self.handle, t, v.ctypes.data_as(C.POINTER(C.c_double)))
+
+    def get(self, t: Optional[int] = None) -> np.ndarray:
+        t = self.t if t is None else t
+        out = np.empty(self.dim, dtype=np.complex128)
+        A.call("qd_state_download", self.handle, t, out.ctypes.data_as(C.POINTER(C.c_double)))
+        return out
+
+    def mat(self) -> np.ndarray:
+        return self.get(self.t)
+
+    def device_ptr(self, t: int) -> int:
+        p = C.c_void_p()
+        A.call("qd_state_device_ptr", self.handle, t, C.byref(p))
+        return p.value
+
+    def eval(self, t: int, ham: Hamiltonian) -> complex:
+        out = (C.c_double * 2)()
+        A.call("qd_state_eval", self.handle, t, ham.handle, out)
+        return complex(out[0], out[1])
+
+    def close(self):
+        if getattr(self, "handle", None):
+            A.lib().qd_state_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def getState(index: Sector, nt: int) -> State:
+    return State(index, nt)
+
+
+def apply(ham: Hamiltonian, x: State, t_in: int, y: State, t_out: int) -> None:
+    A.call("qd_ham_apply", ham.handle, x.handle, t_in, y.handle, t_out)
+
+
+def start_vector(dim: int, seed: int) -> np.ndarray:
+    """Seeded i.i.d. uniform[-1, 1] real start vector (the harness's shuffle_state)."""
+    return np.random.Generator(np.random.PCG64(seed)).uniform(-1.0, 1.0, dim)
+
+
+def shuffle_state(psi: State, seed: int = 12345) -> None:
+    v = start_vector(psi.dim, seed)
+    v = v / np.sqrt(np.dot(v, v))
+    psi.set(psi.t, v.astype(np.complex128))
+
+
+class LanczosSolver:
+    """Arnoldi::getLanczosSolver(index, kry_dim) -- ArnoldiSolver<T, herm=1>."""
+
+    def __init__(self, index: Sector, kry_dim: int, spmv: int = A.QD_SPMV_CSR,
+                 ritz: int = A.QD_RITZ_STORED_BASIS):
+        self.index = index
+        self.kry_dim = kry_dim
+        self.spmv = spmv
+        self.ritz = ritz
+        self._evals = np.empty(0)
+        self._act = 0
+        self._err = 0.0
+        self.result = None
+
+    def getGroundState(self, H: Hamiltonian, psi: State, tstp: int, add_dim: int = -1):
+        if add_dim != -1:
+            raise NotImplementedError("incremental add_dim restarts are not supported")
+        opts = A.qd_lanczos_opts(self.kry_dim, self.spmv, self.ritz, 0)
+        evals = np.empty(self.kry_dim, dtype=np.float64)
+        res = A.qd_lanczos_result()
+        A.call("qd_lanczos_ground", H.handle, psi.handle, tstp, C.byref(opts),
+               evals.ctypes.data_as(C.POINTER(C.c_double)), C.byref(res))
+        self._act = res.act_dim
+        self._evals = evals[:res.act_dim].copy()
+        self._err = res.err
+        self.result = res
+        return res
+
+    def act_dim(self) -> int:
+        return self._act
+
+    def error(self) -> float:
+        return self._err
+
+    def eigenvalues(self) -> np.ndarray:
+        return self._evals
+
+    def storeE(self, fname: str) -> None:
+        with open(fname, "w") as f:
+            for e in self._evals:
+                f.write(f"{e:.6g}\n")
+
+
+class Arnoldi:
+    @staticmethod
+    def getLanczosSolver(index: Sector, kry_dim: int, **kw) -> LanczosSolver:
+        return LanczosSolver(index, kry_dim, **kw)
