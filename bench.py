@@ -330,6 +330,27 @@ def gpu_arm(args, rank, world, local):
     return 0
 
 
+def spmv_only(args, local):
+    """Time CSR product kernels alone on the L=24 matrix (also the ncu target)."""
+    import qudrip_gb300 as q
+    from qudrip_gb300 import _capi as A
+    from qudrip_gb300 import chains
+    ctx = q.Context(local)
+    spec, ham = chains.xxz_chain(L)
+    sec = q.Sector(spec.index, spec.constraints, ctx=ctx)
+    H = sec.lower(ham)
+    kernels = sorted(A.SPMV_KERNELS) if args.spmv_only == 1 else [args.spmv_only]
+    hbm_peak, _ = peaks()
+    for k in kernels:
+        ms = C.c_double(0)
+        nb = C.c_double(0)
+        A.call("qd_ham_time_spmv", H.handle, k, args.iters, C.byref(ms), C.byref(nb))
+        gbs = nb.value / (ms.value * 1e-3) / 1e9
+        print(json.dumps({"kernel": A.SPMV_KERNELS[k], "id": k, "ms": ms.value, "GBps": gbs,
+                          "frac": gbs / hbm_peak, "matvecs_per_s": 1e3 / ms.value}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -337,10 +358,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--spmv-only", type=int, default=0, metavar="KERNEL",
+                    help="only time CSR product kernel KERNEL (100..105; 1 = all) on the L=24 matrix")
+    ap.add_argument("--iters", type=int, default=50)
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
         return reference_arm(args, rank, world)
+    if args.spmv_only:
+        return spmv_only(args, local)
     return gpu_arm(args, rank, world, local)
 
 

@@ -232,6 +232,14 @@ qd_status qd_lanczos_ground(qd_ham *ham, qd_state *psi, int t,
 qd_status qd_ham_time_spmv(qd_ham *ham, int spmv, int iters, double *avg_ms,
                            double *bytes_per_launch);
 
+/* CSR product kernels: 100 warp tile (lane per row), 101 balanced warp tile
+ * (equal nnz per lane), 102/103/104 two/four/eight lanes per row, 105 thread
+ * per row.  All give the same products up to summation order. */
+qd_status qd_ham_set_spmv_kernel(qd_ham *ham, int kernel);
+/* Time every product kernel on this Hamiltonian and keep the fastest for the
+ * solvers (the autotuner); returns the choice and its average ms. */
+qd_status qd_ham_autotune(qd_ham *ham, int iters, int *chosen, double *best_ms);
+
 #ifdef __cplusplus
 }
 #endif

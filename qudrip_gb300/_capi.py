@@ -36,6 +36,8 @@ QD_SPMV_CSR = 0
 QD_SPMV_MATRIX_FREE = 1
 QD_RITZ_STORED_BASIS = 0
 QD_RITZ_SECOND_PASS = 1
+SPMV_KERNELS = {100: "tile", 101: "balanced", 102: "vector2", 103: "vector4", 104: "vector8",
+                105: "scalar"}
 
 
 class qd_cq_term(C.Structure):
@@ -97,6 +99,8 @@ _SIGNATURES = {
     "qd_host_alloc": [C.c_int64, _PP],
     "qd_host_free": [_P],
     "qd_ham_time_spmv": [_P, C.c_int, C.c_int, _DP, _DP],
+    "qd_ham_set_spmv_kernel": [_P, C.c_int],
+    "qd_ham_autotune": [_P, C.c_int, C.POINTER(C.c_int), _DP],
     "qd_status_string": [C.c_int],
     "qd_last_error": [],
     "qd_api_version": [],

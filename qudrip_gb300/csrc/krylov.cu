@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kVecThreads) cdot_kernel(int64_t n, const cplx
 // ---------------------------------------------------------------- launches
 template <typename MV, typename VV>
 void launch_spmv(Ctx* ctx, const qd_ham* H, const MV* vals, const VV* x, VV* y, double scale, const VV* dotv,
-                 GridRed<VV> red, VV* dot_out, const int* stop, int step) {
+                 GridRed<VV> red, VV* dot_out, const int* stop, int step, int variant) {
   SpmvArgs<MV, VV> A;
   A.dim = H->dim;
   A.rowptr = H->rowptr.p;
@@ -156,7 +156,28 @@ void launch_spmv(Ctx* ctx, const qd_ham* H, const MV* vals, const VV* x, VV* y, 
   A.dot_out = dot_out;
   A.stop = stop;
   A.step = step;
-  spmv_tile_kernel<MV, VV><<<spmv_grid(ctx, H->dim), kSpmvThreads, 0, ctx->stream>>>(A);
+  if (variant < 0) variant = H->spmv_variant;
+  const int64_t vg = std::max<int64_t>(1, std::min<int64_t>(ceil_div(H->dim, 256 / 4), (int64_t)ctx->num_sms * 8));
+  switch (variant) {
+    case kSpmvTile:
+      spmv_tile_kernel<MV, VV><<<spmv_grid(ctx, H->dim), kSpmvThreads, 0, ctx->stream>>>(A);
+      break;
+    case kSpmvBalanced:
+      spmv_balanced_kernel<MV, VV><<<spmv_grid(ctx, H->dim), kSpmvThreads, 0, ctx->stream>>>(A);
+      break;
+    case kSpmvVector2:
+      spmv_vector_kernel<MV, VV, 2><<<(unsigned)vg, 256, 0, ctx->stream>>>(A);
+      break;
+    case kSpmvVector4:
+      spmv_vector_kernel<MV, VV, 4><<<(unsigned)vg, 256, 0, ctx->stream>>>(A);
+      break;
+    case kSpmvVector8:
+      spmv_vector_kernel<MV, VV, 8><<<(unsigned)vg, 256, 0, ctx->stream>>>(A);
+      break;
+    default:
+      spmv_vector_kernel<MV, VV, 1><<<(unsigned)vg, 256, 0, ctx->stream>>>(A);
+      break;
+  }
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
 }
@@ -180,9 +201,9 @@ Workspace& ham_workspace(qd_ham* H) {
 void ham_apply_c(qd_ham* H, const cplx* x, cplx* y) {
   Workspace& W = ham_workspace(H);
   if (H->flags & QD_HAM_REAL)
-    launch_spmv<double, cplx>(H->ctx, H, H->vals_r.p, x, y, 1.0, nullptr, W.red_c(0), nullptr, nullptr, 0);
+    launch_spmv<double, cplx>(H->ctx, H, H->vals_r.p, x, y, 1.0, nullptr, W.red_c(0), nullptr, nullptr, 0, -1);
   else
-    launch_spmv<cplx, cplx>(H->ctx, H, H->vals_c.p, x, y, 1.0, nullptr, W.red_c(0), nullptr, nullptr, 0);
+    launch_spmv<cplx, cplx>(H->ctx, H, H->vals_c.p, x, y, 1.0, nullptr, W.red_c(0), nullptr, nullptr, 0, -1);
 }
 
 cplx state_eval(qd_ham* H, const cplx* psi) {
@@ -192,9 +213,9 @@ cplx state_eval(qd_ham* H, const cplx* psi) {
   DBuf<cplx> out(1);
   // psi^dagger (H psi): the product and the dot in one pass
   if (H->flags & QD_HAM_REAL)
-    launch_spmv<double, cplx>(ctx, H, H->vals_r.p, psi, tmp.p, 1.0, psi, W.red_c(0), out.p, nullptr, 0);
+    launch_spmv<double, cplx>(ctx, H, H->vals_r.p, psi, tmp.p, 1.0, psi, W.red_c(0), out.p, nullptr, 0, -1);
   else
-    launch_spmv<cplx, cplx>(ctx, H, H->vals_c.p, psi, tmp.p, 1.0, psi, W.red_c(0), out.p, nullptr, 0);
+    launch_spmv<cplx, cplx>(ctx, H, H->vals_c.p, psi, tmp.p, 1.0, psi, W.red_c(0), out.p, nullptr, 0, -1);
   cplx h;
   QD_CUDA(cudaMemcpyAsync(&h, out.p, sizeof(cplx), cudaMemcpyDeviceToHost, ctx->stream));
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -210,13 +231,14 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   const size_t vb = real ? sizeof(double) : sizeof(cplx);
   DBuf<char> x((n + 32) * vb), y((n + 32) * vb);
   QD_CUDA(cudaMemsetAsync(x.p, 0, x.bytes(), ctx->stream));
+  const int variant = (spmv >= kSpmvTile) ? spmv : -1;
   auto launch = [&]() {
     if (real)
       launch_spmv<double, double>(ctx, H, H->vals_r.p, (const double*)x.p, (double*)y.p, 1.0, nullptr,
-                                  W.red_d(0), nullptr, nullptr, 0);
+                                  W.red_d(0), nullptr, nullptr, 0, variant);
     else
       launch_spmv<cplx, cplx>(ctx, H, H->vals_c.p, (const cplx*)x.p, (cplx*)y.p, 1.0, nullptr, W.red_c(0),
-                              nullptr, nullptr, 0);
+                              nullptr, nullptr, 0, variant);
   };
   for (int i = 0; i < 3; ++i) launch();
   QD_CUDA(cudaEventRecord(ctx->events[14], ctx->stream));
@@ -240,7 +262,7 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int kd
     const VV* v1 = B.V.p + (int64_t)(k - 1) * B.ld;
     const VV* v2 = (k >= 2) ? B.V.p + (int64_t)(k - 2) * B.ld : nullptr;
     VV* vout = B.V.p + (int64_t)k * B.ld;
-    launch_spmv<MV, VV>(ctx, H, vals, v1, B.w.p, 1.0, v2, W.red_c_or_d<VV>(1), B.beta.p + k, B.stop.p, k);
+    launch_spmv<MV, VV>(ctx, H, vals, v1, B.w.p, 1.0, v2, W.red_c_or_d<VV>(1), B.beta.p + k, B.stop.p, k, -1);
     lz_k2_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.stop.p, k, B.w.p, v1, v2, B.beta.p + k,
                                                            B.alpha.p + k, W.red_c_or_d<VV>(2));
     QD_CHECK_LAUNCH();

@@ -10,6 +10,16 @@ namespace qd {
 
 constexpr int kMaxGrid = 8192;  // upper bound on blocks of any reduction kernel
 
+// CSR product kernels (qd_ham::spmv_variant; qd_ham_time_spmv accepts them as `spmv`)
+enum SpmvVariant {
+  kSpmvTile = 100,      // warp tile, lane per row, staged in shared memory
+  kSpmvBalanced = 101,  // warp tile, equal nnz per lane
+  kSpmvVector2 = 102,   // 2 lanes per row
+  kSpmvVector4 = 103,
+  kSpmvVector8 = 104,
+  kSpmvScalar = 105,    // thread per row
+};
+
 inline double real_part(double v) { return v; }
 inline double real_part(cplx v) { return v.re; }
 

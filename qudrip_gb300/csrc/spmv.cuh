@@ -87,3 +87,173 @@ __global__ void __launch_bounds__(kSpmvThreads) spmv_tile_kernel(SpmvArgs<MV, VV
 }
 
 }  // namespace qd
+
+namespace qd {
+
+// ---------------------------------------------------------------------------
+// Balanced warp tile: the tile's nnz are split into 32 equal contiguous
+// chunks (one per lane, an odd chunk length so shared-memory reads are free
+// of bank conflicts), so every lane issues the same number of FMAs whatever
+// the row lengths.  Rows cut by a chunk boundary are finished by the lane
+// that holds their first entry, adding the later pieces in lane order.
+// Staging uses 16-byte vector loads from the (padded) CSR arrays.
+template <typename MV, typename VV>
+__global__ void __launch_bounds__(kSpmvThreads) spmv_balanced_kernel(SpmvArgs<MV, VV> A) {
+  constexpr int kVecV = 16 / (int)sizeof(MV);  // values per 16-byte load
+  constexpr int kSpan = ((40 * 1024) / (kSpmvWarps * (int)(sizeof(int32_t) + sizeof(MV))) - 8) / 16 * 16;
+  __shared__ __align__(16) int32_t s_col[kSpmvWarps][kSpan + 8];
+  __shared__ __align__(16) MV s_val[kSpmvWarps][kSpan + 8];
+  __shared__ int s_rp[kSpmvWarps][33];
+  __shared__ VV s_head[kSpmvWarps][32];
+  __shared__ int s_headrow[kSpmvWarps][32];
+  __shared__ VV s_y[kSpmvWarps][32];
+  if (A.stop) {
+    const int st = *A.stop;
+    if (st != 0 && st < A.step) return;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t ntiles = (A.dim + 31) >> 5;
+  const int64_t nw = (int64_t)gridDim.x * kSpmvWarps;
+  VV dotacc = vzero(VV{});
+  int* rp = s_rp[warp];
+  for (int64_t tile = (int64_t)blockIdx.x * kSpmvWarps + warp; tile < ntiles; tile += nw) {
+    const int64_t r0 = tile << 5;
+    const int nrows = (int)min((int64_t)32, A.dim - r0);
+    const int64_t kb = A.rowptr[r0];
+    if (lane < nrows) rp[lane] = (int)(A.rowptr[r0 + lane] - kb);
+    if (lane == 0) rp[nrows] = (int)(A.rowptr[r0 + nrows] - kb);
+    s_y[warp][lane] = vzero(VV{});
+    s_headrow[warp][lane] = -1;
+    __syncwarp();
+    const int span = rp[nrows];
+    if (span > kSpan) {
+      // long rows: lane per row straight from global memory
+      if (lane < nrows) {
+        VV acc = vzero(VV{});
+        for (int64_t k = kb + rp[lane]; k < kb + rp[lane + 1]; ++k)
+          acc = vfma(A.vals[k], ld_ro(A.x + A.colidx[k]), acc);
+        s_y[warp][lane] = acc;
+      }
+    } else {
+      // stage with 16-byte loads from aligned starts
+      const int64_t kv = kb & ~(int64_t)(kVecV - 1);
+      const int offv = (int)(kb - kv);
+      const int nv = (offv + span + kVecV - 1) / kVecV;
+      const int4* gv = reinterpret_cast<const int4*>(A.vals + kv);
+      int4* sv = reinterpret_cast<int4*>(s_val[warp]);
+      for (int i = lane; i < nv; i += 32) sv[i] = __ldg(gv + i);
+      const int64_t kc = kb & ~(int64_t)3;
+      const int offc = (int)(kb - kc);
+      const int nc = (offc + span + 3) / 4;
+      const int4* gc = reinterpret_cast<const int4*>(A.colidx + kc);
+      int4* sc = reinterpret_cast<int4*>(s_col[warp]);
+      for (int i = lane; i < nc; i += 32) sc[i] = __ldg(gc + i);
+      __syncwarp();
+      int q = (span + 31) >> 5;
+      q |= 1;
+      const int a = min(lane * q, span), b = min(a + q, span);
+      if (a < b) {
+        // row containing entry a: last j with rp[j] <= a
+        int lo = 0, hi = nrows - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (rp[mid] <= a) lo = mid;
+          else hi = mid - 1;
+        }
+        int j = lo;
+        int next = rp[j + 1];
+        const bool head_cont = rp[j] < a;  // row j began in an earlier lane
+        bool first = true;
+        VV acc = vzero(VV{});
+        const MV* sval = s_val[warp] + offv;
+        const int32_t* scol = s_col[warp] + offc;
+        for (int k = a; k < b; ++k) {
+          while (k == next) {  // row j ends before k
+            if (first && head_cont) {
+              s_head[warp][lane] = acc;
+              s_headrow[warp][lane] = j;
+            } else {
+              s_y[warp][j] = acc;  // complete inside this lane
+            }
+            first = false;
+            acc = vzero(VV{});
+            ++j;
+            next = rp[j + 1];
+          }
+          acc = vfma(sval[k], ld_ro(A.x + scol[k]), acc);
+        }
+        // last row touched: complete, a head piece, or continues into later lanes
+        if (first && head_cont) {
+          s_head[warp][lane] = acc;
+          s_headrow[warp][lane] = j;
+        } else if (next <= b) {
+          s_y[warp][j] = acc;
+        } else {
+          // this lane owns row j, which continues past b: keep the piece
+          s_y[warp][j] = acc;
+        }
+      }
+      __syncwarp();
+      // owners of rows cut at their chunk end add the later pieces in lane order
+      if (a < b) {
+        int lo = 0, hi = nrows - 1;
+        const int last = b - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (rp[mid] <= last) lo = mid;
+          else hi = mid - 1;
+        }
+        const int j = lo;
+        if (rp[j] >= a && rp[j + 1] > b) {
+          VV acc = s_y[warp][j];
+          for (int l = lane + 1; l < 32 && s_headrow[warp][l] == j; ++l) acc = vadd(acc, s_head[warp][l]);
+          s_y[warp][j] = acc;
+        }
+      }
+    }
+    __syncwarp();
+    if (lane < nrows) {
+      const int64_t r = r0 + lane;
+      const VV yv = vscale(A.scale, s_y[warp][lane]);
+      A.y[r] = yv;
+      if (A.dotv) dotacc = vdotfma(A.dotv[r], yv, dotacc);
+    }
+    __syncwarp();
+  }
+  if (A.dotv) grid_sum(dotacc, A.red, A.dot_out);
+}
+
+// ---------------------------------------------------------------------------
+// G lanes per row ("vector CSR"): each group strides its row, then a
+// shuffle reduction.
+template <typename MV, typename VV, int G>
+__global__ void __launch_bounds__(256) spmv_vector_kernel(SpmvArgs<MV, VV> A) {
+  if (A.stop) {
+    const int st = *A.stop;
+    if (st != 0 && st < A.step) return;
+  }
+  const int64_t gt = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int sub = threadIdx.x & (G - 1);
+  const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;
+  VV dotacc = vzero(VV{});
+  // every thread iterates the same number of times so the shuffles stay converged
+  const int64_t iters = (A.dim + ngroups - 1) / ngroups;
+  for (int64_t it = 0; it < iters; ++it) {
+    const int64_t r = gt / G + it * ngroups;
+    VV acc = vzero(VV{});
+    if (r < A.dim) {
+      const int64_t e = A.rowptr[r + 1];
+      for (int64_t k = A.rowptr[r] + sub; k < e; k += G) acc = vfma(A.vals[k], ld_ro(A.x + A.colidx[k]), acc);
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) acc = vadd(acc, shfl_xor(acc, o));
+    if (r < A.dim && sub == 0) {
+      const VV yv = vscale(A.scale, acc);
+      A.y[r] = yv;
+      if (A.dotv) dotacc = vdotfma(A.dotv[r], yv, dotacc);
+    }
+  }
+  if (A.dotv) grid_sum(dotacc, A.red, A.dot_out);
+}
+
+}  // namespace qd

@@ -172,8 +172,14 @@ def test_lanczos_xy16_config1(ctx, golden):
     check_energies(oh, ores, solver, res, gpsi, E)
     exact = golden["xy_open_closed_form"]["16"]
     assert abs(res.ritz_value - exact) <= 1e-12 * abs(exact)
+    # without reorthogonalisation copies ("ghosts") of the converged ground
+    # level appear at rounding-dependent positions; the first genuinely
+    # excited level is converged and must agree
     ev = solver.eigenvalues()
-    assert np.allclose(ev[:3], ores["evals"][:3], rtol=0, atol=1e-9)
+    lam0 = ev[0]
+    first = ev[ev > lam0 + 1e-3][0]
+    ofirst = ores["evals"][ores["evals"] > lam0 + 1e-3][0]
+    assert abs(first - ofirst) <= 1e-9
 
 
 def test_lanczos_complex_hamiltonian(ctx):
@@ -228,3 +234,44 @@ def test_xxz_L24_config2_full_size(ctx, golden):
     g = psi.get(0)
     rq = psi.eval(0, gh).real / np.vdot(g, g).real
     assert abs(rq - e0) <= E_TOL * abs(e0)
+
+
+def all_to_all_hopping(L):
+    """Long rows (every pair hops): exercises the long-row fallbacks of the tile kernels."""
+    pre = getQbits(L)
+    spec = SectorSpec(pre, [getNset(pre) == L // 2])
+    gc = q.getBoseGate(pre)
+    ga = q.getBoseGate(pre)
+    gc << 0.5 * (pauli_x + II * pauli_y)
+    ga << 0.5 * (pauli_x - II * pauli_y)
+    ham = getEmptyOperator()
+    for i in range(L):
+        for j in range(L):
+            if i != j:
+                ham = ham + (0.1 * (i + 1) + 0.01 * j) * (gc(i) * ga(j))
+    return spec, ham
+
+
+@pytest.mark.parametrize("name", ["xxz14_fields", "fermi_complex10", "all_to_all12"])
+def test_every_product_kernel(ctx, name):
+    import ctypes as C
+    from qudrip_gb300 import _capi as A
+    spec, ham = all_to_all_hopping(12) if name == "all_to_all12" else SYSTEMS[name]()
+    oh = O.Ham(O.Sector(spec), ham)
+    gsec, gh = gpu_objects(spec, ham)
+    rng = np.random.default_rng(2)
+    x = rng.normal(size=gh.dim) + 1j * rng.normal(size=gh.dim)
+    yo = oh.apply(x)
+    st = q.getState(gsec, 2)
+    st.set(0, x)
+    for kern in sorted(A.SPMV_KERNELS):
+        A.call("qd_ham_set_spmv_kernel", gh.handle, kern)
+        q.apply(gh, st, 0, st, 1)
+        y = st.get(1)
+        assert np.abs(y - yo).max() <= 1e-13 * np.abs(yo).max(), A.SPMV_KERNELS[kern]
+        e = st.eval(0, gh)
+        assert abs(e - oh.eval(x)) <= 1e-12 * abs(e)
+    chosen = C.c_int(0)
+    ms = C.c_double(0)
+    A.call("qd_ham_autotune", gh.handle, 3, C.byref(chosen), C.byref(ms))
+    assert chosen.value in A.SPMV_KERNELS and ms.value > 0
