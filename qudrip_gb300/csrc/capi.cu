@@ -418,7 +418,7 @@ qd_status qd_lanczos_ground(qd_ham* ham, qd_state* psi, int t, const qd_lanczos_
 qd_status qd_ham_time_spmv(qd_ham* ham, int spmv, int iters, double* avg_ms, double* bytes_per_launch) {
   return guard([&] {
     QD_REQUIRE(ham && avg_ms && bytes_per_launch && iters >= 1, QD_ERR_INVALID, "bad argument");
-    QD_REQUIRE(spmv == QD_SPMV_CSR || (spmv >= kSpmvTile && spmv <= kSpmvScalar), QD_ERR_UNSUPPORTED,
+    QD_REQUIRE(spmv == QD_SPMV_CSR || (spmv >= kSpmvTile && spmv <= kSpmvLast), QD_ERR_UNSUPPORTED,
                "qd_ham_time_spmv: unknown product kernel %d", spmv);
     DeviceGuard dg(ham->ctx->device);
     time_spmv(ham, spmv, iters, avg_ms, bytes_per_launch);
@@ -427,7 +427,7 @@ qd_status qd_ham_time_spmv(qd_ham* ham, int spmv, int iters, double* avg_ms, dou
 
 qd_status qd_ham_set_spmv_kernel(qd_ham* ham, int kernel) {
   return guard([&] {
-    QD_REQUIRE(ham && kernel >= kSpmvTile && kernel <= kSpmvScalar, QD_ERR_INVALID, "unknown product kernel");
+    QD_REQUIRE(ham && kernel >= kSpmvTile && kernel <= kSpmvLast, QD_ERR_INVALID, "unknown product kernel");
     ham->spmv_variant = kernel;
   });
 }
@@ -438,7 +438,7 @@ qd_status qd_ham_autotune(qd_ham* ham, int iters, int* chosen, double* best_ms) 
     DeviceGuard dg(ham->ctx->device);
     double best = 1e300, bytes = 0;
     int pick = ham->spmv_variant;
-    for (int v = kSpmvTile; v <= kSpmvScalar; ++v) {
+    for (int v = kSpmvTile; v <= kSpmvLast; ++v) {
       double ms = 0;
       time_spmv(ham, v, iters, &ms, &bytes);
       if (ms < best) {

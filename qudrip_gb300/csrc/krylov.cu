@@ -174,6 +174,18 @@ void launch_spmv(Ctx* ctx, const qd_ham* H, const MV* vals, const VV* x, VV* y, 
     case kSpmvVector8:
       spmv_vector_kernel<MV, VV, 8><<<(unsigned)vg, 256, 0, ctx->stream>>>(A);
       break;
+    case kSpmvRow4:
+      spmv_rowunroll_kernel<MV, VV, 4, false><<<(unsigned)ceil_div(H->dim, 256), 256, 0, ctx->stream>>>(A);
+      break;
+    case kSpmvRow8:
+      spmv_rowunroll_kernel<MV, VV, 8, false><<<(unsigned)ceil_div(H->dim, 256), 256, 0, ctx->stream>>>(A);
+      break;
+    case kSpmvRow4Stream:
+      spmv_rowunroll_kernel<MV, VV, 4, true><<<(unsigned)ceil_div(H->dim, 256), 256, 0, ctx->stream>>>(A);
+      break;
+    case kSpmvRow8Stream:
+      spmv_rowunroll_kernel<MV, VV, 8, true><<<(unsigned)ceil_div(H->dim, 256), 256, 0, ctx->stream>>>(A);
+      break;
     default:
       spmv_vector_kernel<MV, VV, 1><<<(unsigned)vg, 256, 0, ctx->stream>>>(A);
       break;

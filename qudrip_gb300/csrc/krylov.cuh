@@ -18,6 +18,11 @@ enum SpmvVariant {
   kSpmvVector4 = 103,
   kSpmvVector8 = 104,
   kSpmvScalar = 105,    // thread per row
+  kSpmvRow4 = 106,      // thread per row, 4 loads in flight
+  kSpmvRow8 = 107,      // thread per row, 8 loads in flight
+  kSpmvRow4Stream = 108,  // as 106 with evict-first matrix loads
+  kSpmvRow8Stream = 109,  // as 107 with evict-first matrix loads
+  kSpmvLast = 109,
 };
 
 inline double real_part(double v) { return v; }

@@ -257,3 +257,58 @@ __global__ void __launch_bounds__(256) spmv_vector_kernel(SpmvArgs<MV, VV> A) {
 }
 
 }  // namespace qd
+
+namespace qd {
+
+__device__ __forceinline__ double ld_stream(const double* p) { return __ldcs(p); }
+__device__ __forceinline__ float ld_stream(const float* p) { return __ldcs(p); }
+__device__ __forceinline__ int32_t ld_stream(const int32_t* p) { return __ldcs(p); }
+__device__ __forceinline__ cplx ld_stream(const cplx* p) {
+  const double2 d = __ldcs(reinterpret_cast<const double2*>(p));
+  return mkc(d.x, d.y);
+}
+__device__ __forceinline__ double ld_plain(const double* p) { return __ldg(p); }
+__device__ __forceinline__ float ld_plain(const float* p) { return __ldg(p); }
+__device__ __forceinline__ int32_t ld_plain(const int32_t* p) { return __ldg(p); }
+__device__ __forceinline__ cplx ld_plain(const cplx* p) { return ld_ro(p); }
+
+// Thread per row with U independent (column, value, x) loads in flight per
+// iteration; FMAs stay in column order.  STREAM marks the matrix loads
+// evict-first so the gathered vector keeps its place in L1/L2.
+template <typename MV, typename VV, int U, bool STREAM>
+__global__ void __launch_bounds__(256) spmv_rowunroll_kernel(SpmvArgs<MV, VV> A) {
+  if (A.stop) {
+    const int st = *A.stop;
+    if (st != 0 && st < A.step) return;
+  }
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  VV yv = vzero(VV{});
+  if (r < A.dim) {
+    const int64_t b = A.rowptr[r], e = A.rowptr[r + 1];
+    VV acc = vzero(VV{});
+    for (int64_t k = b; k < e; k += U) {
+      int32_t c[U];
+      MV v[U];
+      VV xv[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const bool ok = k + u < e;
+        c[u] = ok ? (STREAM ? ld_stream(A.colidx + k + u) : ld_plain(A.colidx + k + u)) : 0;
+        v[u] = ok ? (STREAM ? ld_stream(A.vals + k + u) : ld_plain(A.vals + k + u)) : MV{};
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) xv[u] = (k + u < e) ? ld_ro(A.x + c[u]) : vzero(VV{});
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (k + u < e) acc = vfma(v[u], xv[u], acc);
+    }
+    yv = vscale(A.scale, acc);
+    A.y[r] = yv;
+  }
+  if (A.dotv) {
+    VV d = (r < A.dim) ? vdotfma(A.dotv[r], yv, vzero(VV{})) : vzero(VV{});
+    grid_sum(d, A.red, A.dot_out);
+  }
+}
+
+}  // namespace qd
