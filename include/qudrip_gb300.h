@@ -240,6 +240,22 @@ qd_status qd_ham_set_spmv_kernel(qd_ham *ham, int kernel);
  * solvers (the autotuner); returns the choice and its average ms. */
 qd_status qd_ham_autotune(qd_ham *ham, int iters, int *chosen, double *best_ms);
 
+/* <psi|H|psi> for a CSR Hamiltonian, with no device allocation at all.
+ * No counterpart in the reference: it serves callers that must not call
+ * cudaMalloc (an application that owns the device memory pool, or an
+ * allocation-free request path).  The caller passes device buffers it owns:
+ * d_rowptr (dim+1), d_colidx and d_vals (nnz complex128, interleaved), d_psi
+ * (dim complex128) and d_result (2 doubles, written on `stream`).  The work
+ * runs on `stream` on the current device.  Scratch is a fixed 32 KB array in
+ * the library's device image, so dim is limited to 4,194,304 rows (larger
+ * sizes are rejected with QD_ERR_INVALID).  The first call on each device
+ * looks that array up; make it before any stream capture.  Calls that overlap
+ * on one device race on the shared scratch. */
+qd_status qd_csr_expect_noalloc(const int64_t *d_rowptr, const int32_t *d_colidx,
+                                const double *d_vals, int64_t dim,
+                                const double *d_psi, double *d_result,
+                                void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -101,6 +101,7 @@ _SIGNATURES = {
     "qd_ham_time_spmv": [_P, C.c_int, C.c_int, _DP, _DP],
     "qd_ham_set_spmv_kernel": [_P, C.c_int],
     "qd_ham_autotune": [_P, C.c_int, C.POINTER(C.c_int), _DP],
+    "qd_csr_expect_noalloc": [_P, _P, _P, C.c_int64, _P, _P, _P],
     "qd_status_string": [C.c_int],
     "qd_last_error": [],
     "qd_api_version": [],
