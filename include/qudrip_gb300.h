@@ -225,6 +225,18 @@ qd_status qd_lanczos_ground(qd_ham *ham, qd_state *psi, int t,
                             const qd_lanczos_opts *opts, double *evals_out,
                             qd_lanczos_result *res);
 
+/* ------------------------------------------------------------------ */
+/* Krylov real-time step                                              */
+/*   replaces ArnoldiSolver<T,0>::evolve (sparse_algorithm.hpp:548-562)*/
+/*   with expandBasis<0> (:372-393) and MatrixExp (matrix.hpp:20)     */
+/* psi(:, t_out) = V exp(-i K h) e_0 with m-1 Arnoldi products from      */
+/* psi(:, t_in) normalised; unit norm for Hermitian H.  t_out may equal  */
+/* t_in.  act_dim (may be NULL) receives the Krylov dimension used.      */
+/* m (the solver's kry_dim) must be in 2..33.                           */
+/* ------------------------------------------------------------------ */
+qd_status qd_arnoldi_evolve(qd_ham *ham, qd_state *psi, int t_in, int t_out,
+                            double h, int m, int *act_dim);
+
 /* Average device time of the sparse product kernel the solvers use on this
  * Hamiltonian (iters back-to-back launches on the context stream, timed with
  * CUDA events), and the kernel's algorithmic HBM bytes per launch:

@@ -3,6 +3,7 @@
 #include <cstring>
 #include <string>
 
+#include "evolve.cuh"
 #include "ham.cuh"
 #include "krylov.cuh"
 #include "sector.cuh"
@@ -422,6 +423,16 @@ qd_status qd_ham_time_spmv(qd_ham* ham, int spmv, int iters, double* avg_ms, dou
                "qd_ham_time_spmv: unknown product kernel %d", spmv);
     DeviceGuard dg(ham->ctx->device);
     time_spmv(ham, spmv, iters, avg_ms, bytes_per_launch);
+  });
+}
+
+qd_status qd_arnoldi_evolve(qd_ham* ham, qd_state* psi, int t_in, int t_out, double h, int m, int* act_dim) {
+  return guard([&] {
+    QD_REQUIRE(ham && psi, QD_ERR_INVALID, "null argument");
+    QD_REQUIRE(psi->dim == ham->dim, QD_ERR_INVALID, "dimension mismatch");
+    QD_REQUIRE(t_in >= 0 && t_in < psi->nt && t_out >= 0 && t_out < psi->nt, QD_ERR_INVALID, "bad column");
+    DeviceGuard dg(ham->ctx->device);
+    arnoldi_evolve(ham, psi->col(t_in), psi->col(t_out), h, m, act_dim);
   });
 }
 

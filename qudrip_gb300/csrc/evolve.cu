@@ -1,0 +1,261 @@
+// evolve.cu -- Krylov real-time step psi <- exp(-i H h) psi.
+//
+// Restates ArnoldiSolver<T, herm=0>::evolve (sparse_algorithm.hpp:548-562)
+// with expandBasis<0> (:372-393) and updateKrylovRepr (:521-546):
+//   v_0 = psi / ||psi||;  for idx = 1 .. m-1:
+//     w = H v_{idx-1};  orthogonalise w against v_0 .. v_{idx-1};
+//     h_{idx, idx-1} = ||w||;  v_idx = w / ||w||;  stop (keeping the step)
+//     when ||w|| < 1e-10;
+//   act = number of columns;  psi_out = V[:, :act] exp(-i h K[:act, :act])[:, 0].
+// The reference orthogonalises by modified Gram-Schmidt, one dot and one axpy
+// per previous vector.  On the device each pass is instead one multi-dot
+// kernel (all projections at once) and one update kernel, applied twice
+// (classical Gram-Schmidt with reorthogonalisation): the same projector up to
+// rounding, with better orthogonality, in 4 launches per step instead of
+// 2 * idx.  The small exponential runs on the host (dense.h).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "dense.h"
+#include "evolve.cuh"
+#include "krylov.cuh"
+#include "spmv.cuh"
+
+namespace qd {
+
+constexpr int kEvThreads = 256;
+
+static int ev_grid(Ctx* ctx, int64_t n) {
+  const int64_t want = ceil_div(n, kEvThreads * 4);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->num_sms * 2));
+}
+
+__device__ __forceinline__ bool ev_stopped(const int* stop, int step) {
+  const int st = *stop;
+  return st != 0 && st < step;
+}
+
+// out[j] = <V_j, w> for j < J (J <= JB); deterministic grid reduction.
+template <int JB>
+__global__ void __launch_bounds__(kEvThreads) multidot_kernel(int64_t n, const cplx* __restrict__ V, int64_t ld,
+                                                              int J, const cplx* __restrict__ w, cplx* partials,
+                                                              unsigned* ticket, cplx* out, const int* stop,
+                                                              int step) {
+  if (ev_stopped(stop, step)) return;
+  __shared__ cplx s_part[kEvThreads / 32][JB];
+  __shared__ bool last;
+  cplx acc[JB];
+#pragma unroll
+  for (int j = 0; j < JB; ++j) acc[j] = mkc(0.0, 0.0);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const cplx wi = w[i];
+#pragma unroll
+    for (int j = 0; j < JB; ++j)
+      if (j < J) acc[j] = vdotfma(V[(int64_t)j * ld + i], wi, acc[j]);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < JB; ++j) {
+    const cplx v = warp_sum(acc[j]);
+    if (lane == 0) s_part[warp][j] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < JB) {
+    cplx b = mkc(0.0, 0.0);
+    for (int q = 0; q < kEvThreads / 32; ++q) b = vadd(b, s_part[q][threadIdx.x]);
+    partials[(int64_t)blockIdx.x * JB + threadIdx.x] = b;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (threadIdx.x < J) {
+    cplx t = mkc(0.0, 0.0);
+    for (unsigned b = 0; b < gridDim.x; ++b) t = vadd(t, ld_cg(partials + (int64_t)b * JB + threadIdx.x));
+    out[threadIdx.x] = t;
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
+}
+
+// w -= sum_{j<J} c_j V_j;  acc_h[j] += c_j (the Hessenberg column gathers both passes)
+__global__ void __launch_bounds__(kEvThreads) gs_update_kernel(int64_t n, const cplx* __restrict__ V, int64_t ld,
+                                                               int J, const cplx* c, cplx* __restrict__ w,
+                                                               cplx* hcol, int first_pass, const int* stop, int step) {
+  if (ev_stopped(stop, step)) return;
+  __shared__ cplx s_c[64];
+  if (threadIdx.x < J) s_c[threadIdx.x] = c[threadIdx.x];
+  __syncthreads();
+  if (blockIdx.x == 0 && threadIdx.x < J)
+    hcol[threadIdx.x] = first_pass ? s_c[threadIdx.x] : vadd(hcol[threadIdx.x], s_c[threadIdx.x]);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    cplx wi = w[i];
+    for (int j = 0; j < J; ++j) wi = vsubmul(wi, s_c[j], V[(int64_t)j * ld + i]);
+    w[i] = wi;
+  }
+}
+
+__global__ void __launch_bounds__(kEvThreads) ev_norm_kernel(int64_t n, const cplx* __restrict__ w, double* nrm2,
+                                                             double* nrm, GridRed<double> red, int* stop, int step) {
+  if (ev_stopped(stop, step)) return;
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc += vnorm2(w[i]);
+  if (grid_sum(acc, red, nrm2) && threadIdx.x == 0) {
+    const double nr = sqrt(*nrm2);
+    *nrm = nr;
+    if (nr < 1e-10 && *stop == 0) *stop = step;  // sparse_algorithm.hpp:387
+  }
+}
+
+__global__ void __launch_bounds__(kEvThreads) ev_scale_kernel(int64_t n, const cplx* __restrict__ w,
+                                                              const double* nrm, cplx* __restrict__ vout,
+                                                              const int* stop, int step) {
+  if (ev_stopped(stop, step)) return;
+  const double inv = 1.0 / *nrm;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    vout[i] = vscale(inv, w[i]);
+}
+
+__global__ void __launch_bounds__(kEvThreads) ev_init_kernel(int64_t n, const cplx* psi, const double* nrm2,
+                                                             cplx* v0) {
+  const double inv = 1.0 / sqrt(*nrm2);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    v0[i] = vscale(inv, psi[i]);
+}
+
+__global__ void __launch_bounds__(kEvThreads) ev_norm_only_kernel(int64_t n, const cplx* psi, double* nrm2,
+                                                                  GridRed<double> red) {
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc += vnorm2(psi[i]);
+  grid_sum(acc, red, nrm2);
+}
+
+// out = sum_{j<a} e_j V_j
+__global__ void __launch_bounds__(kEvThreads) ev_combine_kernel(int64_t n, const cplx* __restrict__ V, int64_t ld,
+                                                                int a, const cplx* e, cplx* __restrict__ out) {
+  __shared__ cplx s_e[64];
+  if (threadIdx.x < a) s_e[threadIdx.x] = e[threadIdx.x];
+  __syncthreads();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    cplx acc = mkc(0.0, 0.0);
+    for (int j = 0; j < a; ++j) acc = vfma(s_e[j], V[(int64_t)j * ld + i], acc);
+    out[i] = acc;
+  }
+}
+
+void ArnoldiBuffers::ensure(int64_t n_, int m_, int grid) {
+  if (n_ == n && m_ == m && grid <= grid_cap) return;
+  n = n_;
+  m = m_;
+  ld = (n + 31) / 32 * 32;
+  grid_cap = std::max(grid, 1);
+  V.alloc((size_t)(m + 1) * ld);
+  w.alloc(ld);
+  proj.alloc(64);
+  hcol.alloc((size_t)(m + 1) * 64);
+  nrm.alloc(m + 2);
+  nrm2.alloc(m + 2);
+  stop.alloc(1);
+  e.alloc(64);
+  partials.alloc((size_t)grid_cap * 32);
+  rpart.alloc(kMaxGrid);
+  tickets.alloc(4);
+  QD_CUDA(cudaMemset(tickets.p, 0, 4 * sizeof(unsigned)));
+}
+
+template <typename MV>
+static void arnoldi_steps(qd_ham* H, const MV* vals, ArnoldiBuffers& B, int steps) {
+  Ctx* ctx = H->ctx;
+  Workspace& W = ham_workspace(H);
+  const int64_t n = B.n;
+  const int g = ev_grid(ctx, n);
+  for (int idx = 1; idx <= steps; ++idx) {
+    const cplx* vprev = B.V.p + (int64_t)(idx - 1) * B.ld;
+    launch_spmv<MV, cplx>(ctx, H, vals, vprev, B.w.p, 1.0, nullptr, W.red_c(0), nullptr, B.stop.p, idx, -1);
+    cplx* hcol = B.hcol.p + (int64_t)(idx - 1) * 64;
+    for (int pass = 0; pass < 2; ++pass) {
+      if (idx <= 8)
+        multidot_kernel<8><<<g, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, idx, B.w.p, B.partials.p,
+                                                               B.tickets.p, B.proj.p, B.stop.p, idx);
+      else if (idx <= 16)
+        multidot_kernel<16><<<g, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, idx, B.w.p, B.partials.p,
+                                                                B.tickets.p, B.proj.p, B.stop.p, idx);
+      else
+        multidot_kernel<32><<<g, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, idx, B.w.p, B.partials.p,
+                                                                B.tickets.p, B.proj.p, B.stop.p, idx);
+      QD_CHECK_LAUNCH();
+      QD_LAUNCHED(ctx);
+      gs_update_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, idx, B.proj.p, B.w.p, hcol, pass == 0,
+                                                           B.stop.p, idx);
+      QD_CHECK_LAUNCH();
+      QD_LAUNCHED(ctx);
+    }
+    ev_norm_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, B.w.p, B.nrm2.p + idx, B.nrm.p + idx,
+                                                       GridRed<double>{B.rpart.p, B.tickets.p + 1}, B.stop.p, idx);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+    ev_scale_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, B.w.p, B.nrm.p + idx, B.V.p + (int64_t)idx * B.ld,
+                                                        B.stop.p, idx);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+  }
+}
+
+void arnoldi_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int m, int* act_out) {
+  Ctx* ctx = H->ctx;
+  QD_REQUIRE(m >= 2 && m <= 33, QD_ERR_UNSUPPORTED, "Krylov dimension m must be in 2..33");
+  const int64_t n = H->dim;
+  if (!H->arnoldi) H->arnoldi.reset(new ArnoldiBuffers());
+  ArnoldiBuffers& B = *H->arnoldi;
+  const int g = ev_grid(ctx, n);
+  B.ensure(n, m, g);
+  // v_0 = psi / ||psi||
+  ev_norm_only_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, psi_in, B.nrm2.p, GridRed<double>{B.rpart.p, B.tickets.p + 1});
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  ev_init_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, psi_in, B.nrm2.p, B.V.p);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  QD_CUDA(cudaMemsetAsync(B.stop.p, 0, sizeof(int), ctx->stream));
+  const int steps = m - 1;  // updateKrylovRepr(H, kry_dim_rt - 1)
+  if (H->flags & QD_HAM_REAL)
+    arnoldi_steps<double>(H, H->vals_r.p, B, steps);
+  else
+    arnoldi_steps<cplx>(H, H->vals_c.p, B, steps);
+  std::vector<cplx> hc((size_t)(m + 1) * 64);
+  std::vector<double> nrm(m + 2);
+  int stop = 0;
+  QD_CUDA(cudaMemcpyAsync(hc.data(), B.hcol.p, hc.size() * sizeof(cplx), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(nrm.data(), B.nrm.p, nrm.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(&stop, B.stop.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  const int act = stop ? stop : steps;  // expandBasis<0> return value
+  // K(j, i) = projection of H v_i on v_j (j <= i), K(i+1, i) = ||w_{i+1}||
+  dense::Mat A((size_t)act * act, dense::cd(0.0, 0.0));
+  for (int i = 0; i < act; ++i) {
+    for (int j = 0; j <= i; ++j) {
+      const cplx v = hc[(size_t)i * 64 + j];
+      A[(size_t)i * act + j] = dense::cd(v.re, v.im);
+    }
+    if (i + 1 < act) A[(size_t)i * act + i + 1] = nrm[i + 1];
+  }
+  for (auto& a : A) a *= dense::cd(0.0, -h);  // -i K h
+  dense::Mat E;
+  QD_REQUIRE(dense::expm(A, act, E), QD_ERR_INVALID, "matrix exponential failed");
+  std::vector<cplx> e(act);
+  for (int j = 0; j < act; ++j) e[j] = mkc(E[j].real(), E[j].imag());
+  QD_CUDA(cudaMemcpyAsync(B.e.p, e.data(), act * sizeof(cplx), cudaMemcpyHostToDevice, ctx->stream));
+  ev_combine_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, act, B.e.p, psi_out);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (act_out) *act_out = act;
+}
+
+void ArnoldiDeleter::operator()(ArnoldiBuffers* b) const { delete b; }
+
+}  // namespace qd

@@ -20,6 +20,10 @@ struct Workspace;
 struct WorkspaceDeleter {
   void operator()(Workspace* w) const;
 };
+struct ArnoldiBuffers;
+struct ArnoldiDeleter {
+  void operator()(ArnoldiBuffers* b) const;
+};
 
 struct GateDev {
   int kind, site, site_b, string;
@@ -78,6 +82,7 @@ struct qd_ham {
   std::vector<qd_term> host_terms;
   std::vector<qd_gate> host_gates;
   std::unique_ptr<qd::Workspace, qd::WorkspaceDeleter> ws;  // solver buffers, reused across calls
+  std::unique_ptr<qd::ArnoldiBuffers, qd::ArnoldiDeleter> arnoldi;
 };
 
 namespace qd {

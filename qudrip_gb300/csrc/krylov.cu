@@ -31,11 +31,6 @@ static int vec_grid(Ctx* ctx, int64_t n) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->num_sms * 8));
 }
 
-static int spmv_grid(Ctx* ctx, int64_t dim) {
-  const int64_t tiles = (dim + 31) / 32;
-  const int64_t want = ceil_div(tiles, kSpmvWarps);
-  return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->num_sms * 16));
-}
 
 // ---------------------------------------------------------------- kernels
 __device__ __forceinline__ bool stopped(const int* stop, int step) {
@@ -44,48 +39,87 @@ __device__ __forceinline__ bool stopped(const int* stop, int step) {
   return st != 0 && st < step;
 }
 
+// The basis is stored unnormalised: V[k] = n_k v_k, with s_k = 1 / n_k kept on
+// the device (s_0 = 1).  Every consumer folds s into its scalars, so no pass
+// is spent rescaling a vector.  Loops are unrolled four wide with independent
+// partial sums so each thread keeps several loads in flight.
+constexpr int kVecUnroll = 4;
+
+// K2: w -= (beta' s2) V2;  alpha = s1 <V1, w>
 template <typename VV>
-__global__ void __launch_bounds__(kVecThreads) lz_k2_kernel(int64_t n, const int* stop, int step, VV* w,
-                                                            const VV* v1, const VV* v2, const VV* beta,
-                                                            VV* alpha, GridRed<VV> red) {
+__global__ void __launch_bounds__(kVecThreads) lz_k2_kernel(int64_t n, const int* stop, int step, VV* __restrict__ w,
+                                                            const VV* __restrict__ V1, const VV* __restrict__ V2,
+                                                            const double* s1, const double* s2,
+                                                            const VV* beta, VV* alpha, GridRed<VV> red) {
   if (stopped(stop, step)) return;
-  const VV b = v2 ? *beta : vzero(VV{});
-  VV acc = vzero(VV{});
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    VV wi = w[i];
-    if (v2) wi = vsubmul(wi, b, v2[i]);
-    w[i] = wi;
-    acc = vdotfma(v1[i], wi, acc);
+  const VV b = V2 ? vscale(*s2, *beta) : vzero(VV{});
+  VV acc[kVecUnroll];
+#pragma unroll
+  for (int u = 0; u < kVecUnroll; ++u) acc[u] = vzero(VV{});
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + (kVecUnroll - 1) * stride < n; i += kVecUnroll * stride) {
+    VV wv[kVecUnroll], v1[kVecUnroll], v2[kVecUnroll];
+#pragma unroll
+    for (int u = 0; u < kVecUnroll; ++u) {
+      wv[u] = w[i + u * stride];
+      v1[u] = V1[i + u * stride];
+      v2[u] = V2 ? V2[i + u * stride] : vzero(VV{});
+    }
+#pragma unroll
+    for (int u = 0; u < kVecUnroll; ++u) {
+      if (V2) wv[u] = vsubmul(wv[u], b, v2[u]);
+      w[i + u * stride] = wv[u];
+      acc[u] = vdotfma(v1[u], wv[u], acc[u]);
+    }
   }
-  grid_sum(acc, red, alpha);
+  for (; i < n; i += stride) {
+    VV wi = w[i];
+    if (V2) wi = vsubmul(wi, b, V2[i]);
+    w[i] = wi;
+    acc[0] = vdotfma(V1[i], wi, acc[0]);
+  }
+  const VV tot = vadd(vadd(acc[0], acc[1]), vadd(acc[2], acc[3]));
+  if (grid_sum(tot, red, alpha) && threadIdx.x == 0) *alpha = vscale(*s1, *alpha);
 }
 
+// K3: V[k] = w - (alpha s1) V1;  n_k = ||V[k]||, s_k = 1 / n_k, stop if n_k < 1e-10
 template <typename VV>
-__global__ void __launch_bounds__(kVecThreads) lz_k3_kernel(int64_t n, int* stop, int step, VV* w,
-                                                            const VV* v1, const VV* alpha, double* nrm2,
-                                                            double* nrm, GridRed<double> red) {
+__global__ void __launch_bounds__(kVecThreads) lz_k3_kernel(int64_t n, int* stop, int step, const VV* __restrict__ w,
+                                                            const VV* __restrict__ V1, const double* s1,
+                                                            const VV* alpha, VV* __restrict__ Vk, double* nrm2,
+                                                            double* nrm, double* sk, GridRed<double> red) {
   if (stopped(stop, step)) return;
-  const VV a = *alpha;
-  double acc = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const VV wi = vsubmul(w[i], a, v1[i]);
-    w[i] = wi;
-    acc += vnorm2(wi);
+  const VV a = vscale(*s1, *alpha);
+  double acc[kVecUnroll] = {0.0, 0.0, 0.0, 0.0};
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + (kVecUnroll - 1) * stride < n; i += kVecUnroll * stride) {
+    VV wv[kVecUnroll], v1[kVecUnroll];
+#pragma unroll
+    for (int u = 0; u < kVecUnroll; ++u) {
+      wv[u] = w[i + u * stride];
+      v1[u] = V1[i + u * stride];
+    }
+#pragma unroll
+    for (int u = 0; u < kVecUnroll; ++u) {
+      const VV o = vsubmul(wv[u], a, v1[u]);
+      Vk[i + u * stride] = o;
+      acc[u] += vnorm2(o);
+    }
   }
-  if (grid_sum(acc, red, nrm2) && threadIdx.x == 0) {
+  for (; i < n; i += stride) {
+    const VV o = vsubmul(w[i], a, V1[i]);
+    Vk[i] = o;
+    acc[0] += vnorm2(o);
+  }
+  const double tot = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+  if (grid_sum(tot, red, nrm2) && threadIdx.x == 0) {
     const double nr = sqrt(*nrm2);
     *nrm = nr;
+    *sk = 1.0 / nr;
     if (nr < 1e-10 && *stop == 0) *stop = step;  // sparse_algorithm.hpp:421
   }
-}
-
-template <typename VV>
-__global__ void __launch_bounds__(kVecThreads) lz_k4_kernel(int64_t n, const int* stop, int step, const VV* w,
-                                                            const double* nrm, VV* vout) {
-  if (stopped(stop, step)) return;
-  const double inv = 1.0 / *nrm;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    vout[i] = vscale(inv, w[i]);
 }
 
 // ||psi||^2 of a complex column, and whether its imaginary part vanishes.
@@ -137,61 +171,6 @@ __global__ void __launch_bounds__(kVecThreads) cdot_kernel(int64_t n, const cplx
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     acc = vdotfma(a[i], b[i], acc);
   grid_sum(acc, red, out);
-}
-
-// ---------------------------------------------------------------- launches
-template <typename MV, typename VV>
-void launch_spmv(Ctx* ctx, const qd_ham* H, const MV* vals, const VV* x, VV* y, double scale, const VV* dotv,
-                 GridRed<VV> red, VV* dot_out, const int* stop, int step, int variant) {
-  SpmvArgs<MV, VV> A;
-  A.dim = H->dim;
-  A.rowptr = H->rowptr.p;
-  A.colidx = H->colidx.p;
-  A.vals = vals;
-  A.x = x;
-  A.y = y;
-  A.scale = scale;
-  A.dotv = dotv;
-  A.red = red;
-  A.dot_out = dot_out;
-  A.stop = stop;
-  A.step = step;
-  if (variant < 0) variant = H->spmv_variant;
-  const int64_t vg = std::max<int64_t>(1, std::min<int64_t>(ceil_div(H->dim, 256 / 4), (int64_t)ctx->num_sms * 8));
-  switch (variant) {
-    case kSpmvTile:
-      spmv_tile_kernel<MV, VV><<<spmv_grid(ctx, H->dim), kSpmvThreads, 0, ctx->stream>>>(A);
-      break;
-    case kSpmvBalanced:
-      spmv_balanced_kernel<MV, VV><<<spmv_grid(ctx, H->dim), kSpmvThreads, 0, ctx->stream>>>(A);
-      break;
-    case kSpmvVector2:
-      spmv_vector_kernel<MV, VV, 2><<<(unsigned)vg, 256, 0, ctx->stream>>>(A);
-      break;
-    case kSpmvVector4:
-      spmv_vector_kernel<MV, VV, 4><<<(unsigned)vg, 256, 0, ctx->stream>>>(A);
-      break;
-    case kSpmvVector8:
-      spmv_vector_kernel<MV, VV, 8><<<(unsigned)vg, 256, 0, ctx->stream>>>(A);
-      break;
-    case kSpmvRow4:
-      spmv_rowunroll_kernel<MV, VV, 4, false><<<(unsigned)ceil_div(H->dim, 256), 256, 0, ctx->stream>>>(A);
-      break;
-    case kSpmvRow8:
-      spmv_rowunroll_kernel<MV, VV, 8, false><<<(unsigned)ceil_div(H->dim, 256), 256, 0, ctx->stream>>>(A);
-      break;
-    case kSpmvRow4Stream:
-      spmv_rowunroll_kernel<MV, VV, 4, true><<<(unsigned)ceil_div(H->dim, 256), 256, 0, ctx->stream>>>(A);
-      break;
-    case kSpmvRow8Stream:
-      spmv_rowunroll_kernel<MV, VV, 8, true><<<(unsigned)ceil_div(H->dim, 256), 256, 0, ctx->stream>>>(A);
-      break;
-    default:
-      spmv_vector_kernel<MV, VV, 1><<<(unsigned)vg, 256, 0, ctx->stream>>>(A);
-      break;
-  }
-  QD_CHECK_LAUNCH();
-  QD_LAUNCHED(ctx);
 }
 
 Workspace::Workspace(Ctx* c) : ctx(c) {
@@ -271,19 +250,20 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int kd
   const int64_t n = H->dim;
   const int vg = vec_grid(ctx, n);
   for (int k = 1; k <= kdim; ++k) {
-    const VV* v1 = B.V.p + (int64_t)(k - 1) * B.ld;
-    const VV* v2 = (k >= 2) ? B.V.p + (int64_t)(k - 2) * B.ld : nullptr;
-    VV* vout = B.V.p + (int64_t)k * B.ld;
-    launch_spmv<MV, VV>(ctx, H, vals, v1, B.w.p, 1.0, v2, W.red_c_or_d<VV>(1), B.beta.p + k, B.stop.p, k, -1);
-    lz_k2_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.stop.p, k, B.w.p, v1, v2, B.beta.p + k,
+    const VV* V1 = B.V.p + (int64_t)(k - 1) * B.ld;
+    const VV* V2 = (k >= 2) ? B.V.p + (int64_t)(k - 2) * B.ld : nullptr;
+    VV* Vk = B.V.p + (int64_t)k * B.ld;
+    const double* s1 = B.scl.p + (k - 1);
+    const double* s2 = (k >= 2) ? B.scl.p + (k - 2) : nullptr;
+    // K1: w = s1 * H V1, beta' = s2 <V2, w>
+    launch_spmv<MV, VV>(ctx, H, vals, V1, B.w.p, 1.0, V2, W.red_c_or_d<VV>(1), B.beta.p + k, B.stop.p, k, -1, s1,
+                        s2);
+    lz_k2_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.stop.p, k, B.w.p, V1, V2, s1, s2, B.beta.p + k,
                                                            B.alpha.p + k, W.red_c_or_d<VV>(2));
     QD_CHECK_LAUNCH();
     QD_LAUNCHED(ctx);
-    lz_k3_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.stop.p, k, B.w.p, v1, B.alpha.p + k,
-                                                           B.nrm2.p + k, B.nrm.p + k, W.red_d(3));
-    QD_CHECK_LAUNCH();
-    QD_LAUNCHED(ctx);
-    lz_k4_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.stop.p, k, B.w.p, B.nrm.p + k, vout);
+    lz_k3_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.stop.p, k, B.w.p, V1, s1, B.alpha.p + k, Vk,
+                                                           B.nrm2.p + k, B.nrm.p + k, B.scl.p + k, W.red_d(3));
     QD_CHECK_LAUNCH();
     QD_LAUNCHED(ctx);
   }
@@ -316,6 +296,8 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
   else vals = H->vals_c.p;
   const int vg = vec_grid(ctx, n);
   QD_CUDA(cudaMemsetAsync(B.stop.p, 0, sizeof(int), ctx->stream));
+  const double one = 1.0;
+  QD_CUDA(cudaMemcpyAsync(B.scl.p, &one, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   init_v0_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, psi, psi_nrm2, B.V.p);
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
@@ -352,7 +334,12 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
     lanczos_run<MV, VV>(H, vals, B, act, W);
     matvecs += act;
   }
-  QD_CUDA(cudaMemcpyAsync(B.y.p, z.data(), act * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  // psi = sum_k y_k v_k = sum_k (y_k s_k) V[k]
+  std::vector<double> scl(kdim + 1), yk(act);
+  QD_CUDA(cudaMemcpyAsync(scl.data(), B.scl.p, (kdim + 1) * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  for (int i = 0; i < act; ++i) yk[i] = z[i] * scl[i];
+  QD_CUDA(cudaMemcpyAsync(B.y.p, yk.data(), act * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   ritz_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, B.y.p, act, psi);
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);

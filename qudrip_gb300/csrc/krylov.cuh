@@ -4,26 +4,12 @@
 #include <type_traits>
 
 #include "ham.cuh"
+#include "spmv.cuh"
 #include "vec.cuh"
 
 namespace qd {
 
-constexpr int kMaxGrid = 8192;  // upper bound on blocks of any reduction kernel
 
-// CSR product kernels (qd_ham::spmv_variant; qd_ham_time_spmv accepts them as `spmv`)
-enum SpmvVariant {
-  kSpmvTile = 100,      // warp tile, lane per row, staged in shared memory
-  kSpmvBalanced = 101,  // warp tile, equal nnz per lane
-  kSpmvVector2 = 102,   // 2 lanes per row
-  kSpmvVector4 = 103,
-  kSpmvVector8 = 104,
-  kSpmvScalar = 105,    // thread per row
-  kSpmvRow4 = 106,      // thread per row, 4 loads in flight
-  kSpmvRow8 = 107,      // thread per row, 8 loads in flight
-  kSpmvRow4Stream = 108,  // as 106 with evict-first matrix loads
-  kSpmvRow8Stream = 109,  // as 107 with evict-first matrix loads
-  kSpmvLast = 109,
-};
 
 inline double real_part(double v) { return v; }
 inline double real_part(cplx v) { return v.re; }
@@ -37,7 +23,7 @@ struct LanczosBuffers {
   DBuf<VV> V;      // (kdim + 1) x ld basis vectors
   DBuf<VV> w;
   DBuf<VV> alpha, beta;
-  DBuf<double> nrm, nrm2, y;
+  DBuf<double> nrm, nrm2, y, scl;  // scl[k] = 1 / ||V[k]|| (basis stored unnormalised)
   DBuf<int> stop;
   cudaGraphExec_t exec = nullptr;
   int64_t graph_kernels = 0;
@@ -55,6 +41,7 @@ struct LanczosBuffers {
     nrm.alloc(kdim + 2);
     nrm2.alloc(kdim + 2);
     y.alloc(kdim + 2);
+    scl.alloc(kdim + 2);
     stop.alloc(1);
   }
   void drop_graph() {

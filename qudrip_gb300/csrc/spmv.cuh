@@ -14,6 +14,23 @@
 
 namespace qd {
 
+constexpr int kMaxGrid = 8192;  // upper bound on blocks of any reduction kernel
+
+// CSR product kernels (qd_ham::spmv_variant; qd_ham_time_spmv accepts them as `spmv`)
+enum SpmvVariant {
+  kSpmvTile = 100,      // warp tile, lane per row, staged in shared memory
+  kSpmvBalanced = 101,  // warp tile, equal nnz per lane
+  kSpmvVector2 = 102,   // 2 lanes per row
+  kSpmvVector4 = 103,
+  kSpmvVector8 = 104,
+  kSpmvScalar = 105,    // thread per row
+  kSpmvRow4 = 106,      // thread per row, 4 loads in flight
+  kSpmvRow8 = 107,      // thread per row, 8 loads in flight
+  kSpmvRow4Stream = 108,  // as 106 with evict-first matrix loads
+  kSpmvRow8Stream = 109,  // as 107 with evict-first matrix loads
+  kSpmvLast = 109,
+};
+
 constexpr int kSpmvWarps = 4;  // warps per block
 constexpr int kSpmvThreads = kSpmvWarps * 32;
 // staged entries per warp tile: the block's staging fits in 46 KB of static shared memory
@@ -36,7 +53,20 @@ struct SpmvArgs {
   VV* dot_out;         // final <dotv, y> (thread 0 of the last block)
   const int* stop;     // if non-null and *stop != 0 and *stop < step: do nothing
   int step;
+  const double* scale_dev;      // if non-null, the scale is read from the device
+  const double* dot_scale_dev;  // if non-null, the final dot is multiplied by *dot_scale_dev
 };
+
+template <typename MV, typename VV>
+__device__ __forceinline__ double spmv_scale(const SpmvArgs<MV, VV>& A) {
+  return A.scale_dev ? *A.scale_dev : A.scale;
+}
+
+template <typename MV, typename VV>
+__device__ __forceinline__ void spmv_finish_dot(const SpmvArgs<MV, VV>& A, VV dotacc) {
+  if (grid_sum(dotacc, A.red, A.dot_out) && threadIdx.x == 0 && A.dot_scale_dev)
+    *A.dot_out = vscale(*A.dot_scale_dev, *A.dot_out);
+}
 
 template <typename T>
 __device__ __forceinline__ void stage_copy(T* dst, const T* src, int n, int lane) {
@@ -78,12 +108,12 @@ __global__ void __launch_bounds__(kSpmvThreads) spmv_tile_kernel(SpmvArgs<MV, VV
       for (int64_t k = rb; k < re; ++k) acc = vfma(A.vals[k], ld_ro(A.x + A.colidx[k]), acc);
     }
     if (live) {
-      const VV yv = vscale(A.scale, acc);
+      const VV yv = vscale(spmv_scale(A), acc);
       A.y[r] = yv;
       if (A.dotv) dotacc = vdotfma(A.dotv[r], yv, dotacc);
     }
   }
-  if (A.dotv) grid_sum(dotacc, A.red, A.dot_out);
+  if (A.dotv) spmv_finish_dot(A, dotacc);
 }
 
 }  // namespace qd
@@ -214,13 +244,13 @@ __global__ void __launch_bounds__(kSpmvThreads) spmv_balanced_kernel(SpmvArgs<MV
     __syncwarp();
     if (lane < nrows) {
       const int64_t r = r0 + lane;
-      const VV yv = vscale(A.scale, s_y[warp][lane]);
+      const VV yv = vscale(spmv_scale(A), s_y[warp][lane]);
       A.y[r] = yv;
       if (A.dotv) dotacc = vdotfma(A.dotv[r], yv, dotacc);
     }
     __syncwarp();
   }
-  if (A.dotv) grid_sum(dotacc, A.red, A.dot_out);
+  if (A.dotv) spmv_finish_dot(A, dotacc);
 }
 
 // ---------------------------------------------------------------------------
@@ -248,12 +278,12 @@ __global__ void __launch_bounds__(256) spmv_vector_kernel(SpmvArgs<MV, VV> A) {
 #pragma unroll
     for (int o = G / 2; o > 0; o >>= 1) acc = vadd(acc, shfl_xor(acc, o));
     if (r < A.dim && sub == 0) {
-      const VV yv = vscale(A.scale, acc);
+      const VV yv = vscale(spmv_scale(A), acc);
       A.y[r] = yv;
       if (A.dotv) dotacc = vdotfma(A.dotv[r], yv, dotacc);
     }
   }
-  if (A.dotv) grid_sum(dotacc, A.red, A.dot_out);
+  if (A.dotv) spmv_finish_dot(A, dotacc);
 }
 
 }  // namespace qd
@@ -281,9 +311,9 @@ __global__ void __launch_bounds__(256) spmv_rowunroll_kernel(SpmvArgs<MV, VV> A)
     const int st = *A.stop;
     if (st != 0 && st < A.step) return;
   }
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  VV yv = vzero(VV{});
-  if (r < A.dim) {
+  VV dotacc = vzero(VV{});
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < A.dim; r += stride) {
     const int64_t b = A.rowptr[r], e = A.rowptr[r + 1];
     VV acc = vzero(VV{});
     for (int64_t k = b; k < e; k += U) {
@@ -302,13 +332,65 @@ __global__ void __launch_bounds__(256) spmv_rowunroll_kernel(SpmvArgs<MV, VV> A)
       for (int u = 0; u < U; ++u)
         if (k + u < e) acc = vfma(v[u], xv[u], acc);
     }
-    yv = vscale(A.scale, acc);
+    const VV yv = vscale(spmv_scale(A), acc);
     A.y[r] = yv;
+    if (A.dotv) dotacc = vdotfma(A.dotv[r], yv, dotacc);
   }
-  if (A.dotv) {
-    VV d = (r < A.dim) ? vdotfma(A.dotv[r], yv, vzero(VV{})) : vzero(VV{});
-    grid_sum(d, A.red, A.dot_out);
+  if (A.dotv) spmv_finish_dot(A, dotacc);
+}
+
+}  // namespace qd
+
+namespace qd {
+
+inline int spmv_grid(Ctx* ctx, int64_t dim) {
+  const int64_t tiles = (dim + 31) / 32;
+  const int64_t want = ceil_div(tiles, kSpmvWarps);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->num_sms * 16));
+}
+
+// ---------------------------------------------------------------- launches
+template <typename MV, typename VV>
+inline void launch_spmv(Ctx* ctx, const qd_ham* H, const MV* vals, const VV* x, VV* y, double scale, const VV* dotv,
+                 GridRed<VV> red, VV* dot_out, const int* stop, int step, int variant,
+                 const double* scale_dev = nullptr, const double* dot_scale_dev = nullptr) {
+  SpmvArgs<MV, VV> A;
+  A.dim = H->dim;
+  A.rowptr = H->rowptr.p;
+  A.colidx = H->colidx.p;
+  A.vals = vals;
+  A.x = x;
+  A.y = y;
+  A.scale = scale;
+  A.dotv = dotv;
+  A.red = red;
+  A.dot_out = dot_out;
+  A.stop = stop;
+  A.step = step;
+  A.scale_dev = scale_dev;
+  A.dot_scale_dev = dot_scale_dev;
+  if (variant < 0) variant = H->spmv_variant;
+  // every grid is capped so the block partials of a fused dot fit in kMaxGrid slots
+  const unsigned vg = (unsigned)std::max<int64_t>(
+      1, std::min<int64_t>(ceil_div(H->dim, 256 / 4), (int64_t)ctx->num_sms * 8));
+  const unsigned rg = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(H->dim, 256), (int64_t)ctx->num_sms * 8));
+  const unsigned tg = (unsigned)spmv_grid(ctx, H->dim);
+  QD_REQUIRE(vg <= (unsigned)kMaxGrid && rg <= (unsigned)kMaxGrid && tg <= (unsigned)kMaxGrid, QD_ERR_UNSUPPORTED,
+             "reduction grid exceeds its partials buffer");
+  switch (variant) {
+    case kSpmvTile: spmv_tile_kernel<MV, VV><<<tg, kSpmvThreads, 0, ctx->stream>>>(A); break;
+    case kSpmvBalanced: spmv_balanced_kernel<MV, VV><<<tg, kSpmvThreads, 0, ctx->stream>>>(A); break;
+    case kSpmvVector2: spmv_vector_kernel<MV, VV, 2><<<vg, 256, 0, ctx->stream>>>(A); break;
+    case kSpmvVector4: spmv_vector_kernel<MV, VV, 4><<<vg, 256, 0, ctx->stream>>>(A); break;
+    case kSpmvVector8: spmv_vector_kernel<MV, VV, 8><<<vg, 256, 0, ctx->stream>>>(A); break;
+    case kSpmvRow4: spmv_rowunroll_kernel<MV, VV, 4, false><<<rg, 256, 0, ctx->stream>>>(A); break;
+    case kSpmvRow8: spmv_rowunroll_kernel<MV, VV, 8, false><<<rg, 256, 0, ctx->stream>>>(A); break;
+    case kSpmvRow4Stream: spmv_rowunroll_kernel<MV, VV, 4, true><<<rg, 256, 0, ctx->stream>>>(A); break;
+    case kSpmvRow8Stream: spmv_rowunroll_kernel<MV, VV, 8, true><<<rg, 256, 0, ctx->stream>>>(A); break;
+    default: spmv_vector_kernel<MV, VV, 1><<<vg, 256, 0, ctx->stream>>>(A); break;
   }
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
 }
 
 }  // namespace qd

@@ -306,7 +306,37 @@ class LanczosSolver:
                 f.write(f"{e:.6g}\n")
 
 
+class ArnoldiSolver:
+    """Arnoldi::getSolver(index, kry_dim) -- ArnoldiSolver<T, herm=0> (real-time steps)."""
+
+    def __init__(self, index: Sector, kry_dim: int):
+        self.index = index
+        self.kry_dim = kry_dim
+        self._act = 0
+
+    def evolve(self, H: Hamiltonian, psi: State, tstp: int, h: float, kry_dim_rt: int = 0) -> None:
+        """psi(tstp + 1) = exp(-i H h) psi(tstp) / ||psi(tstp)|| (sparse_algorithm.hpp:548-562)."""
+        if tstp + 1 >= psi.nt():
+            raise IndexError("evolve writes psi(tstp + 1)")
+        m = kry_dim_rt or self.kry_dim
+        act = C.c_int(0)
+        A.call("qd_arnoldi_evolve", H.handle, psi.handle, tstp, tstp + 1, float(h), m, C.byref(act))
+        self._act = act.value
+
+    def evolve_inplace(self, H: Hamiltonian, psi: State, t: int, h: float, m: int = 0) -> None:
+        act = C.c_int(0)
+        A.call("qd_arnoldi_evolve", H.handle, psi.handle, t, t, float(h), m or self.kry_dim, C.byref(act))
+        self._act = act.value
+
+    def act_dim(self) -> int:
+        return self._act
+
+
 class Arnoldi:
     @staticmethod
     def getLanczosSolver(index: Sector, kry_dim: int, **kw) -> LanczosSolver:
         return LanczosSolver(index, kry_dim, **kw)
+
+    @staticmethod
+    def getSolver(index: Sector, kry_dim: int) -> ArnoldiSolver:
+        return ArnoldiSolver(index, kry_dim)
