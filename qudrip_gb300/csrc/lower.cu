@@ -329,20 +329,26 @@ void ham_lower(qd_ham* H, const qd_term* terms, int nterms, const qd_gate* gates
   P.gates = dgates.p;
   P.nterms = nterms;
 
+  // Start with the smallest column capacity that the leaf count allows and
+  // grow it only if a column overflows (most operators have short columns).
   int cap = 0;
-  const int64_t cap_needed = std::min<int64_t>(leaf_total, std::max<int64_t>(dim, 1));
-  LowerFn fn = pick_lower(std::min<int64_t>(cap_needed, 512), max_leaves, cap);
-  QD_REQUIRE(fn != nullptr, QD_ERR_UNSUPPORTED, "lowering: products with %d leaves are not supported", max_leaves);
-
+  const int64_t cap_bound = std::min<int64_t>(leaf_total, std::max<int64_t>(dim, 1));
   DBuf<int> overflow(1);
-  QD_CUDA(cudaMemsetAsync(overflow.p, 0, sizeof(int), ctx->stream));
   DBuf<int64_t> colptr(dim + 1);
-  QD_CUDA(cudaMemsetAsync(colptr.p, 0, (dim + 1) * 8, ctx->stream));
-  if (dim > 0) fn(ctx, P, 0, colptr.p, nullptr, nullptr, nullptr, overflow.p);
-  int ovf = 0;
-  QD_CUDA(cudaMemcpyAsync(&ovf, overflow.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  QD_CUDA(cudaStreamSynchronize(ctx->stream));
-  QD_REQUIRE(ovf == 0, QD_ERR_OVERFLOW, "lowering: a column has more than %d entries", cap);
+  LowerFn fn = nullptr;
+  for (int64_t try_cap = 32;; try_cap *= 4) {
+    fn = pick_lower(std::min<int64_t>(std::min<int64_t>(try_cap, cap_bound), 512), max_leaves, cap);
+    QD_REQUIRE(fn != nullptr, QD_ERR_UNSUPPORTED, "lowering: products with %d leaves are not supported",
+               max_leaves);
+    QD_CUDA(cudaMemsetAsync(overflow.p, 0, sizeof(int), ctx->stream));
+    QD_CUDA(cudaMemsetAsync(colptr.p, 0, (dim + 1) * 8, ctx->stream));
+    if (dim > 0) fn(ctx, P, 0, colptr.p, nullptr, nullptr, nullptr, overflow.p);
+    int ovf = 0;
+    QD_CUDA(cudaMemcpyAsync(&ovf, overflow.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    QD_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (!ovf) break;
+    QD_REQUIRE(cap < 512 && cap < cap_bound, QD_ERR_OVERFLOW, "lowering: a column has more than %d entries", cap);
+  }
   exclusive_scan_i64(ctx, colptr.p, colptr.p, dim + 1);
   int64_t nnz = 0;
   QD_CUDA(cudaMemcpyAsync(&nnz, colptr.p + dim, 8, cudaMemcpyDeviceToHost, ctx->stream));

@@ -14,7 +14,7 @@
 
 namespace qd {
 
-constexpr int kMaxGrid = 8192;  // upper bound on blocks of any reduction kernel
+constexpr int kMaxGrid = 65536;  // upper bound on blocks of any reduction kernel
 
 // CSR product kernels (qd_ham::spmv_variant; qd_ham_time_spmv accepts them as `spmv`)
 enum SpmvVariant {
@@ -28,7 +28,8 @@ enum SpmvVariant {
   kSpmvRow8 = 107,      // thread per row, 8 loads in flight
   kSpmvRow4Stream = 108,  // as 106 with evict-first matrix loads
   kSpmvRow8Stream = 109,  // as 107 with evict-first matrix loads
-  kSpmvLast = 109,
+  kSpmvRowExact = 110,  // thread per row, groups of 4 loads, exact-count tail
+  kSpmvLast = 110,
 };
 
 constexpr int kSpmvWarps = 4;  // warps per block
@@ -343,6 +344,46 @@ __global__ void __launch_bounds__(256) spmv_rowunroll_kernel(SpmvArgs<MV, VV> A)
 
 namespace qd {
 
+// Thread per row: groups of four (column, value, x) loads in flight, then an
+// exact-count tail, so no FMA slot is spent on predicated-off entries.
+template <typename MV, typename VV>
+__global__ void __launch_bounds__(256) spmv_rowexact_kernel(SpmvArgs<MV, VV> A) {
+  if (A.stop) {
+    const int st = *A.stop;
+    if (st != 0 && st < A.step) return;
+  }
+  VV dotacc = vzero(VV{});
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < A.dim; r += stride) {
+    const int64_t b = A.rowptr[r], e = A.rowptr[r + 1];
+    VV acc = vzero(VV{});
+    int64_t k = b;
+    for (; k + 4 <= e; k += 4) {
+      int32_t c[4];
+      MV v[4];
+      VV xv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        c[u] = ld_plain(A.colidx + k + u);
+        v[u] = ld_plain(A.vals + k + u);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) xv[u] = ld_ro(A.x + c[u]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc = vfma(v[u], xv[u], acc);
+    }
+    for (; k < e; ++k) acc = vfma(ld_plain(A.vals + k), ld_ro(A.x + ld_plain(A.colidx + k)), acc);
+    const VV yv = vscale(spmv_scale(A), acc);
+    A.y[r] = yv;
+    if (A.dotv) dotacc = vdotfma(A.dotv[r], yv, dotacc);
+  }
+  if (A.dotv) spmv_finish_dot(A, dotacc);
+}
+
+}  // namespace qd
+
+namespace qd {
+
 inline int spmv_grid(Ctx* ctx, int64_t dim) {
   const int64_t tiles = (dim + 31) / 32;
   const int64_t want = ceil_div(tiles, kSpmvWarps);
@@ -373,7 +414,7 @@ inline void launch_spmv(Ctx* ctx, const qd_ham* H, const MV* vals, const VV* x, 
   // every grid is capped so the block partials of a fused dot fit in kMaxGrid slots
   const unsigned vg = (unsigned)std::max<int64_t>(
       1, std::min<int64_t>(ceil_div(H->dim, 256 / 4), (int64_t)ctx->num_sms * 8));
-  const unsigned rg = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(H->dim, 256), (int64_t)ctx->num_sms * 8));
+  const unsigned rg = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(H->dim, 256), (int64_t)kMaxGrid));
   const unsigned tg = (unsigned)spmv_grid(ctx, H->dim);
   QD_REQUIRE(vg <= (unsigned)kMaxGrid && rg <= (unsigned)kMaxGrid && tg <= (unsigned)kMaxGrid, QD_ERR_UNSUPPORTED,
              "reduction grid exceeds its partials buffer");
@@ -387,6 +428,7 @@ inline void launch_spmv(Ctx* ctx, const qd_ham* H, const MV* vals, const VV* x, 
     case kSpmvRow8: spmv_rowunroll_kernel<MV, VV, 8, false><<<rg, 256, 0, ctx->stream>>>(A); break;
     case kSpmvRow4Stream: spmv_rowunroll_kernel<MV, VV, 4, true><<<rg, 256, 0, ctx->stream>>>(A); break;
     case kSpmvRow8Stream: spmv_rowunroll_kernel<MV, VV, 8, true><<<rg, 256, 0, ctx->stream>>>(A); break;
+    case kSpmvRowExact: spmv_rowexact_kernel<MV, VV><<<rg, 256, 0, ctx->stream>>>(A); break;
     default: spmv_vector_kernel<MV, VV, 1><<<vg, 256, 0, ctx->stream>>>(A); break;
   }
   QD_CHECK_LAUNCH();
