@@ -316,14 +316,14 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
   const int act = stop ? stop - 1 : kdim;  // expandBasis<1> return value
   QD_REQUIRE(act >= 1, QD_ERR_BREAKDOWN, "Lanczos broke down at the first step (start vector in an "
              "invariant subspace of dimension 1)");
-  std::vector<double> d(act), e(act), z((size_t)act * act, 0.0);
+  std::vector<double> d(act), e(act), z(act), ev(act);
   for (int i = 0; i < act; ++i) {
     d[i] = real_part(alpha[i + 1]);
     e[i] = (i + 1 < act) ? nrm[i + 1] : 0.0;
-    z[(size_t)i * act + i] = 1.0;
   }
-  QD_REQUIRE(tridiag_ql<double>(act, d.data(), e.data(), z.data(), act) == 0, QD_ERR_INVALID,
+  QD_REQUIRE(tridiag_lowest<double>(act, d.data(), e.data(), ev.data(), z.data()) == 0, QD_ERR_INVALID,
              "tridiagonal eigensolver did not converge");
+  d = ev;
   if (o.ritz == QD_RITZ_SECOND_PASS) {
     // getState<1> regenerates v_1..v_act with the same kernels (same bits);
     // run it for the reference's work pattern (act more products).
