@@ -237,6 +237,21 @@ qd_status qd_lanczos_ground(qd_ham *ham, qd_state *psi, int t,
 qd_status qd_arnoldi_evolve(qd_ham *ham, qd_state *psi, int t_in, int t_out,
                             double h, int m, int *act_dim);
 
+/* ------------------------------------------------------------------ */
+/* Batched mixed-precision Lanczos ground states                      */
+/*   many independent getGroundState solves (sparse_algorithm.hpp:    */
+/*   564-585) in one persistent launch                                 */
+/* Each instance: real Hamiltonian `hams[i]` (same context), host start  */
+/* vector v0s[i] (dim doubles), `steps` Lanczos steps with FP32 products  */
+/* and basis, FP64 accumulation of inner products, one full             */
+/* reorthogonalisation pass per step, a device tridiagonal solve and one  */
+/* FP64 Rayleigh-quotient refinement.  out: 8 doubles per instance --     */
+/* lowest Krylov eigenvalue, refined energy, psi^T psi, act_dim,          */
+/* breakdown flag, 3 reserved.                                           */
+/* ------------------------------------------------------------------ */
+qd_status qd_batch_lanczos(qd_ctx *ctx, int ninst, qd_ham *const *hams,
+                           const double *const *v0s, int steps, double *out);
+
 /* Average device time of the sparse product kernel the solvers use on this
  * Hamiltonian (iters back-to-back launches on the context stream, timed with
  * CUDA events), and the kernel's algorithmic HBM bytes per launch:

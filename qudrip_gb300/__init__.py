@@ -9,5 +9,6 @@ from .operators import (II, id, pauli_x, pauli_y, pauli_z, getQbits, getNset, ge
                         getNd, getNh, getBoseGate, getFermiGate, getHopFermiGate, getHopBoseGate,
                         getEmptyOperator, Operator, OperatorSum, QbitsIndex, SectorSpec)
 from .engine import (Context, default_context, Sector, Constrain, LooseConstrain, Hamiltonian,  # noqa: F401
-                     State, getState, apply, start_vector, shuffle_state, LanczosSolver, ArnoldiSolver, Arnoldi)
+                     State, getState, apply, start_vector, shuffle_state, LanczosSolver, ArnoldiSolver, Arnoldi,
+                     batch_lanczos)
 from . import _capi  # noqa: F401

@@ -104,6 +104,7 @@ _SIGNATURES = {
     "qd_ham_autotune": [_P, C.c_int, C.POINTER(C.c_int), _DP],
     "qd_csr_expect_noalloc": [_P, _P, _P, C.c_int64, _P, _P, _P],
     "qd_arnoldi_evolve": [_P, _P, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int)],
+    "qd_batch_lanczos": [_P, C.c_int, C.POINTER(C.c_void_p), C.POINTER(_DP), C.c_int, _DP],
     "qd_status_string": [C.c_int],
     "qd_last_error": [],
     "qd_api_version": [],

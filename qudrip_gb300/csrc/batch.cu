@@ -1,0 +1,360 @@
+// batch.cu -- many Lanczos ground states in one persistent launch.
+//
+// The mixed-precision form of the reference's Lanczos (sparse_algorithm.hpp:
+// 395-425, 564-585) for a packed work list of independent, uneven instances:
+//   * one CTA owns one instance at a time and takes the next one from an
+//     atomic counter; the list is sorted by decreasing nnz (longest first);
+//   * matrix values and Krylov vectors are FP32 and so is the product;
+//   * every inner product keeps FP32 partial sums over at most 64 elements per
+//     thread and adds those partials in FP64 (threads, warps, the block);
+//   * after the three-term step (the reference's local orthogonalisation
+//     against the two previous vectors) the new vector is orthogonalised
+//     once more against the whole stored basis (classical Gram-Schmidt);
+//   * the tridiagonal matrix (FP64) is solved on the device: eigenvalues by
+//     implicit QL, the lowest eigenvector by inverse iteration;
+//   * the Ritz vector gets one FP64 refinement: E = psi^T H psi / psi^T psi with
+//     the FP64 matrix values and FP64 accumulation.
+// No block waits on another block, so nothing can hang: the only shared state
+// is the work counter.
+#include <algorithm>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "batch.cuh"
+#include "krylov.cuh"
+#include "tridiag.cuh"
+
+namespace qd {
+
+constexpr int kBatchThreads = 1024;
+constexpr int kBatchMaxSteps = 256;
+constexpr int kChunk = 64;  // FP32 partial sums cover at most this many elements
+
+struct BlockScratch {
+  double red[kBatchThreads / 32];
+  double bcast;
+  double alpha[kBatchMaxSteps + 2];
+  double beta[kBatchMaxSteps + 2];
+  double y[kBatchMaxSteps + 2];
+  double h[kBatchMaxSteps + 2];
+  int stop;
+  int idx;
+};
+
+// FP64 sum over the block of per-thread values; every thread gets the result.
+__device__ double block_sum_all(double v, BlockScratch& S) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) S.red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    double t = (lane < (int)(blockDim.x >> 5)) ? S.red[lane] : 0.0;
+    t = warp_sum(t);
+    if (lane == 0) S.bcast = t;
+  }
+  __syncthreads();
+  return S.bcast;
+}
+
+// <a, b> with FP32 products and partials over <= kChunk elements, FP64 beyond.
+__device__ double block_dot(const float* __restrict__ a, const float* __restrict__ b, int64_t n, BlockScratch& S) {
+  double dacc = 0.0;
+  float acc = 0.f;
+  int cnt = 0;
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    acc = fmaf(a[i], b[i], acc);
+    if (++cnt == kChunk) {
+      dacc += (double)acc;
+      acc = 0.f;
+      cnt = 0;
+    }
+  }
+  dacc += (double)acc;
+  return block_sum_all(dacc, S);
+}
+
+// w -= c * v
+__device__ void block_axpy(float* __restrict__ w, float c, const float* __restrict__ v, int64_t n) {
+  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) w[i] = fmaf(-c, v[i], w[i]);
+}
+
+// y = H x (FP32 values, FP32 accumulation), one thread per row.
+__device__ void block_spmv_f32(const BatchInst& I, const float* __restrict__ x, float* __restrict__ y) {
+  for (int64_t r = threadIdx.x; r < I.dim; r += blockDim.x) {
+    const int64_t b = I.rowptr[r], e = I.rowptr[r + 1];
+    float acc = 0.f;
+    int64_t k = b;
+    for (; k + 4 <= e; k += 4) {
+      const int32_t c0 = I.colidx[k], c1 = I.colidx[k + 1], c2 = I.colidx[k + 2], c3 = I.colidx[k + 3];
+      const float v0 = I.vals_f[k], v1 = I.vals_f[k + 1], v2 = I.vals_f[k + 2], v3 = I.vals_f[k + 3];
+      const float x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
+      acc = fmaf(v0, x0, acc);
+      acc = fmaf(v1, x1, acc);
+      acc = fmaf(v2, x2, acc);
+      acc = fmaf(v3, x3, acc);
+    }
+    for (; k < e; ++k) acc = fmaf(I.vals_f[k], __ldg(x + I.colidx[k]), acc);
+    y[r] = acc;
+  }
+}
+
+// Lowest eigenpair of tridiag(d, e) (n <= kBatchMaxSteps), one thread:
+// eigenvalues by QL, eigenvector by two steps of inverse iteration with
+// partial pivoting (the reorthogonalised Lanczos matrix has no spurious copies).
+__device__ double device_tridiag_lowest(int n, const double* d_in, const double* e_in, double* y, double* work) {
+  double* d = work;
+  double* e = work + (kBatchMaxSteps + 2);
+  for (int i = 0; i < n; ++i) {
+    d[i] = d_in[i];
+    e[i] = (i + 1 < n) ? e_in[i] : 0.0;
+  }
+  tridiag_ql<double>(n, d, e, nullptr, 0);
+  const double lam = d[0];
+  // (T - sigma I) y = b, sigma just below lam; Gaussian elimination with
+  // partial pivoting on the tridiagonal band (three diagonals + fill-in)
+  double* dl = work + 2 * (kBatchMaxSteps + 2);
+  double* dd = work + 3 * (kBatchMaxSteps + 2);
+  double* du = work + 4 * (kBatchMaxSteps + 2);
+  double* du2 = work + 5 * (kBatchMaxSteps + 2);
+  int* piv = reinterpret_cast<int*>(work + 6 * (kBatchMaxSteps + 2));
+  const double scale = fmax(fabs(lam), 1.0);
+  const double sigma = lam - 1e-10 * scale;
+  for (int i = 0; i < n; ++i) y[i] = 1.0;
+  for (int it = 0; it < 3; ++it) {
+    for (int i = 0; i < n; ++i) {
+      dd[i] = d_in[i] - sigma;
+      du[i] = (i + 1 < n) ? e_in[i] : 0.0;
+      dl[i] = (i + 1 < n) ? e_in[i] : 0.0;
+      du2[i] = 0.0;
+    }
+    // factor
+    for (int i = 0; i < n - 1; ++i) {
+      if (fabs(dd[i]) >= fabs(dl[i])) {
+        piv[i] = i;
+        const double f = (dd[i] != 0.0) ? dl[i] / dd[i] : 0.0;
+        dl[i] = f;
+        dd[i + 1] -= f * du[i];
+      } else {
+        piv[i] = i + 1;
+        const double f = dd[i] / dl[i];
+        dd[i] = dl[i];
+        dl[i] = f;
+        const double t = du[i];
+        du[i] = dd[i + 1];
+        dd[i + 1] = t - f * dd[i + 1];
+        if (i < n - 2) {
+          du2[i] = du[i + 1];
+          du[i + 1] = -f * du[i + 1];
+        }
+      }
+    }
+    // solve L U x = P b
+    for (int i = 0; i < n - 1; ++i) {
+      if (piv[i] == i) {
+        y[i + 1] -= dl[i] * y[i];
+      } else {
+        const double t = y[i];
+        y[i] = y[i + 1];
+        y[i + 1] = t - dl[i] * y[i + 1];
+      }
+    }
+    for (int i = n - 1; i >= 0; --i) {
+      double s = y[i];
+      if (i + 1 < n) s -= du[i] * y[i + 1];
+      if (i + 2 < n) s -= du2[i] * y[i + 2];
+      const double p = (dd[i] != 0.0) ? dd[i] : 1e-300;
+      y[i] = s / p;
+    }
+    double nr = 0.0;
+    for (int i = 0; i < n; ++i) nr += y[i] * y[i];
+    nr = sqrt(nr);
+    for (int i = 0; i < n; ++i) y[i] /= nr;
+  }
+  return lam;
+}
+
+__global__ void __launch_bounds__(kBatchThreads) batch_lanczos_kernel(const BatchInst* __restrict__ list, int ninst,
+                                                                     unsigned* counter, double* tri_work) {
+  __shared__ BlockScratch S;
+  for (;;) {
+    if (threadIdx.x == 0) S.idx = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    const int idx = S.idx;
+    __syncthreads();
+    if (idx >= ninst) return;
+    const BatchInst I = list[idx];
+    const int64_t n = I.dim;
+    float* V = I.V;
+    float* w = I.w;
+    // v_0 = v0 / ||v0||
+    const double nrm0 = sqrt(block_dot(I.v0, I.v0, n, S));
+    const float inv0 = (float)(1.0 / nrm0);
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) V[i] = I.v0[i] * inv0;
+    if (threadIdx.x == 0) S.stop = 0;
+    __syncthreads();
+    int act = I.steps;
+    for (int k = 1; k <= I.steps; ++k) {
+      const float* v1 = V + (int64_t)(k - 1) * I.ld;
+      const float* v2 = (k >= 2) ? V + (int64_t)(k - 2) * I.ld : nullptr;
+      block_spmv_f32(I, v1, w);
+      __syncthreads();
+      double bp = 0.0;
+      if (v2) {
+        bp = block_dot(v2, w, n, S);
+        block_axpy(w, (float)bp, v2, n);
+        __syncthreads();
+      }
+      const double al = block_dot(v1, w, n, S);
+      block_axpy(w, (float)al, v1, n);
+      __syncthreads();
+      // one full Gram-Schmidt pass against v_0 .. v_{k-1}: a warp per basis vector
+      {
+        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        for (int j = warp; j < k; j += nw) {
+          const float* vj = V + (int64_t)j * I.ld;
+          double dacc = 0.0;
+          float acc = 0.f;
+          int cnt = 0;
+          for (int64_t i = lane; i < n; i += 32) {
+            acc = fmaf(vj[i], w[i], acc);
+            if (++cnt == kChunk) {
+              dacc += (double)acc;
+              acc = 0.f;
+              cnt = 0;
+            }
+          }
+          dacc += (double)acc;
+          dacc = warp_sum(dacc);
+          if (lane == 0) S.h[j] = dacc;
+        }
+        __syncthreads();
+        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+          float wi = w[i];
+          for (int j = 0; j < k; ++j) wi = fmaf(-(float)S.h[j], V[(int64_t)j * I.ld + i], wi);
+          w[i] = wi;
+        }
+        __syncthreads();
+      }
+      const double nr = sqrt(block_dot(w, w, n, S));
+      if (threadIdx.x == 0) {
+        S.alpha[k] = al + S.h[k - 1];
+        S.beta[k] = nr;
+        if (nr < 1e-10) S.stop = k;  // breakdown (sparse_algorithm.hpp:421)
+      }
+      __syncthreads();
+      if (S.stop) {
+        act = k - 1;
+        break;
+      }
+      const float inv = (float)(1.0 / nr);
+      float* vk = V + (int64_t)k * I.ld;
+      for (int64_t i = threadIdx.x; i < n; i += blockDim.x) vk[i] = w[i] * inv;
+      __syncthreads();
+    }
+    if (act < 1) act = 1;
+    // lowest Ritz pair of tridiag(alpha_1..act, beta_1..act-1)
+    if (threadIdx.x == 0) {
+      double* work = tri_work + (size_t)blockIdx.x * 8 * (kBatchMaxSteps + 2);
+      const double lam = device_tridiag_lowest(act, S.alpha + 1, S.beta + 1, S.y, work);
+      I.out[0] = lam;
+      I.out[3] = act;
+      I.out[4] = S.stop ? 1 : 0;
+    }
+    __syncthreads();
+    // Ritz vector psi = sum_k y_k v_k (FP32 storage)
+    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+      float acc = 0.f;
+      for (int k = 0; k < act; ++k) acc = fmaf((float)S.y[k], V[(int64_t)k * I.ld + i], acc);
+      I.psi[i] = acc;
+    }
+    __syncthreads();
+    // FP64 refinement: Rayleigh quotient with the FP64 values
+    double num = 0.0, den = 0.0;
+    for (int64_t r = threadIdx.x; r < n; r += blockDim.x) {
+      double hr = 0.0;
+      for (int64_t e = I.rowptr[r]; e < I.rowptr[r + 1]; ++e) hr = fma(I.vals_d[e], (double)I.psi[I.colidx[e]], hr);
+      const double pr = (double)I.psi[r];
+      num = fma(pr, hr, num);
+      den = fma(pr, pr, den);
+    }
+    num = block_sum_all(num, S);
+    den = block_sum_all(den, S);
+    if (threadIdx.x == 0) {
+      I.out[1] = num / den;
+      I.out[2] = den;
+    }
+    __syncthreads();
+  }
+}
+
+void batch_lanczos(Ctx* ctx, qd_ham* const* hams, const double* const* v0s, int ninst, int steps, double* out) {
+  QD_REQUIRE(ninst >= 1, QD_ERR_INVALID, "empty batch");
+  QD_REQUIRE(steps >= 1 && steps <= kBatchMaxSteps, QD_ERR_INVALID, "steps must be in 1..%d", kBatchMaxSteps);
+  std::vector<int> order(ninst);
+  std::iota(order.begin(), order.end(), 0);
+  for (int i = 0; i < ninst; ++i) {
+    QD_REQUIRE(hams[i] && v0s[i], QD_ERR_INVALID, "instance %d: null argument", i);
+    QD_REQUIRE(hams[i]->flags & QD_HAM_REAL, QD_ERR_UNSUPPORTED,
+               "instance %d: the batched mixed-precision solver needs a real Hamiltonian", i);
+    QD_REQUIRE(hams[i]->ctx == ctx, QD_ERR_INVALID, "instance %d: Hamiltonian of another context", i);
+  }
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hams[a]->nnz > hams[b]->nnz; });
+  // one arena for every instance's start vector, basis, work vector, Ritz vector
+  std::vector<int64_t> off_v0(ninst), off_V(ninst), off_w(ninst), off_psi(ninst);
+  int64_t total = 0;
+  for (int i = 0; i < ninst; ++i) {
+    const int64_t ld = (hams[i]->dim + 31) / 32 * 32;
+    off_v0[i] = total;
+    total += ld;
+    off_V[i] = total;
+    total += (int64_t)(steps + 1) * ld;
+    off_w[i] = total;
+    total += ld;
+    off_psi[i] = total;
+    total += ld;
+  }
+  DBuf<float> arena(total);
+  DBuf<double> dout((size_t)ninst * 8);
+  std::vector<float> h32;
+  for (int i = 0; i < ninst; ++i) {
+    h32.assign(v0s[i], v0s[i] + hams[i]->dim);
+    for (int64_t q = 0; q < hams[i]->dim; ++q) h32[q] = (float)v0s[i][q];
+    QD_CUDA(cudaMemcpyAsync(arena.p + off_v0[i], h32.data(), hams[i]->dim * sizeof(float), cudaMemcpyHostToDevice,
+                            ctx->stream));
+    QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  std::vector<BatchInst> list(ninst);
+  for (int q = 0; q < ninst; ++q) {
+    const int i = order[q];
+    const qd_ham* H = hams[i];
+    BatchInst& I = list[q];
+    std::memset(&I, 0, sizeof(I));
+    I.dim = H->dim;
+    I.steps = steps;
+    I.ld = (H->dim + 31) / 32 * 32;
+    I.rowptr = H->rowptr.p;
+    I.colidx = H->colidx.p;
+    I.vals_f = H->vals_f.p;
+    I.vals_d = H->vals_r.p;
+    I.v0 = arena.p + off_v0[i];
+    I.V = arena.p + off_V[i];
+    I.w = arena.p + off_w[i];
+    I.psi = arena.p + off_psi[i];
+    I.out = dout.p + (size_t)i * 8;
+  }
+  DBuf<BatchInst> dlist(ninst);
+  QD_CUDA(cudaMemcpyAsync(dlist.p, list.data(), ninst * sizeof(BatchInst), cudaMemcpyHostToDevice, ctx->stream));
+  DBuf<unsigned> counter(1);
+  QD_CUDA(cudaMemsetAsync(counter.p, 0, sizeof(unsigned), ctx->stream));
+  const int grid = std::min(ninst, ctx->num_sms);
+  DBuf<double> tri_work((size_t)grid * 8 * (kBatchMaxSteps + 2));
+  batch_lanczos_kernel<<<grid, kBatchThreads, 0, ctx->stream>>>(dlist.p, ninst, counter.p, tri_work.p);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  QD_CUDA(cudaMemcpyAsync(out, dout.p, (size_t)ninst * 8 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+}  // namespace qd

@@ -3,6 +3,7 @@
 #include <cstring>
 #include <string>
 
+#include "batch.cuh"
 #include "evolve.cuh"
 #include "ham.cuh"
 #include "krylov.cuh"
@@ -433,6 +434,15 @@ qd_status qd_arnoldi_evolve(qd_ham* ham, qd_state* psi, int t_in, int t_out, dou
     QD_REQUIRE(t_in >= 0 && t_in < psi->nt && t_out >= 0 && t_out < psi->nt, QD_ERR_INVALID, "bad column");
     DeviceGuard dg(ham->ctx->device);
     arnoldi_evolve(ham, psi->col(t_in), psi->col(t_out), h, m, act_dim);
+  });
+}
+
+qd_status qd_batch_lanczos(qd_ctx* ctx, int ninst, qd_ham* const* hams, const double* const* v0s, int steps,
+                           double* out) {
+  return guard([&] {
+    QD_REQUIRE(ctx && hams && v0s && out, QD_ERR_INVALID, "null argument");
+    DeviceGuard dg(ctx->device);
+    batch_lanczos(ctx, hams, v0s, ninst, steps, out);
   });
 }
 

@@ -340,3 +340,19 @@ class Arnoldi:
     @staticmethod
     def getSolver(index: Sector, kry_dim: int) -> ArnoldiSolver:
         return ArnoldiSolver(index, kry_dim)
+
+
+def batch_lanczos(hams, v0s, steps: int, ctx: Optional[Context] = None) -> np.ndarray:
+    """Many ground states in one persistent launch (mixed precision, FP64 refinement).
+
+    Returns an (ninst, 8) array: lowest Krylov eigenvalue, refined FP64 energy,
+    psi^T psi, act_dim, breakdown flag, 3 reserved.
+    """
+    n = len(hams)
+    ctx = ctx or hams[0].ctx
+    hp = (C.c_void_p * n)(*[h.handle.value for h in hams])
+    keep = [np.ascontiguousarray(v, dtype=np.float64) for v in v0s]
+    vp = (A._DP * n)(*[k.ctypes.data_as(A._DP) for k in keep])
+    out = np.zeros((n, 8))
+    A.call("qd_batch_lanczos", ctx.handle, n, hp, vp, steps, out.ctypes.data_as(A._DP))
+    return out

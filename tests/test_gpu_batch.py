@@ -1,0 +1,58 @@
+"""Batched mixed-precision Lanczos vs the FP64 oracle, instance by instance."""
+import numpy as np
+import pytest
+
+import oracle as O
+import qudrip_gb300 as q
+from qudrip_gb300 import chains
+
+pytestmark = pytest.mark.gpu
+
+DE_TOL = 1e-8  # relative, refined energy vs the FP64 oracle
+
+
+def disorder_instances(n, Ls, seed):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for i in range(n):
+        L = int(rng.choice(Ls))
+        h = rng.uniform(-2.0, 2.0, L)
+        out.append((L, h))
+    return out
+
+
+def test_batch_matches_fp64_oracle(ctx):
+    inst = disorder_instances(12, [10, 12, 14], 3)
+    hams, v0s, oracles = [], [], []
+    for L, h in inst:
+        spec, ham = chains.xxz_chain(L, 1.0, 1.0, True, h)
+        sec = q.Sector(spec.index, spec.constraints)
+        hams.append(sec.lower(ham))
+        v0 = q.start_vector(sec.dim, 100 + L)
+        v0s.append(v0)
+        oh = O.Ham(O.Sector(spec), ham)
+        oracles.append(oh.lanczos_ground(v0, 80))
+        hams[-1]._keep = sec
+    out = q.batch_lanczos(hams, v0s, 80)
+    for i, o in enumerate(oracles):
+        ref = o["ritz"]
+        assert abs(out[i, 1] - ref) <= DE_TOL * abs(ref), (i, out[i], ref)
+        assert abs(out[i, 0] - ref) <= 1e-5 * abs(ref)  # FP32 Krylov eigenvalue before refinement
+        assert out[i, 3] == 80 and out[i, 4] == 0
+
+
+def test_batch_small_spaces_break_down(ctx):
+    # dims below the step count: the recurrence stops, the result is still exact
+    hams, v0s, exact = [], [], []
+    for L in (4, 6, 8):
+        spec, ham = chains.xxz_chain(L, 1.0, 0.5, True, np.linspace(-1, 1, L))
+        sec = q.Sector(spec.index, spec.constraints)
+        H = sec.lower(ham)
+        H._keep = sec
+        hams.append(H)
+        v0s.append(q.start_vector(sec.dim, L))
+        exact.append(np.linalg.eigvalsh(H.scipy().toarray())[0])
+    out = q.batch_lanczos(hams, v0s, 40)
+    for i, e in enumerate(exact):
+        assert out[i, 4] == 1
+        assert abs(out[i, 1] - e) <= 1e-9 * abs(e)
