@@ -27,7 +27,7 @@
 
 namespace qd {
 
-constexpr int kBatchThreads = 1024;
+constexpr int kBatchThreads = 512;  // two CTAs per SM
 constexpr int kBatchMaxSteps = 256;
 constexpr int kChunk = 64;  // FP32 partial sums cover at most this many elements
 
@@ -59,25 +59,46 @@ __device__ double block_sum_all(double v, BlockScratch& S) {
 }
 
 // <a, b> with FP32 products and partials over <= kChunk elements, FP64 beyond.
+// a and b are 16-byte aligned (every vector starts on a 32-element boundary).
 __device__ double block_dot(const float* __restrict__ a, const float* __restrict__ b, int64_t n, BlockScratch& S) {
   double dacc = 0.0;
   float acc = 0.f;
   int cnt = 0;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-    acc = fmaf(a[i], b[i], acc);
-    if (++cnt == kChunk) {
+  const int64_t n4 = n >> 2;
+  const float4* a4 = reinterpret_cast<const float4*>(a);
+  const float4* b4 = reinterpret_cast<const float4*>(b);
+  for (int64_t i = threadIdx.x; i < n4; i += blockDim.x) {
+    const float4 x = a4[i], y = b4[i];
+    acc = fmaf(x.x, y.x, acc);
+    acc = fmaf(x.y, y.y, acc);
+    acc = fmaf(x.z, y.z, acc);
+    acc = fmaf(x.w, y.w, acc);
+    if (++cnt == kChunk / 4) {
       dacc += (double)acc;
       acc = 0.f;
       cnt = 0;
     }
   }
+  for (int64_t i = (n4 << 2) + threadIdx.x; i < n; i += blockDim.x) acc = fmaf(a[i], b[i], acc);
   dacc += (double)acc;
   return block_sum_all(dacc, S);
 }
 
 // w -= c * v
 __device__ void block_axpy(float* __restrict__ w, float c, const float* __restrict__ v, int64_t n) {
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) w[i] = fmaf(-c, v[i], w[i]);
+  const int64_t n4 = n >> 2;
+  float4* w4 = reinterpret_cast<float4*>(w);
+  const float4* v4 = reinterpret_cast<const float4*>(v);
+  for (int64_t i = threadIdx.x; i < n4; i += blockDim.x) {
+    float4 x = w4[i];
+    const float4 y = v4[i];
+    x.x = fmaf(-c, y.x, x.x);
+    x.y = fmaf(-c, y.y, x.y);
+    x.z = fmaf(-c, y.z, x.z);
+    x.w = fmaf(-c, y.w, x.w);
+    w4[i] = x;
+  }
+  for (int64_t i = (n4 << 2) + threadIdx.x; i < n; i += blockDim.x) w[i] = fmaf(-c, v[i], w[i]);
 }
 
 // y = H x (FP32 values, FP32 accumulation), one thread per row.
@@ -175,7 +196,7 @@ __device__ double device_tridiag_lowest(int n, const double* d_in, const double*
   return lam;
 }
 
-__global__ void __launch_bounds__(kBatchThreads) batch_lanczos_kernel(const BatchInst* __restrict__ list, int ninst,
+__global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const BatchInst* __restrict__ list, int ninst,
                                                                      unsigned* counter, double* tri_work) {
   __shared__ BlockScratch S;
   for (;;) {
@@ -212,25 +233,46 @@ __global__ void __launch_bounds__(kBatchThreads) batch_lanczos_kernel(const Batc
       // one full Gram-Schmidt pass against v_0 .. v_{k-1}: a warp per basis vector
       {
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        const int64_t n4 = n >> 2;
+        const float4* w4 = reinterpret_cast<const float4*>(w);
         for (int j = warp; j < k; j += nw) {
           const float* vj = V + (int64_t)j * I.ld;
+          const float4* vj4 = reinterpret_cast<const float4*>(vj);
           double dacc = 0.0;
           float acc = 0.f;
           int cnt = 0;
-          for (int64_t i = lane; i < n; i += 32) {
-            acc = fmaf(vj[i], w[i], acc);
-            if (++cnt == kChunk) {
+          for (int64_t i = lane; i < n4; i += 32) {
+            const float4 x = vj4[i], y = w4[i];
+            acc = fmaf(x.x, y.x, acc);
+            acc = fmaf(x.y, y.y, acc);
+            acc = fmaf(x.z, y.z, acc);
+            acc = fmaf(x.w, y.w, acc);
+            if (++cnt == kChunk / 4) {
               dacc += (double)acc;
               acc = 0.f;
               cnt = 0;
             }
           }
+          for (int64_t i = (n4 << 2) + lane; i < n; i += 32) acc = fmaf(vj[i], w[i], acc);
           dacc += (double)acc;
           dacc = warp_sum(dacc);
           if (lane == 0) S.h[j] = dacc;
         }
         __syncthreads();
-        for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+        float4* wm4 = reinterpret_cast<float4*>(w);
+        for (int64_t i = threadIdx.x; i < n4; i += blockDim.x) {
+          float4 x = wm4[i];
+          for (int j = 0; j < k; ++j) {
+            const float c = -(float)S.h[j];
+            const float4 y = reinterpret_cast<const float4*>(V + (int64_t)j * I.ld)[i];
+            x.x = fmaf(c, y.x, x.x);
+            x.y = fmaf(c, y.y, x.y);
+            x.z = fmaf(c, y.z, x.z);
+            x.w = fmaf(c, y.w, x.w);
+          }
+          wm4[i] = x;
+        }
+        for (int64_t i = (n4 << 2) + threadIdx.x; i < n; i += blockDim.x) {
           float wi = w[i];
           for (int j = 0; j < k; ++j) wi = fmaf(-(float)S.h[j], V[(int64_t)j * I.ld + i], wi);
           w[i] = wi;
@@ -241,11 +283,14 @@ __global__ void __launch_bounds__(kBatchThreads) batch_lanczos_kernel(const Batc
       if (threadIdx.x == 0) {
         S.alpha[k] = al + S.h[k - 1];
         S.beta[k] = nr;
-        if (nr < 1e-10) S.stop = k;  // breakdown (sparse_algorithm.hpp:421)
+        // breakdown (sparse_algorithm.hpp:421): the reference's 1e-10, or the
+        // FP32 resolution of the recurrence, or an exhausted space
+        const double scale = fabs(al) + fabs(bp) + (k >= 2 ? S.beta[k - 1] : 0.0);
+        if (nr < 1e-10 || nr < 1e-5 * scale || k >= n) S.stop = k;
       }
       __syncthreads();
       if (S.stop) {
-        act = k - 1;
+        act = k;  // v_0 .. v_{k-1} span an invariant subspace: T_k is exact
         break;
       }
       const float inv = (float)(1.0 / nr);
@@ -348,7 +393,7 @@ void batch_lanczos(Ctx* ctx, qd_ham* const* hams, const double* const* v0s, int 
   QD_CUDA(cudaMemcpyAsync(dlist.p, list.data(), ninst * sizeof(BatchInst), cudaMemcpyHostToDevice, ctx->stream));
   DBuf<unsigned> counter(1);
   QD_CUDA(cudaMemsetAsync(counter.p, 0, sizeof(unsigned), ctx->stream));
-  const int grid = std::min(ninst, ctx->num_sms);
+  const int grid = std::min(ninst, 2 * ctx->num_sms);
   DBuf<double> tri_work((size_t)grid * 8 * (kBatchMaxSteps + 2));
   batch_lanczos_kernel<<<grid, kBatchThreads, 0, ctx->stream>>>(dlist.p, ninst, counter.p, tri_work.p);
   QD_CHECK_LAUNCH();

@@ -15,6 +15,9 @@
 // basis -- the values the reference's second Lanczos pass (getState<1>)
 // regenerates, obtained without repeating the kry_dim products.
 #include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -302,7 +305,11 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
 
+  const bool timing = std::getenv("QD_TIMING") != nullptr;
+  const auto host_t0 = std::chrono::steady_clock::now();
+  if (timing) QD_CUDA(cudaEventRecord(ctx->events[12], ctx->stream));
   B.run_graph(ctx, [&]() { lanczos_run<MV, VV>(H, vals, B, kdim, W); });
+  if (timing) QD_CUDA(cudaEventRecord(ctx->events[13], ctx->stream));
   int matvecs = kdim;
 
   std::vector<VV> alpha(kdim + 1);
@@ -344,6 +351,14 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (timing) {
+    float g = 0.f;
+    QD_CUDA(cudaEventElapsedTime(&g, ctx->events[12], ctx->events[13]));
+    const double host_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_t0).count();
+    std::fprintf(stderr, "[qd timing] lanczos n=%lld k=%d: recurrence %.3f ms (%.1f us/step), whole solve %.3f ms\n",
+                 (long long)n, kdim, g, 1e3 * g / kdim, host_ms);
+  }
   if (evals_out) std::memcpy(evals_out, d.data(), act * sizeof(double));
   res->act_dim = act;
   res->breakdown = stop ? 1 : 0;

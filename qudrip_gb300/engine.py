@@ -9,6 +9,7 @@ library; nothing here computes on the CPU.  Names follow the reference:
 from __future__ import annotations
 
 import ctypes as C
+import atexit
 import threading
 from typing import Optional
 
@@ -40,7 +41,7 @@ class Context:
         return s.value or 0
 
     def close(self):
-        if self.handle:
+        if self.handle and not _SHUTDOWN[0]:
             A.lib().qd_ctx_destroy(self.handle)
             self.handle = C.c_void_p()
 
@@ -52,6 +53,10 @@ class Context:
 
 
 _default = None
+# At interpreter exit the handles are left to the process teardown: Python may
+# finalise a context before the objects made from it.
+_SHUTDOWN = [False]
+atexit.register(lambda: _SHUTDOWN.__setitem__(0, True))
 _default_lock = threading.Lock()
 
 
@@ -102,7 +107,7 @@ class Sector(SectorSpec):
         return Hamiltonian(self, opsum)
 
     def close(self):
-        if getattr(self, "handle", None):
+        if getattr(self, "handle", None) and not _SHUTDOWN[0]:
             A.lib().qd_sector_destroy(self.handle)
             self.handle = C.c_void_p()
 
@@ -172,7 +177,7 @@ class Hamiltonian:
         return sp.csr_matrix((vals, idx, ptr), shape=(self.dim, self.dim))
 
     def close(self):
-        if getattr(self, "handle", None):
+        if getattr(self, "handle", None) and not _SHUTDOWN[0]:
             A.lib().qd_ham_destroy(self.handle)
             self.handle = C.c_void_p()
 
@@ -233,7 +238,7 @@ class State:
         return complex(out[0], out[1])
 
     def close(self):
-        if getattr(self, "handle", None):
+        if getattr(self, "handle", None) and not _SHUTDOWN[0]:
             A.lib().qd_state_destroy(self.handle)
             self.handle = C.c_void_p()
 
