@@ -402,7 +402,7 @@ def spmv_only(args, local):
         nb = C.c_double(0)
         A.call("qd_ham_time_spmv", H.handle, k, args.iters, C.byref(ms), C.byref(nb))
         gbs = nb.value / (ms.value * 1e-3) / 1e9
-        print(json.dumps({"kernel": A.SPMV_KERNELS[k], "id": k, "ms": ms.value, "GBps": gbs,
+        print(json.dumps({"kernel": A.SPMV_KERNELS.get(k % 1000, "") + ("+dot" if 2000 <= k < 3000 else "") + ({3001: "lanczos_k2", 3002: "lanczos_k3"}.get(k, "")), "id": k, "ms": ms.value, "GBps": gbs,
                           "frac": gbs / hbm_peak, "matvecs_per_s": 1e3 / ms.value}))
     return 0
 

@@ -255,7 +255,9 @@ qd_status qd_batch_lanczos(qd_ctx *ctx, int ninst, qd_ham *const *hams,
 /* Average device time of the sparse product kernel the solvers use on this
  * Hamiltonian (iters back-to-back launches on the context stream, timed with
  * CUDA events), and the kernel's algorithmic HBM bytes per launch:
- * CSR: nnz*(value + 4) + (dim+1)*8 + dim*(x + y) bytes. */
+ * CSR: nnz*(value + 4) + (dim+1)*8 + dim*(x + y) bytes.  Diagnostic codes:
+ * 2000 + kernel times the product with the fused Lanczos dot epilogue; 3001
+ * and 3002 time the two Lanczos vector kernels alone (real Hamiltonians). */
 qd_status qd_ham_time_spmv(qd_ham *ham, int spmv, int iters, double *avg_ms,
                            double *bytes_per_launch);
 

@@ -420,8 +420,10 @@ qd_status qd_lanczos_ground(qd_ham* ham, qd_state* psi, int t, const qd_lanczos_
 qd_status qd_ham_time_spmv(qd_ham* ham, int spmv, int iters, double* avg_ms, double* bytes_per_launch) {
   return guard([&] {
     QD_REQUIRE(ham && avg_ms && bytes_per_launch && iters >= 1, QD_ERR_INVALID, "bad argument");
-    QD_REQUIRE(spmv == QD_SPMV_CSR || (spmv >= kSpmvTile && spmv <= kSpmvLast), QD_ERR_UNSUPPORTED,
-               "qd_ham_time_spmv: unknown product kernel %d", spmv);
+    const bool plain = spmv == QD_SPMV_CSR || (spmv >= kSpmvTile && spmv <= kSpmvLast);
+    const bool fused = spmv >= 2000 + kSpmvTile && spmv <= 2000 + kSpmvLast;
+    const bool vec = spmv == 3001 || spmv == 3002;
+    QD_REQUIRE(plain || fused || vec, QD_ERR_UNSUPPORTED, "qd_ham_time_spmv: unknown kernel code %d", spmv);
     DeviceGuard dg(ham->ctx->device);
     time_spmv(ham, spmv, iters, avg_ms, bytes_per_launch);
   });

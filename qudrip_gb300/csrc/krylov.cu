@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(kVecThreads) lz_k3_kernel(int64_t n, int* stop
     const double nr = sqrt(*nrm2);
     *nrm = nr;
     *sk = 1.0 / nr;
-    if (nr < 1e-10 && *stop == 0) *stop = step;  // sparse_algorithm.hpp:421
+    if (nr < 1e-10 && stop && *stop == 0) *stop = step;  // sparse_algorithm.hpp:421
   }
 }
 
@@ -225,14 +225,43 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   const size_t vb = real ? sizeof(double) : sizeof(cplx);
   DBuf<char> x((n + 32) * vb), y((n + 32) * vb);
   QD_CUDA(cudaMemsetAsync(x.p, 0, x.bytes(), ctx->stream));
-  const int variant = (spmv >= kSpmvTile) ? spmv : -1;
+  // diagnostic codes: 2000 + kernel = product with the fused Lanczos dot;
+  // 3001 / 3002 = the Lanczos vector kernels K2 / K3 alone (real path)
+  const int mode = spmv >= 3000 ? 3 : (spmv >= 2000 ? 2 : 1);
+  const int code = spmv % 1000;
+  const int variant = (mode == 2) ? spmv - 2000 : ((spmv >= kSpmvTile && mode == 1) ? spmv : -1);
+  DBuf<char> z((n + 32) * vb), scal(64);
+  QD_CUDA(cudaMemsetAsync(z.p, 0, z.bytes(), ctx->stream));
+  QD_CUDA(cudaMemsetAsync(scal.p, 0, 64, ctx->stream));
+  const double one = 1.0;
+  QD_CUDA(cudaMemcpyAsync(scal.p, &one, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  const double* s1 = (const double*)scal.p;
   auto launch = [&]() {
+    if (mode == 3) {
+      QD_REQUIRE(real, QD_ERR_UNSUPPORTED, "vector-kernel timing is for real Hamiltonians");
+      const int vg = vec_grid(ctx, n);
+      double* d = (double*)scal.p;
+      if (code == 1)
+        lz_k2_kernel<double><<<vg, kVecThreads, 0, ctx->stream>>>(n, nullptr, 0, (double*)y.p, (const double*)x.p,
+                                                                   (const double*)z.p, s1, s1, d + 1, d + 2,
+                                                                   W.red_d(2));
+      else
+        lz_k3_kernel<double><<<vg, kVecThreads, 0, ctx->stream>>>(n, nullptr, 0, (const double*)y.p,
+                                                                   (const double*)x.p, s1, d + 1, (double*)z.p,
+                                                                   d + 3, d + 4, d + 5, W.red_d(3));
+      QD_CHECK_LAUNCH();
+      QD_LAUNCHED(ctx);
+      return;
+    }
+    const bool dot = (mode == 2);
     if (real)
-      launch_spmv<double, double>(ctx, H, H->vals_r.p, (const double*)x.p, (double*)y.p, 1.0, nullptr,
-                                  W.red_d(0), nullptr, nullptr, 0, variant);
+      launch_spmv<double, double>(ctx, H, H->vals_r.p, (const double*)x.p, (double*)y.p, 1.0,
+                                  dot ? (const double*)z.p : nullptr, W.red_d(1), dot ? (double*)scal.p + 6 : nullptr,
+                                  nullptr, 0, variant, dot ? s1 : nullptr, dot ? s1 : nullptr);
     else
-      launch_spmv<cplx, cplx>(ctx, H, H->vals_c.p, (const cplx*)x.p, (cplx*)y.p, 1.0, nullptr, W.red_c(0),
-                              nullptr, nullptr, 0, variant);
+      launch_spmv<cplx, cplx>(ctx, H, H->vals_c.p, (const cplx*)x.p, (cplx*)y.p, 1.0,
+                              dot ? (const cplx*)z.p : nullptr, W.red_c(1), dot ? (cplx*)scal.p + 2 : nullptr,
+                              nullptr, 0, variant, dot ? s1 : nullptr, dot ? s1 : nullptr);
   };
   for (int i = 0; i < 3; ++i) launch();
   QD_CUDA(cudaEventRecord(ctx->events[14], ctx->stream));

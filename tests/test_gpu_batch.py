@@ -44,7 +44,7 @@ def test_batch_matches_fp64_oracle(ctx):
 def test_batch_small_spaces_break_down(ctx):
     # dims below the step count: the recurrence stops, the result is still exact
     hams, v0s, exact = [], [], []
-    for L in (4, 6, 8):
+    for L in (4, 6, 8):  # dims 6 and 20 are exhausted within 40 steps, 70 is not
         spec, ham = chains.xxz_chain(L, 1.0, 0.5, True, np.linspace(-1, 1, L))
         sec = q.Sector(spec.index, spec.constraints)
         H = sec.lower(ham)
@@ -54,5 +54,5 @@ def test_batch_small_spaces_break_down(ctx):
         exact.append(np.linalg.eigvalsh(H.scipy().toarray())[0])
     out = q.batch_lanczos(hams, v0s, 40)
     for i, e in enumerate(exact):
-        assert out[i, 4] == 1
+        assert out[i, 4] == (1 if i < 2 else 0)
         assert abs(out[i, 1] - e) <= 1e-9 * abs(e)
