@@ -179,12 +179,18 @@ __global__ void __launch_bounds__(kVecThreads) cdot_kernel(int64_t n, const cplx
 Workspace::Workspace(Ctx* c) : ctx(c) {
   partials_d.alloc(kMaxGrid);
   partials_c.alloc(kMaxGrid);
-  tickets.alloc(8);
-  QD_CUDA(cudaMemsetAsync(tickets.p, 0, 8 * sizeof(unsigned), c->stream));
+  gpart_d.alloc(kRedMaxGroups);
+  gpart_c.alloc(kRedMaxGroups);
+  tickets.alloc(8 * (1 + kRedMaxGroups));
+  QD_CUDA(cudaMemsetAsync(tickets.p, 0, tickets.bytes(), c->stream));
 }
 
-GridRed<double> Workspace::red_d(int slot) { return GridRed<double>{partials_d.p, tickets.p + slot}; }
-GridRed<cplx> Workspace::red_c(int slot) { return GridRed<cplx>{partials_c.p, tickets.p + slot}; }
+GridRed<double> Workspace::red_d(int slot) {
+  return GridRed<double>{partials_d.p, tickets.p + (size_t)slot * (1 + kRedMaxGroups), gpart_d.p};
+}
+GridRed<cplx> Workspace::red_c(int slot) {
+  return GridRed<cplx>{partials_c.p, tickets.p + (size_t)slot * (1 + kRedMaxGroups), gpart_c.p};
+}
 
 Workspace& ham_workspace(qd_ham* H) {
   if (!H->ws) H->ws.reset(new Workspace(H->ctx));

@@ -77,8 +77,8 @@ struct LanczosBuffers {
 
 struct Workspace {
   Ctx* ctx;
-  DBuf<double> partials_d;
-  DBuf<cplx> partials_c;
+  DBuf<double> partials_d, gpart_d;
+  DBuf<cplx> partials_c, gpart_c;
   DBuf<unsigned> tickets;
   LanczosBuffers<double> lz_d;
   LanczosBuffers<cplx> lz_c;

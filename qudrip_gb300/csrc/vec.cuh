@@ -88,16 +88,25 @@ __device__ __forceinline__ T block_sum(T v, T* smem) {
 }
 
 // Grid reduction slot: per-block partials and a ticket counter (zero at rest).
+// Grid reduction slot: per-block partials and ticket counters (zero at rest).
+// With `gpart` set the reduction is two-level: blocks are grouped by
+// kRedGroup, the last block of each group sums the group (ticket[1 + group]),
+// the last group sums the group totals (ticket[0]).  Without it the last
+// block sums every block partial.
+constexpr int kRedGroup = 64;
+constexpr int kRedMaxGroups = 1024;
+
 template <typename T>
 struct GridRed {
   T* partials;
   unsigned int* ticket;
+  T* gpart = nullptr;
 };
 
 // Every thread of every block calls this with its value; the last block to
 // arrive returns true in all its threads and thread 0 of it writes *total.
 template <typename T>
-__device__ __forceinline__ bool grid_sum(T v, GridRed<T> R, T* total) {
+__device__ __forceinline__ bool grid_sum_flat(T v, GridRed<T> R, T* total) {
   __shared__ T smem[32];
   __shared__ bool last;
   const T b = block_sum(v, smem);
@@ -113,6 +122,45 @@ __device__ __forceinline__ bool grid_sum(T v, GridRed<T> R, T* total) {
   T acc = vzero(v);
   for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) acc = vadd(acc, ld_cg(R.partials + i));
   const T tot = block_sum(acc, smem);
+  if (threadIdx.x == 0) {
+    *total = tot;
+    *R.ticket = 0u;
+  }
+  return true;
+}
+
+template <typename T>
+__device__ __forceinline__ bool grid_sum(T v, GridRed<T> R, T* total) {
+  if (!R.gpart) return grid_sum_flat(v, R, total);
+  __shared__ T smem2[32];
+  __shared__ bool last2;
+  const T b = block_sum(v, smem2);
+  const unsigned group = blockIdx.x / kRedGroup;
+  const unsigned gsize = min((unsigned)kRedGroup, gridDim.x - group * kRedGroup);
+  const unsigned ngroups = (gridDim.x + kRedGroup - 1) / kRedGroup;
+  if (threadIdx.x == 0) {
+    R.partials[blockIdx.x] = b;
+    __threadfence();
+    last2 = (atomicAdd(R.ticket + 1 + group, 1u) == gsize - 1);
+  }
+  __syncthreads();
+  if (!last2) return false;
+  __threadfence();
+  T acc = vzero(v);
+  for (unsigned i = threadIdx.x; i < gsize; i += blockDim.x) acc = vadd(acc, ld_cg(R.partials + group * kRedGroup + i));
+  const T gs = block_sum(acc, smem2);
+  if (threadIdx.x == 0) {
+    R.gpart[group] = gs;
+    R.ticket[1 + group] = 0u;
+    __threadfence();
+    last2 = (atomicAdd(R.ticket, 1u) == ngroups - 1);
+  }
+  __syncthreads();
+  if (!last2) return false;
+  __threadfence();
+  T acc2 = vzero(v);
+  for (unsigned i = threadIdx.x; i < ngroups; i += blockDim.x) acc2 = vadd(acc2, ld_cg(R.gpart + i));
+  const T tot = block_sum(acc2, smem2);
   if (threadIdx.x == 0) {
     *total = tot;
     *R.ticket = 0u;
