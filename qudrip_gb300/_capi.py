@@ -38,7 +38,7 @@ QD_RITZ_STORED_BASIS = 0
 QD_RITZ_SECOND_PASS = 1
 SPMV_KERNELS = {100: "tile", 101: "balanced", 102: "vector2", 103: "vector4", 104: "vector8",
                 105: "scalar", 106: "row4", 107: "row8", 108: "row4_stream", 109: "row8_stream",
-                110: "row_exact"}
+                110: "row_exact", 111: "row_sorted"}
 
 
 class qd_cq_term(C.Structure):

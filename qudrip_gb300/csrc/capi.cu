@@ -425,6 +425,7 @@ qd_status qd_ham_time_spmv(qd_ham* ham, int spmv, int iters, double* avg_ms, dou
     const bool vec = spmv == 3001 || spmv == 3002;
     QD_REQUIRE(plain || fused || vec, QD_ERR_UNSUPPORTED, "qd_ham_time_spmv: unknown kernel code %d", spmv);
     DeviceGuard dg(ham->ctx->device);
+    if (spmv % 1000 == kSpmvRowSorted) ham_ensure_row_order(ham);
     time_spmv(ham, spmv, iters, avg_ms, bytes_per_launch);
   });
 }
@@ -451,6 +452,8 @@ qd_status qd_batch_lanczos(qd_ctx* ctx, int ninst, qd_ham* const* hams, const do
 qd_status qd_ham_set_spmv_kernel(qd_ham* ham, int kernel) {
   return guard([&] {
     QD_REQUIRE(ham && kernel >= kSpmvTile && kernel <= kSpmvLast, QD_ERR_INVALID, "unknown product kernel");
+    DeviceGuard dg(ham->ctx->device);
+    if (kernel == kSpmvRowSorted) ham_ensure_row_order(ham);
     ham->spmv_variant = kernel;
   });
 }
@@ -461,6 +464,7 @@ qd_status qd_ham_autotune(qd_ham* ham, int iters, int* chosen, double* best_ms) 
     DeviceGuard dg(ham->ctx->device);
     double best = 1e300, bytes = 0;
     int pick = ham->spmv_variant;
+    ham_ensure_row_order(ham);
     for (int v = kSpmvTile; v <= kSpmvLast; ++v) {
       double ms = 0;
       time_spmv(ham, v, iters, &ms, &bytes);

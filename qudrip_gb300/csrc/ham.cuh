@@ -72,6 +72,7 @@ struct qd_ham {
   qd::DBuf<cplx> vals_c;
   qd::DBuf<double> vals_r;
   qd::DBuf<float> vals_f;  // fp32 copy of vals_r for the mixed-precision SpMV
+  qd::DBuf<int32_t> row_order;  // rows by decreasing length inside 256-row windows (kernel 111)
   // matrix-free form
   bool has_mf = false;
   qd::DBuf<double> diag_r;
@@ -90,4 +91,5 @@ void ham_lower(qd_ham* H, const qd_term* terms, int nterms, const qd_gate* gates
 void ham_transpose(Ctx* ctx, int64_t n, const int64_t* ptr, const int32_t* idx, const cplx* vals,
                    int64_t nnz, int64_t* out_ptr, int32_t* out_idx, cplx* out_vals);
 void ham_build_matrix_free(qd_ham* H);
+void ham_ensure_row_order(qd_ham* H);
 }  // namespace qd

@@ -395,4 +395,23 @@ void ham_lower(qd_ham* H, const qd_term* terms, int nterms, const qd_gate* gates
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
+void ham_ensure_row_order(qd_ham* H) {
+  if (H->row_order.p) return;
+  const int64_t n = H->dim;
+  std::vector<int64_t> rp(n + 1);
+  QD_CUDA(cudaMemcpyAsync(rp.data(), H->rowptr.p, (n + 1) * 8, cudaMemcpyDeviceToHost, H->ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(H->ctx->stream));
+  std::vector<int32_t> order(n > 0 ? n : 1);
+  constexpr int64_t kWindow = 256;
+  for (int64_t w0 = 0; w0 < n; w0 += kWindow) {
+    const int64_t w1 = std::min(n, w0 + kWindow);
+    for (int64_t r = w0; r < w1; ++r) order[r] = (int32_t)r;
+    std::stable_sort(order.begin() + w0, order.begin() + w1,
+                     [&](int32_t a, int32_t b) { return rp[a + 1] - rp[a] > rp[b + 1] - rp[b]; });
+  }
+  H->row_order.alloc(order.size());
+  QD_CUDA(cudaMemcpyAsync(H->row_order.p, order.data(), order.size() * 4, cudaMemcpyHostToDevice, H->ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(H->ctx->stream));
+}
+
 }  // namespace qd

@@ -29,7 +29,8 @@ enum SpmvVariant {
   kSpmvRow4Stream = 108,  // as 106 with evict-first matrix loads
   kSpmvRow8Stream = 109,  // as 107 with evict-first matrix loads
   kSpmvRowExact = 110,  // thread per row, groups of 4 loads, exact-count tail
-  kSpmvLast = 110,
+  kSpmvRowSorted = 111, // as 110, rows taken in length order within 256-row windows
+  kSpmvLast = 111,
 };
 
 constexpr int kSpmvWarps = 4;  // warps per block
@@ -56,6 +57,7 @@ struct SpmvArgs {
   int step;
   const double* scale_dev;      // if non-null, the scale is read from the device
   const double* dot_scale_dev;  // if non-null, the final dot is multiplied by *dot_scale_dev
+  const int32_t* row_order;     // row permutation for the length-sorted kernel
 };
 
 template <typename MV, typename VV>
@@ -380,6 +382,44 @@ __global__ void __launch_bounds__(256) spmv_rowexact_kernel(SpmvArgs<MV, VV> A) 
   if (A.dotv) spmv_finish_dot(A, dotacc);
 }
 
+// As spmv_rowexact_kernel, but the i-th thread of the grid takes row
+// row_order[i]: rows are sorted by length inside windows of 256, so the lanes
+// of a warp issue nearly the same number of FMAs (less idle FP64 issue).
+template <typename MV, typename VV>
+__global__ void __launch_bounds__(256) spmv_rowsorted_kernel(SpmvArgs<MV, VV> A) {
+  if (A.stop) {
+    const int st = *A.stop;
+    if (st != 0 && st < A.step) return;
+  }
+  VV dotacc = vzero(VV{});
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < A.dim; i += stride) {
+    const int64_t r = A.row_order[i];
+    const int64_t b = A.rowptr[r], e = A.rowptr[r + 1];
+    VV acc = vzero(VV{});
+    int64_t k = b;
+    for (; k + 4 <= e; k += 4) {
+      int32_t c[4];
+      MV v[4];
+      VV xv[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        c[u] = ld_plain(A.colidx + k + u);
+        v[u] = ld_plain(A.vals + k + u);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) xv[u] = ld_ro(A.x + c[u]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc = vfma(v[u], xv[u], acc);
+    }
+    for (; k < e; ++k) acc = vfma(ld_plain(A.vals + k), ld_ro(A.x + ld_plain(A.colidx + k)), acc);
+    const VV yv = vscale(spmv_scale(A), acc);
+    A.y[r] = yv;
+    if (A.dotv) dotacc = vdotfma(A.dotv[r], yv, dotacc);
+  }
+  if (A.dotv) spmv_finish_dot(A, dotacc);
+}
+
 }  // namespace qd
 
 namespace qd {
@@ -410,6 +450,7 @@ inline void launch_spmv(Ctx* ctx, const qd_ham* H, const MV* vals, const VV* x, 
   A.step = step;
   A.scale_dev = scale_dev;
   A.dot_scale_dev = dot_scale_dev;
+  A.row_order = H->row_order.p;
   if (variant < 0) variant = H->spmv_variant;
   // every grid is capped so the block partials of a fused dot fit in kMaxGrid slots
   const unsigned vg = (unsigned)std::max<int64_t>(
@@ -429,6 +470,10 @@ inline void launch_spmv(Ctx* ctx, const qd_ham* H, const MV* vals, const VV* x, 
     case kSpmvRow4Stream: spmv_rowunroll_kernel<MV, VV, 4, true><<<rg, 256, 0, ctx->stream>>>(A); break;
     case kSpmvRow8Stream: spmv_rowunroll_kernel<MV, VV, 8, true><<<rg, 256, 0, ctx->stream>>>(A); break;
     case kSpmvRowExact: spmv_rowexact_kernel<MV, VV><<<rg, 256, 0, ctx->stream>>>(A); break;
+    case kSpmvRowSorted:
+      QD_REQUIRE(H->row_order.p != nullptr, QD_ERR_INVALID, "length-sorted kernel without a row order");
+      spmv_rowsorted_kernel<MV, VV><<<rg, 256, 0, ctx->stream>>>(A);
+      break;
     default: spmv_vector_kernel<MV, VV, 1><<<vg, 256, 0, ctx->stream>>>(A); break;
   }
   QD_CHECK_LAUNCH();
