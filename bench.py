@@ -299,6 +299,7 @@ def gpu_arm(args, rank, world, local):
     extras = {}
     if not args.no_extras:
         extras["batched_disorder_sweep"] = batched_sweep(ctx)
+        extras["jump_trajectories"] = trajectory_ensemble(ctx, with_oracle=not args.no_cpu)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -384,6 +385,48 @@ def batched_sweep(ctx, n_inst=512, steps=80, seed=2024):
             "lowering_s_all_instances": lower_s, "mixed_form": "fp32 products/basis, fp64 accumulation, "
             "full reorthogonalisation, device tridiagonal, fp64 Rayleigh refinement; one persistent launch",
             "plain_form": "fp64 Lanczos (reference algorithm), one solve after another"}
+
+
+def trajectory_ensemble(ctx, with_oracle=True):
+    """Dissipative Hubbard chain: L=8, N_up=N_dn=4 (dim 4900), t=1, U=4, open, jumps
+    sqrt(gamma) n_{i,s} on all 16 site-spins, gamma=0.1, 4096 trajectories, m=30,
+    dt=0.01, T=10; observable <n_{i,up} n_{i,dn}>(t).  Starts from the Lanczos ground state."""
+    import qudrip_gb300 as q
+    from qudrip_gb300 import chains
+    from qudrip_gb300.operators import getHopFermiGate
+    Lh, gamma, dt, nsteps, ntraj, m, seed = 8, 0.1, 0.01, 1000, 4096, 30, 4242
+    spec, ham = chains.hubbard_chain(Lh, 4, 4, 4.0, -1.0)
+    sec = q.Sector(spec.index, spec.constraints, ctx=ctx)
+    H = sec.lower(ham)
+    psi = q.getState(sec, 1)
+    psi.set(0, q.start_vector(sec.dim, 11))
+    q.Arnoldi.getLanczosSolver(sec, 100).getGroundState(H, psi(0), 0)
+    psi0 = psi.get(0)
+    gate = getHopFermiGate(spec.index)
+    heff = ham
+    for s in range(2 * Lh):
+        heff = heff + (-0.5j * gamma) * gate(s, s)
+    Heff = sec.lower(heff)
+    chan = list(range(2 * Lh))
+    obs = [(i, i + Lh) for i in range(Lh)]
+    t0 = time.perf_counter()
+    mean, err, st = q.traj_run(Heff, psi0, ntraj, nsteps, dt, gamma, seed, m, chan, obs)
+    wall = time.perf_counter() - t0
+    out = {"workload": "dissipative Hubbard L=8 (dim 4900), 4096 trajectories x 1000 steps, m=30, dt=0.01",
+           "trajectory_steps_per_s": ntraj * nsteps / wall, "wall_s": wall,
+           "propagator_ms": st.propagator_ms, "ensemble_ms": st.ensemble_ms, "jumps": int(st.jumps),
+           "docc_t0": float(mean[0].mean()), "docc_T": float(mean[-1].mean()),
+           "docc_T_stderr": float(err[-1].mean())}
+    if with_oracle:
+        import oracle as O
+        osec = O.Sector(spec)
+        oh = O.Ham(osec, heff)
+        nt_c, ns_c = 16, 100
+        ref, rj = O.traj_run(oh, osec.basis(), nt_c, ns_c, dt, gamma, seed, m, chan, obs, psi0)
+        m2, _, st2 = q.traj_run(Heff, psi0, nt_c, ns_c, dt, gamma, seed, m, chan, obs)
+        out["oracle_check"] = {"ntraj": nt_c, "nsteps": ns_c, "max_abs_diff": float(np.abs(m2 - ref).max()),
+                               "jumps_gpu": int(st2.jumps), "jumps_oracle": int(rj)}
+    return out
 
 
 def spmv_only(args, local):

@@ -252,6 +252,57 @@ qd_status qd_arnoldi_evolve(qd_ham *ham, qd_state *psi, int t_in, int t_out,
 qd_status qd_batch_lanczos(qd_ctx *ctx, int ninst, qd_ham *const *hams,
                            const double *const *v0s, int steps, double *out);
 
+/* ------------------------------------------------------------------ */
+/* Batched Krylov real-time steps                                     */
+/*   ArnoldiSolver<T,0>::evolve (sparse_algorithm.hpp:548-562) for     */
+/*   nvec columns at once, one persistent launch, FP64                 */
+/* Y[:, b] = V exp(-i K h) e_0 for X[:, b] (device complex128, leading  */
+/* dimension ldx; X == NULL means the unit vectors e_0 .. e_{nvec-1},   */
+/* i.e. the first nvec columns of exp(-i H h)).  Y is device complex128 */
+/* with leading dimension ldy.  act_dims (host, may be NULL) receives    */
+/* each column's Krylov dimension.  m <= 32.                            */
+/* ------------------------------------------------------------------ */
+qd_status qd_krylov_evolve_batch(qd_ham *ham, const double *d_X, int64_t ldx,
+                                 int nvec, double h, int m, double *d_Y,
+                                 int64_t ldy, int *act_dims);
+
+/* ------------------------------------------------------------------ */
+/* Quantum-jump trajectories                                           */
+/*   the jump loop of programs/hubbard_diss.cpp:439-482 (weights        */
+/*   :520-529, no-jump generator :514-517, channel search :565-577)    */
+/* heff must be the no-jump generator H - (i/2) gamma sum_j n_j of the  */
+/* jump operators L_j = sqrt(gamma) n_{chan_bits[j]}.  Every trajectory  */
+/* starts from psi0 (host complex128), runs nsteps steps of length dt    */
+/* (m Krylov vectors tabulate exp(-i heff dt) once), draws its random    */
+/* numbers from Philox4x32-10 keyed by (seed, trajectory, step), and     */
+/* records <n_{obs_a[k]} n_{obs_b[k]}> after every step.  obs_mean and   */
+/* obs_stderr receive (nsteps+1) x nobs doubles (row = step).           */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  int32_t ntraj;
+  int32_t nsteps;
+  double dt;
+  double gamma;
+  uint64_t seed;
+  int32_t m;
+  int32_t nchan;              /* <= 32 */
+  const int32_t *chan_bits;   /* nchan bit indices */
+  int32_t nobs;               /* <= 16 */
+  int32_t reserved;
+  const int32_t *obs_a;
+  const int32_t *obs_b;
+} qd_traj_desc;
+
+typedef struct {
+  int64_t jumps;        /* jumps over all trajectories */
+  double propagator_ms; /* tabulation of exp(-i heff dt) */
+  double ensemble_ms;   /* the nsteps steps of all trajectories */
+  double reserved;
+} qd_traj_stats;
+
+qd_status qd_traj_run(qd_ham *heff, const qd_traj_desc *desc, const double *psi0,
+                      double *obs_mean, double *obs_stderr, qd_traj_stats *stats);
+
 /* Average device time of the sparse product kernel the solvers use on this
  * Hamiltonian (iters back-to-back launches on the context stream, timed with
  * CUDA events), and the kernel's algorithmic HBM bytes per launch:

@@ -217,3 +217,28 @@ def expm(Amat):
     if rc != 0:
         raise RuntimeError("expm failed")
     return out
+
+
+def traj_run(H: "Ham", basis, ntraj, nsteps, dt, gamma, seed, m, chan_bits, obs_pairs, psi0):
+    """Trajectory ensemble restated from the reference jump loop (mean observables)."""
+    L = lib()
+    if not hasattr(L.qdo_traj_run, "_typed"):
+        L.qdo_traj_run.restype = C.c_int
+        L.qdo_traj_run.argtypes = [_P, C.POINTER(C.c_uint64), C.c_int, C.c_int, C.c_double, C.c_double,
+                                   C.c_uint64, C.c_int, C.c_int, C.POINTER(C.c_int), C.c_int,
+                                   C.POINTER(C.c_int), C.POINTER(C.c_int), _DP, _DP, _I64P]
+        L.qdo_traj_run._typed = True
+    basis = np.ascontiguousarray(basis, dtype=np.uint64)
+    cb = np.ascontiguousarray(chan_bits, dtype=np.int32)
+    oa = np.ascontiguousarray([a for a, _ in obs_pairs], dtype=np.int32)
+    ob = np.ascontiguousarray([b for _, b in obs_pairs], dtype=np.int32)
+    psi0 = as_complex(psi0)
+    out = np.zeros((nsteps + 1, len(obs_pairs)))
+    jumps = C.c_int64(0)
+    rc = L.qdo_traj_run(H.ptr, basis.ctypes.data_as(C.POINTER(C.c_uint64)), ntraj, nsteps, dt, gamma, seed, m,
+                        len(cb), cb.ctypes.data_as(C.POINTER(C.c_int)), len(oa),
+                        oa.ctypes.data_as(C.POINTER(C.c_int)), ob.ctypes.data_as(C.POINTER(C.c_int)),
+                        _dp(psi0), _dp(out), C.byref(jumps))
+    if rc != 0:
+        raise RuntimeError("oracle trajectories failed")
+    return out, jumps.value

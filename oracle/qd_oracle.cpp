@@ -811,3 +811,144 @@ extern "C" int qdo_hermitian_lanczos_ground(const qdo_ham* H, const double* psi0
   if (matvecs_out) *matvecs_out = mv;
   return 0;
 }
+
+// ===========================================================================
+// Quantum-jump trajectories: programs/hubbard_diss.cpp:439-482 (loop),
+// :520-529 (lindblad_weight), :514-517 (QJ_operator), :565-577 (bsearch),
+// for diagonal jump operators L_j = sqrt(gamma) n_{bit_j}.  Random numbers:
+// Philox4x32-10 (Salmon et al., SC11) keyed by (seed) with counter
+// (step, trajectory, 0, 0): two 53-bit uniforms per step, written out here
+// independently of the engine's copy.  Each trajectory starts from psi0.
+// The no-jump step evolves with H_eff + (i/2) gamma wtot I exactly as
+// QJ_operator builds it; the shift is applied to the Hessenberg diagonal.
+// ===========================================================================
+namespace {
+
+void philox_round10(uint32_t c[4], uint32_t k0, uint32_t k1) {
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    const uint32_t c0 = hi1 ^ c[1] ^ k0, c2 = hi0 ^ c[3] ^ k1;
+    c[0] = c0;
+    c[1] = lo1;
+    c[2] = c2;
+    c[3] = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+}
+
+void uniform2(uint64_t seed, uint32_t traj, uint32_t step, double& u1, double& u2) {
+  uint32_t c[4] = {step, traj, 0u, 0u};
+  philox_round10(c, (uint32_t)seed, (uint32_t)(seed >> 32));
+  u1 = ((double)(c[0] >> 5) * 67108864.0 + (double)(c[1] >> 6)) / 9007199254740992.0;
+  u2 = ((double)(c[2] >> 5) * 67108864.0 + (double)(c[3] >> 6)) / 9007199254740992.0;
+}
+
+int bsearch_ref(const std::vector<double>& values, double val) {  // hubbard_diss.cpp:565-577
+  if (val > values.back() || val < values[0]) return -1;
+  int is = 0, ie = (int)values.size();
+  while (ie - is > 1) {
+    const int imid = is + (ie - is) / 2;
+    if (val < values[imid]) ie = imid;
+    else is = imid;
+  }
+  return is;
+}
+
+// ArnoldiSolver<T,0>::evolve with a diagonal shift c added to the Hessenberg
+// matrix (the operator H + c I).
+void evolve_shift(const qdo_ham* H, const cd* psi, double h, int m, cd c, cd* out) {
+  const int64_t n = H->dim;
+  std::vector<std::vector<cd>> V(m + 1, std::vector<cd>(n));
+  const double nrm0 = std::sqrt(norm2(psi, n));
+  for (int64_t k = 0; k < n; ++k) V[0][k] = psi[k] / nrm0;
+  std::vector<cd> hv;
+  int idx;
+  for (idx = 1; idx <= m - 1; ++idx) {
+    spmv_csc(H, V[idx - 1].data(), V[idx].data());
+    for (int i = 0; i < idx; ++i) {
+      const cd nh = dotc(V[i].data(), V[idx].data(), n);
+      for (int64_t k = 0; k < n; ++k) V[idx][k] -= nh * V[i][k];
+      hv.push_back(nh);
+    }
+    const double nr = std::sqrt(norm2(V[idx].data(), n));
+    for (int64_t k = 0; k < n; ++k) V[idx][k] /= nr;
+    hv.push_back(nr);
+    if (nr < kEps) {
+      ++idx;
+      break;
+    }
+  }
+  const int act = idx - 1;
+  std::vector<cd> K((size_t)act * act, cd(0, 0));
+  size_t hp = 0;
+  for (int i = 0; i < act - 1; ++i)
+    for (int j = 0; j <= i + 1; ++j) K[(size_t)i * act + j] = hv[hp++];
+  for (int j = 0; j <= act - 1; ++j) K[(size_t)(act - 1) * act + j] = hv[hp++];
+  for (int i = 0; i < act; ++i) K[(size_t)i * act + i] += c;
+  std::vector<cd> A((size_t)act * act), E((size_t)act * act);
+  for (size_t q = 0; q < A.size(); ++q) A[q] = cd(0.0, -h) * K[q];
+  qdo_expm(act, reinterpret_cast<const double*>(A.data()), reinterpret_cast<double*>(E.data()));
+  for (int64_t k = 0; k < n; ++k) {
+    cd s(0, 0);
+    for (int j = 0; j < act; ++j) s += V[j][k] * E[j];
+    out[k] = s;
+  }
+}
+
+}  // namespace
+
+extern "C" int qdo_traj_run(const qdo_ham* Heff, const uint64_t* basis, int ntraj, int nsteps, double dt,
+                            double gamma, uint64_t seed, int m, int nchan, const int* chan_bits, int nobs,
+                            const int* obs_a, const int* obs_b, const double* psi0, double* obs_mean,
+                            int64_t* jumps_out) {
+  const int64_t n = Heff->dim;
+  const cd* p0 = reinterpret_cast<const cd*>(psi0);
+  std::vector<double> sums((size_t)(nsteps + 1) * nobs, 0.0);
+  std::vector<cd> psi(n), nxt(n);
+  int64_t jumps = 0;
+  auto record = [&](int step) {
+    const double nn = norm2(psi.data(), n);
+    for (int k = 0; k < nobs; ++k) {
+      const uint64_t mask = (1ull << obs_a[k]) | (1ull << obs_b[k]);
+      double s = 0.0;
+      for (int64_t i = 0; i < n; ++i)
+        if ((basis[i] & mask) == mask) s += std::norm(psi[i]);
+      sums[(size_t)step * nobs + k] += s / nn;
+    }
+  };
+  for (int b = 0; b < ntraj; ++b) {
+    const double nrm = std::sqrt(norm2(p0, n));
+    for (int64_t i = 0; i < n; ++i) psi[i] = p0[i] / nrm;
+    record(0);
+    for (int step = 1; step <= nsteps; ++step) {
+      std::vector<double> w(nchan, 0.0);
+      for (int j = 0; j < nchan; ++j)
+        for (int64_t i = 0; i < n; ++i)
+          if ((basis[i] >> chan_bits[j]) & 1ull) w[j] += std::norm(psi[i]);
+      std::vector<double> wt(nchan + 1, 0.0);
+      for (int j = 1; j <= nchan; ++j) wt[j] = wt[j - 1] + w[j - 1];
+      const double wtot = wt[nchan];
+      for (int j = 0; j <= nchan; ++j) wt[j] /= wt[nchan];
+      double u1, u2;
+      uniform2(seed, (uint32_t)b, (uint32_t)step, u1, u2);
+      if (u1 < gamma * wtot * dt) {
+        const int idx = bsearch_ref(wt, u2);
+        const uint64_t bit = 1ull << chan_bits[idx];
+        for (int64_t i = 0; i < n; ++i) nxt[i] = (basis[i] & bit) ? psi[i] : cd(0, 0);
+        ++jumps;
+      } else {
+        evolve_shift(Heff, psi.data(), dt, m, cd(0.0, 0.5 * gamma * wtot), nxt.data());
+      }
+      const double nn = std::sqrt(norm2(nxt.data(), n));
+      for (int64_t i = 0; i < n; ++i) psi[i] = nxt[i] / nn;
+      record(step);
+    }
+  }
+  for (size_t q = 0; q < sums.size(); ++q) obs_mean[q] = sums[q] / ntraj;
+  if (jumps_out) *jumps_out = jumps;
+  return 0;
+}

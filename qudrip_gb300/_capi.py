@@ -77,6 +77,18 @@ class qd_lanczos_result(C.Structure):
                 ("reserved", C.c_int32), ("ritz_value", C.c_double), ("err", C.c_double)]
 
 
+class qd_traj_desc(C.Structure):
+    _fields_ = [("ntraj", C.c_int32), ("nsteps", C.c_int32), ("dt", C.c_double), ("gamma", C.c_double),
+                ("seed", C.c_uint64), ("m", C.c_int32), ("nchan", C.c_int32),
+                ("chan_bits", C.POINTER(C.c_int32)), ("nobs", C.c_int32), ("reserved", C.c_int32),
+                ("obs_a", C.POINTER(C.c_int32)), ("obs_b", C.POINTER(C.c_int32))]
+
+
+class qd_traj_stats(C.Structure):
+    _fields_ = [("jumps", C.c_int64), ("propagator_ms", C.c_double), ("ensemble_ms", C.c_double),
+                ("reserved", C.c_double)]
+
+
 class QDError(RuntimeError):
     def __init__(self, code: int, where: str, msg: str):
         super().__init__(f"{where}: status {code} ({msg})")
@@ -105,6 +117,9 @@ _SIGNATURES = {
     "qd_csr_expect_noalloc": [_P, _P, _P, C.c_int64, _P, _P, _P],
     "qd_arnoldi_evolve": [_P, _P, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int)],
     "qd_batch_lanczos": [_P, C.c_int, C.POINTER(C.c_void_p), C.POINTER(_DP), C.c_int, _DP],
+    "qd_krylov_evolve_batch": [_P, _P, C.c_int64, C.c_int, C.c_double, C.c_int, _P, C.c_int64,
+                               C.POINTER(C.c_int)],
+    "qd_traj_run": [_P, C.POINTER(qd_traj_desc), _DP, _DP, _DP, C.POINTER(qd_traj_stats)],
     "qd_status_string": [C.c_int],
     "qd_last_error": [],
     "qd_api_version": [],

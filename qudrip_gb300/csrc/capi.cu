@@ -4,6 +4,8 @@
 #include <string>
 
 #include "batch.cuh"
+#include "kbatch.cuh"
+#include "traj.cuh"
 #include "evolve.cuh"
 #include "ham.cuh"
 #include "krylov.cuh"
@@ -446,6 +448,37 @@ qd_status qd_batch_lanczos(qd_ctx* ctx, int ninst, qd_ham* const* hams, const do
     QD_REQUIRE(ctx && hams && v0s && out, QD_ERR_INVALID, "null argument");
     DeviceGuard dg(ctx->device);
     batch_lanczos(ctx, hams, v0s, ninst, steps, out);
+  });
+}
+
+qd_status qd_krylov_evolve_batch(qd_ham* ham, const double* d_X, int64_t ldx, int nvec, double h, int m,
+                                 double* d_Y, int64_t ldy, int* act_dims) {
+  return guard([&] {
+    QD_REQUIRE(ham && d_Y && nvec >= 1, QD_ERR_INVALID, "bad argument");
+    QD_REQUIRE(ldy >= ham->dim && (!d_X || ldx >= ham->dim), QD_ERR_INVALID, "leading dimension below dim");
+    QD_REQUIRE(d_X || nvec <= ham->dim, QD_ERR_INVALID, "more unit vectors than the dimension");
+    DeviceGuard dg(ham->ctx->device);
+    krylov_batch(ham, reinterpret_cast<const cplx*>(d_X), ldx, nvec, h, m, reinterpret_cast<cplx*>(d_Y), nullptr,
+                 ldy, act_dims);
+  });
+}
+
+qd_status qd_traj_run(qd_ham* heff, const qd_traj_desc* desc, const double* psi0, double* obs_mean,
+                      double* obs_stderr, qd_traj_stats* stats) {
+  return guard([&] {
+    QD_REQUIRE(heff && desc && psi0 && (obs_mean || desc->nobs == 0), QD_ERR_INVALID, "null argument");
+    QD_REQUIRE(desc->chan_bits && (desc->nobs == 0 || (desc->obs_a && desc->obs_b)), QD_ERR_INVALID,
+               "null channel or observable array");
+    DeviceGuard dg(heff->ctx->device);
+    int64_t jumps = 0;
+    double t[2] = {0, 0};
+    traj_run(heff, *desc, psi0, obs_mean, obs_stderr, &jumps, t);
+    if (stats) {
+      std::memset(stats, 0, sizeof(*stats));
+      stats->jumps = jumps;
+      stats->propagator_ms = t[0];
+      stats->ensemble_ms = t[1];
+    }
   });
 }
 

@@ -66,7 +66,7 @@ struct qd_ham {
   int64_t nnz = 0;
   int flags = 0;
   int max_row_nnz = 0;
-  int spmv_variant = 106;  // CSR product kernel the solvers launch (krylov.cuh SpmvVariant)
+  int spmv_variant = 110;  // CSR product kernel the solvers launch (krylov.cuh SpmvVariant)
   qd::DBuf<int64_t> rowptr;
   qd::DBuf<int32_t> colidx;
   qd::DBuf<cplx> vals_c;

@@ -1,0 +1,14 @@
+// traj.cuh -- quantum-jump trajectory ensembles.
+#pragma once
+
+#include "ham.cuh"
+
+namespace qd {
+
+constexpr int kTrajMaxChan = 32;
+constexpr int kTrajMaxObs = 16;
+
+void traj_run(qd_ham* H, const qd_traj_desc& d, const double* psi0_host, double* obs_mean, double* obs_stderr,
+              int64_t* jumps_total, double* timings);
+
+}  // namespace qd

@@ -361,3 +361,34 @@ def batch_lanczos(hams, v0s, steps: int, ctx: Optional[Context] = None) -> np.nd
     out = np.zeros((n, 8))
     A.call("qd_batch_lanczos", ctx.handle, n, hp, vp, steps, out.ctypes.data_as(A._DP))
     return out
+
+
+def traj_run(heff: Hamiltonian, psi0, ntraj: int, nsteps: int, dt: float, gamma: float, seed: int, m: int,
+             chan_bits, obs_pairs):
+    """Quantum-jump trajectories (diagonal jumps sqrt(gamma) n_bit) on the device.
+
+    Returns (mean, stderr, stats): (nsteps+1) x len(obs_pairs) arrays of
+    <n_a n_b> averaged over the trajectories, and the qd_traj_stats record.
+    """
+    cb = np.ascontiguousarray(chan_bits, dtype=np.int32)
+    oa = np.ascontiguousarray([a for a, _ in obs_pairs], dtype=np.int32)
+    ob = np.ascontiguousarray([b for _, b in obs_pairs], dtype=np.int32)
+    d = A.qd_traj_desc()
+    d.ntraj = ntraj
+    d.nsteps = nsteps
+    d.dt = dt
+    d.gamma = gamma
+    d.seed = seed
+    d.m = m
+    d.nchan = len(cb)
+    d.chan_bits = cb.ctypes.data_as(C.POINTER(C.c_int32))
+    d.nobs = len(oa)
+    d.obs_a = oa.ctypes.data_as(C.POINTER(C.c_int32))
+    d.obs_b = ob.ctypes.data_as(C.POINTER(C.c_int32))
+    psi0 = np.ascontiguousarray(np.asarray(psi0, dtype=np.complex128))
+    mean = np.zeros((nsteps + 1, len(oa)))
+    err = np.zeros((nsteps + 1, len(oa)))
+    st = A.qd_traj_stats()
+    A.call("qd_traj_run", heff.handle, C.byref(d), psi0.ctypes.data_as(A._DP), mean.ctypes.data_as(A._DP),
+           err.ctypes.data_as(A._DP), C.byref(st))
+    return mean, err, st
