@@ -316,7 +316,7 @@ def gpu_arm(args, rank, world, local):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded uniform[-1,1] start vector; Hamiltonian built from the operator tree)",
             "config": {"workload": "xxz_chain_L24_periodic_Sz0_lanczos_k100", "L": L, "Jxy": 1.0, "Jz": 1.0,
-                       "dim": dim, "nnz": H.nnz, "krylov_dim": KRY, "spmv": "csr_thread_per_row_fp64",
+                       "dim": dim, "nnz": H.nnz, "krylov_dim": KRY, "spmv": "csr_row_exact_fp64",
                        "ritz": "stored_basis", "parallelism": f"replicas{world}",
                        "l2": "inputs larger than L2 (CSR 493 MB); no flush",
                        "ritz_value": ritz, "psi_eval": energy.real if energy is not None else None},
@@ -325,7 +325,7 @@ def gpu_arm(args, rank, world, local):
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic,
-                         "kernel": "spmv_rowunroll_kernel<double,double,4>", "peak_kind": peak_kind,
+                         "kernel": "spmv_rowexact_kernel<double,double>", "peak_kind": peak_kind,
                          "bytes_per_launch": nbytes.value, "launch_ms": avg_ms.value},
             "cpu_baseline": cpu,
             "clocks": clk,

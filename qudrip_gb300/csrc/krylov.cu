@@ -2,18 +2,20 @@
 //
 // Lanczos (Arnoldi::ArnoldiSolver<T, herm=1>, sparse_algorithm.hpp:395-425,
 // 458-473, 514-585).  Step k = 1..kry_dim, with v1 = v_{k-1}, v2 = v_{k-2}:
-//   K1  w = H v1                  fused with  beta'_k = <v2, w>   (k >= 2)
-//   K2  w -= beta'_k v2           fused with  alpha_k = <v1, w>
-//   K3  w -= alpha_k v1           fused with  n_k = ||w||, stop if n_k < 1e-10
-//   K4  v_k = w / n_k   (stored: the basis is kept in HBM)
-// This is the reference's order of operations (local orthogonalisation
-// against the two previous vectors, no full reorthogonalisation).  The
-// scalars stay on the device, so the whole recurrence is one CUDA graph with
-// no host round trip; a breakdown sets a device flag that turns the remaining
-// steps into no-ops.  The tridiagonal matrix tridiag(Re alpha, n) is solved on
-// the host and the Ritz vector psi = sum_k y_k v_k is formed from the stored
-// basis -- the values the reference's second Lanczos pass (getState<1>)
-// regenerates, obtained without repeating the kry_dim products.
+//   K1  w = H v1                                  (the product alone)
+//   K2  beta_k = <v2, w>, alpha_k = <v1, w - beta_k v2>   (one read of w, v1, v2)
+//   K3  v_k = (w - beta_k v2) - alpha_k v1,  n_k = ||v_k||,  stop if n_k < 1e-10
+// This is the reference's local orthogonalisation against the two previous
+// vectors (no full reorthogonalisation), with its two subtractions in its
+// order; alpha is expanded as <v1, w> - beta <v1, v2> so that w is read once
+// and never rewritten.  The basis is stored unnormalised with 1 / n_k on the
+// device.  The scalars stay on the device, so the whole recurrence is one
+// CUDA graph with no host round trip; a breakdown sets a device flag that
+// turns the remaining steps into no-ops.  The tridiagonal matrix
+// tridiag(Re alpha, n) is solved on the host and the Ritz vector
+// psi = sum_k y_k v_k is formed from the stored basis -- the values the
+// reference's second Lanczos pass (getState<1>) regenerates, obtained without
+// repeating the kry_dim products.
 #include <algorithm>
 #include <chrono>
 #include <cstdio>
@@ -44,85 +46,175 @@ __device__ __forceinline__ bool stopped(const int* stop, int step) {
 
 // The basis is stored unnormalised: V[k] = n_k v_k, with s_k = 1 / n_k kept on
 // the device (s_0 = 1).  Every consumer folds s into its scalars, so no pass
-// is spent rescaling a vector.  Loops are unrolled four wide with independent
-// partial sums so each thread keeps several loads in flight.
-constexpr int kVecUnroll = 4;
+// is spent rescaling a vector.  The two vector passes of a step read 16 bytes
+// per load (two reals, or one complex) with two loads per operand in flight.
+constexpr int kLzThreads = 256;
+constexpr int kLzBlocksPerSm = 4;
 
-// K2: w -= (beta' s2) V2;  alpha = s1 <V1, w>
-template <typename VV>
-__global__ void __launch_bounds__(kVecThreads) lz_k2_kernel(int64_t n, const int* stop, int step, VV* __restrict__ w,
-                                                            const VV* __restrict__ V1, const VV* __restrict__ V2,
-                                                            const double* s1, const double* s2,
-                                                            const VV* beta, VV* alpha, GridRed<VV> red) {
-  if (stopped(stop, step)) return;
-  const VV b = V2 ? vscale(*s2, *beta) : vzero(VV{});
-  VV acc[kVecUnroll];
-#pragma unroll
-  for (int u = 0; u < kVecUnroll; ++u) acc[u] = vzero(VV{});
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  for (; i + (kVecUnroll - 1) * stride < n; i += kVecUnroll * stride) {
-    VV wv[kVecUnroll], v1[kVecUnroll], v2[kVecUnroll];
-#pragma unroll
-    for (int u = 0; u < kVecUnroll; ++u) {
-      wv[u] = w[i + u * stride];
-      v1[u] = V1[i + u * stride];
-      v2[u] = V2 ? V2[i + u * stride] : vzero(VV{});
-    }
-#pragma unroll
-    for (int u = 0; u < kVecUnroll; ++u) {
-      if (V2) wv[u] = vsubmul(wv[u], b, v2[u]);
-      w[i + u * stride] = wv[u];
-      acc[u] = vdotfma(v1[u], wv[u], acc[u]);
-    }
-  }
-  for (; i < n; i += stride) {
-    VV wi = w[i];
-    if (V2) wi = vsubmul(wi, b, V2[i]);
-    w[i] = wi;
-    acc[0] = vdotfma(V1[i], wi, acc[0]);
-  }
-  const VV tot = vadd(vadd(acc[0], acc[1]), vadd(acc[2], acc[3]));
-  if (grid_sum(tot, red, alpha) && threadIdx.x == 0) *alpha = vscale(*s1, *alpha);
+static int lz_grid(Ctx* ctx, int64_t packs) {
+  const int64_t want = ceil_div(packs, 2 * kLzThreads);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->num_sms * kLzBlocksPerSm));
 }
 
-// K3: V[k] = w - (alpha s1) V1;  n_k = ||V[k]||, s_k = 1 / n_k, stop if n_k < 1e-10
+// 16-byte packs: two reals or one complex element.
 template <typename VV>
-__global__ void __launch_bounds__(kVecThreads) lz_k3_kernel(int64_t n, int* stop, int step, const VV* __restrict__ w,
-                                                            const VV* __restrict__ V1, const double* s1,
-                                                            const VV* alpha, VV* __restrict__ Vk, double* nrm2,
-                                                            double* nrm, double* sk, GridRed<double> red) {
+struct LzPack;
+template <>
+struct LzPack<double> {
+  using T = double2;
+  static constexpr int kPer = 2;
+  __device__ static T load(const double* p, int64_t i) { return reinterpret_cast<const double2*>(p)[i]; }
+  __device__ static T load_last(const double* p, int64_t i) { return __ldcs(reinterpret_cast<const double2*>(p) + i); }
+  __device__ static void store(double* p, int64_t i, T v) { reinterpret_cast<double2*>(p)[i] = v; }
+  __device__ static double dot(T a, T b, double acc) { return fma(a.y, b.y, fma(a.x, b.x, acc)); }
+  __device__ static double nrm(T a, double acc) { return fma(a.y, a.y, fma(a.x, a.x, acc)); }
+  __device__ static T submul(T x, double a, T y) { return make_double2(fma(-a, y.x, x.x), fma(-a, y.y, x.y)); }
+};
+template <>
+struct LzPack<cplx> {
+  using T = cplx;
+  static constexpr int kPer = 1;
+  __device__ static T load(const cplx* p, int64_t i) { return p[i]; }
+  __device__ static T load_last(const cplx* p, int64_t i) {
+    const double2 d = __ldcs(reinterpret_cast<const double2*>(p) + i);
+    return mkc(d.x, d.y);
+  }
+  __device__ static void store(cplx* p, int64_t i, T v) { p[i] = v; }
+  __device__ static cplx dot(T a, T b, cplx acc) { return vdotfma(a, b, acc); }
+  __device__ static double nrm(T a, double acc) { return acc + vnorm2(a); }
+  __device__ static T submul(T x, cplx a, T y) { return vsubmul(x, a, y); }
+};
+
+// K2: the three inner products of step k from one read of w, V1, V2:
+//   d1 = <V2, w>,  d2 = <V1, w>,  d3 = <V1, V2>
+//   beta  = s2 d1                   = <v2, w>
+//   alpha = s1 (d2 - beta s2 d3)    = <v1, w - beta v2>
+// alpha is the reference's <v1, w> taken after w -= beta v2
+// (sparse_algorithm.hpp:405-415), expanded so that w is read once and not
+// written.  For k = 1 there is no V2 and beta = 0.
+template <typename VV, bool kHas2>
+__global__ void __launch_bounds__(kLzThreads, kLzBlocksPerSm)
+    lz_dots_kernel(int64_t n, const int* stop, int step, const VV* __restrict__ w, const VV* __restrict__ V1,
+                   const VV* __restrict__ V2, const double* s1, const double* s2, VV* beta, VV* alpha,
+                   Tri<VV>* dots, GridRed<Tri<VV>> red) {
   if (stopped(stop, step)) return;
-  const VV a = vscale(*s1, *alpha);
-  double acc[kVecUnroll] = {0.0, 0.0, 0.0, 0.0};
+  using P = LzPack<VV>;
+  const int64_t np = n / P::kPer;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  for (; i + (kVecUnroll - 1) * stride < n; i += kVecUnroll * stride) {
-    VV wv[kVecUnroll], v1[kVecUnroll];
-#pragma unroll
-    for (int u = 0; u < kVecUnroll; ++u) {
-      wv[u] = w[i + u * stride];
-      v1[u] = V1[i + u * stride];
-    }
-#pragma unroll
-    for (int u = 0; u < kVecUnroll; ++u) {
-      const VV o = vsubmul(wv[u], a, v1[u]);
-      Vk[i + u * stride] = o;
-      acc[u] += vnorm2(o);
+  Tri<VV> acc0 = vzero(Tri<VV>{});
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; p + stride < np; p += 2 * stride) {
+    const typename P::T w0 = P::load(w, p), w1 = P::load(w, p + stride);
+    const typename P::T a0 = P::load(V1, p), a1 = P::load(V1, p + stride);
+    acc0.b = P::dot(a1, w1, P::dot(a0, w0, acc0.b));
+    if (kHas2) {
+      const typename P::T b0 = P::load(V2, p), b1 = P::load(V2, p + stride);
+      acc0.a = P::dot(b1, w1, P::dot(b0, w0, acc0.a));
+      acc0.c = P::dot(a1, b1, P::dot(a0, b0, acc0.c));
     }
   }
-  for (; i < n; i += stride) {
-    const VV o = vsubmul(w[i], a, V1[i]);
-    Vk[i] = o;
-    acc[0] += vnorm2(o);
+  if (p < np) {
+    const typename P::T w0 = P::load(w, p), a0 = P::load(V1, p);
+    acc0.b = P::dot(a0, w0, acc0.b);
+    if (kHas2) {
+      const typename P::T b0 = P::load(V2, p);
+      acc0.a = P::dot(b0, w0, acc0.a);
+      acc0.c = P::dot(a0, b0, acc0.c);
+    }
   }
-  const double tot = (acc[0] + acc[1]) + (acc[2] + acc[3]);
-  if (grid_sum(tot, red, nrm2) && threadIdx.x == 0) {
+  if (P::kPer == 2 && (n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {  // odd real length: last element
+    acc0.b = vdotfma(V1[n - 1], w[n - 1], acc0.b);
+    if (kHas2) {
+      acc0.a = vdotfma(V2[n - 1], w[n - 1], acc0.a);
+      acc0.c = vdotfma(V1[n - 1], V2[n - 1], acc0.c);
+    }
+  }
+  if (grid_sum(acc0, red, dots) && threadIdx.x == 0) {
+    const Tri<VV> d = *dots;
+    const VV b = kHas2 ? vscale(*s2, d.a) : vzero(VV{});
+    VV t = d.b;
+    if (kHas2) t = vsubmul(t, vscale(*s2, b), d.c);
+    *beta = b;
+    *alpha = vscale(*s1, t);
+  }
+}
+
+// K3: V[k] = (w - (beta s2) V2) - (alpha s1) V1   (the reference's two
+// subtractions in its order);  n_k = ||V[k]||, s_k = 1 / n_k, stop if n_k < 1e-10.
+template <typename VV, bool kHas2>
+__global__ void __launch_bounds__(kLzThreads, kLzBlocksPerSm)
+    lz_update_kernel(int64_t n, int* stop, int step, const VV* __restrict__ w, const VV* __restrict__ V1,
+                     const VV* __restrict__ V2, const double* s1, const double* s2, const VV* alpha,
+                     const VV* beta, VV* __restrict__ Vk, double* nrm2, double* nrm, double* sk,
+                     GridRed<double> red) {
+  if (stopped(stop, step)) return;
+  using P = LzPack<VV>;
+  const VV a = vscale(*s1, *alpha);
+  const VV b = kHas2 ? vscale(*s2, *beta) : vzero(VV{});
+  const int64_t np = n / P::kPer;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  double acc0 = 0.0, acc1 = 0.0;
+  int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; p + stride < np; p += 2 * stride) {
+    typename P::T o0 = P::load_last(w, p), o1 = P::load_last(w, p + stride);
+    const typename P::T a0 = P::load(V1, p), a1 = P::load(V1, p + stride);
+    if (kHas2) {
+      const typename P::T b0 = P::load_last(V2, p), b1 = P::load_last(V2, p + stride);
+      o0 = P::submul(o0, b, b0);
+      o1 = P::submul(o1, b, b1);
+    }
+    o0 = P::submul(o0, a, a0);
+    o1 = P::submul(o1, a, a1);
+    P::store(Vk, p, o0);
+    P::store(Vk, p + stride, o1);
+    acc0 = P::nrm(o0, acc0);
+    acc1 = P::nrm(o1, acc1);
+  }
+  if (p < np) {
+    typename P::T o0 = P::load_last(w, p);
+    if (kHas2) o0 = P::submul(o0, b, P::load_last(V2, p));
+    o0 = P::submul(o0, a, P::load(V1, p));
+    P::store(Vk, p, o0);
+    acc0 = P::nrm(o0, acc0);
+  }
+  if (P::kPer == 2 && (n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    VV o = w[n - 1];
+    if (kHas2) o = vsubmul(o, b, V2[n - 1]);
+    o = vsubmul(o, a, V1[n - 1]);
+    Vk[n - 1] = o;
+    acc0 += vnorm2(o);
+  }
+  if (grid_sum(acc0 + acc1, red, nrm2) && threadIdx.x == 0) {
     const double nr = sqrt(*nrm2);
     *nrm = nr;
     *sk = 1.0 / nr;
     if (nr < 1e-10 && stop && *stop == 0) *stop = step;  // sparse_algorithm.hpp:421
   }
+}
+
+// One Lanczos step's two vector passes (after K1 has written w = s1 H V1).
+template <typename VV>
+static void lz_vector_passes(Ctx* ctx, int64_t n, int* stop, int step, const VV* w, const VV* V1, const VV* V2,
+                             const double* s1, const double* s2, VV* beta, VV* alpha, Tri<VV>* dots, VV* Vk,
+                             double* nrm2, double* nrm, double* sk, GridRed<Tri<VV>> rt, GridRed<double> rd) {
+  const int g = lz_grid(ctx, n / LzPack<VV>::kPer + 1);
+  if (V2) {
+    lz_dots_kernel<VV, true><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V2, s1, s2, beta, alpha, dots,
+                                                                rt);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+    lz_update_kernel<VV, true><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V2, s1, s2, alpha, beta, Vk,
+                                                                  nrm2, nrm, sk, rd);
+  } else {
+    lz_dots_kernel<VV, false><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V1, s1, s1, beta, alpha,
+                                                                 dots, rt);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+    lz_update_kernel<VV, false><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V1, s1, s1, alpha, beta,
+                                                                   Vk, nrm2, nrm, sk, rd);
+  }
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
 }
 
 // ||psi||^2 of a complex column, and whether its imaginary part vanishes.
@@ -179,6 +271,10 @@ __global__ void __launch_bounds__(kVecThreads) cdot_kernel(int64_t n, const cplx
 Workspace::Workspace(Ctx* c) : ctx(c) {
   partials_d.alloc(kMaxGrid);
   partials_c.alloc(kMaxGrid);
+  partials_td.alloc(kMaxGrid);
+  partials_tc.alloc(kMaxGrid);
+  gpart_td.alloc(kRedMaxGroups);
+  gpart_tc.alloc(kRedMaxGroups);
   gpart_d.alloc(kRedMaxGroups);
   gpart_c.alloc(kRedMaxGroups);
   tickets.alloc(8 * (1 + kRedMaxGroups));
@@ -236,25 +332,25 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   const int mode = spmv >= 3000 ? 3 : (spmv >= 2000 ? 2 : 1);
   const int code = spmv % 1000;
   const int variant = (mode == 2) ? spmv - 2000 : ((spmv >= kSpmvTile && mode == 1) ? spmv : -1);
-  DBuf<char> z((n + 32) * vb), scal(64);
+  DBuf<char> z((n + 32) * vb), t((n + 32) * vb), scal(128);
   QD_CUDA(cudaMemsetAsync(z.p, 0, z.bytes(), ctx->stream));
-  QD_CUDA(cudaMemsetAsync(scal.p, 0, 64, ctx->stream));
+  QD_CUDA(cudaMemsetAsync(scal.p, 0, 128, ctx->stream));
   const double one = 1.0;
   QD_CUDA(cudaMemcpyAsync(scal.p, &one, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   const double* s1 = (const double*)scal.p;
   auto launch = [&]() {
     if (mode == 3) {
       QD_REQUIRE(real, QD_ERR_UNSUPPORTED, "vector-kernel timing is for real Hamiltonians");
-      const int vg = vec_grid(ctx, n);
       double* d = (double*)scal.p;
+      const int g = lz_grid(ctx, n / 2 + 1);
       if (code == 1)
-        lz_k2_kernel<double><<<vg, kVecThreads, 0, ctx->stream>>>(n, nullptr, 0, (double*)y.p, (const double*)x.p,
-                                                                   (const double*)z.p, s1, s1, d + 1, d + 2,
-                                                                   W.red_d(2));
+        lz_dots_kernel<double, true><<<g, kLzThreads, 0, ctx->stream>>>(
+            n, nullptr, 0, (const double*)y.p, (const double*)x.p, (const double*)z.p, s1, s1, d + 1, d + 2,
+            reinterpret_cast<Tri<double>*>(d + 6), W.red_tri<double>(2));
       else
-        lz_k3_kernel<double><<<vg, kVecThreads, 0, ctx->stream>>>(n, nullptr, 0, (const double*)y.p,
-                                                                   (const double*)x.p, s1, d + 1, (double*)z.p,
-                                                                   d + 3, d + 4, d + 5, W.red_d(3));
+        lz_update_kernel<double, true><<<g, kLzThreads, 0, ctx->stream>>>(
+            n, nullptr, 0, (const double*)y.p, (const double*)x.p, (const double*)z.p, s1, s1, d + 1, d + 2,
+            (double*)t.p, d + 3, d + 4, d + 5, W.red_d(3));
       QD_CHECK_LAUNCH();
       QD_LAUNCHED(ctx);
       return;
@@ -286,24 +382,18 @@ template <typename MV, typename VV>
 static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int kdim, Workspace& W) {
   Ctx* ctx = H->ctx;
   const int64_t n = H->dim;
-  const int vg = vec_grid(ctx, n);
   for (int k = 1; k <= kdim; ++k) {
     const VV* V1 = B.V.p + (int64_t)(k - 1) * B.ld;
     const VV* V2 = (k >= 2) ? B.V.p + (int64_t)(k - 2) * B.ld : nullptr;
     VV* Vk = B.V.p + (int64_t)k * B.ld;
     const double* s1 = B.scl.p + (k - 1);
     const double* s2 = (k >= 2) ? B.scl.p + (k - 2) : nullptr;
-    // K1: w = s1 * H V1, beta' = s2 <V2, w>
-    launch_spmv<MV, VV>(ctx, H, vals, V1, B.w.p, 1.0, V2, W.red_c_or_d<VV>(1), B.beta.p + k, B.stop.p, k, -1, s1,
-                        s2);
-    lz_k2_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.stop.p, k, B.w.p, V1, V2, s1, s2, B.beta.p + k,
-                                                           B.alpha.p + k, W.red_c_or_d<VV>(2));
-    QD_CHECK_LAUNCH();
-    QD_LAUNCHED(ctx);
-    lz_k3_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.stop.p, k, B.w.p, V1, s1, B.alpha.p + k, Vk,
-                                                           B.nrm2.p + k, B.nrm.p + k, B.scl.p + k, W.red_d(3));
-    QD_CHECK_LAUNCH();
-    QD_LAUNCHED(ctx);
+    // K1: w = s1 * H V1
+    launch_spmv<MV, VV>(ctx, H, vals, V1, B.w.p, 1.0, nullptr, W.red_c_or_d<VV>(1), nullptr, B.stop.p, k, -1, s1,
+                        nullptr);
+    // K2, K3
+    lz_vector_passes<VV>(ctx, n, B.stop.p, k, B.w.p, V1, V2, s1, s2, B.beta.p + k, B.alpha.p + k, B.dots.p + k, Vk,
+                         B.nrm2.p + k, B.nrm.p + k, B.scl.p + k, W.red_tri<VV>(2), W.red_d(3));
   }
 }
 

@@ -23,6 +23,7 @@ struct LanczosBuffers {
   DBuf<VV> V;      // (kdim + 1) x ld basis vectors
   DBuf<VV> w;
   DBuf<VV> alpha, beta;
+  DBuf<Tri<VV>> dots;  // per step: <V2, w>, <V1, w>, <V1, V2>
   DBuf<double> nrm, nrm2, y, scl;  // scl[k] = 1 / ||V[k]|| (basis stored unnormalised)
   DBuf<int> stop;
   cudaGraphExec_t exec = nullptr;
@@ -38,6 +39,7 @@ struct LanczosBuffers {
     w.alloc(ld);
     alpha.alloc(kdim + 2);
     beta.alloc(kdim + 2);
+    dots.alloc(kdim + 2);
     nrm.alloc(kdim + 2);
     nrm2.alloc(kdim + 2);
     y.alloc(kdim + 2);
@@ -79,6 +81,8 @@ struct Workspace {
   Ctx* ctx;
   DBuf<double> partials_d, gpart_d;
   DBuf<cplx> partials_c, gpart_c;
+  DBuf<Tri<double>> partials_td, gpart_td;
+  DBuf<Tri<cplx>> partials_tc, gpart_tc;
   DBuf<unsigned> tickets;
   LanczosBuffers<double> lz_d;
   LanczosBuffers<cplx> lz_c;
@@ -86,6 +90,12 @@ struct Workspace {
   explicit Workspace(Ctx* c);
   GridRed<double> red_d(int slot);
   GridRed<cplx> red_c(int slot);
+  template <typename VV>
+  GridRed<Tri<VV>> red_tri(int slot) {
+    unsigned* t = tickets.p + (size_t)slot * (1 + kRedMaxGroups);
+    if constexpr (std::is_same<VV, double>::value) return GridRed<Tri<double>>{partials_td.p, t, gpart_td.p};
+    else return GridRed<Tri<cplx>>{partials_tc.p, t, gpart_tc.p};
+  }
   template <typename VV>
   GridRed<VV> red_c_or_d(int slot) {
     if constexpr (std::is_same<VV, double>::value) return red_d(slot);

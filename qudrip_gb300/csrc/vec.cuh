@@ -63,6 +63,28 @@ __device__ __forceinline__ cplx ld_ro(const cplx* p) {
   return mkc(d.x, d.y);
 }
 
+// Three sums reduced together in one grid reduction.
+template <typename T>
+struct Tri {
+  T a, b, c;
+};
+template <typename T>
+__device__ __forceinline__ Tri<T> vzero(Tri<T>) {
+  return Tri<T>{vzero(T{}), vzero(T{}), vzero(T{})};
+}
+template <typename T>
+__device__ __forceinline__ Tri<T> vadd(Tri<T> x, Tri<T> y) {
+  return Tri<T>{vadd(x.a, y.a), vadd(x.b, y.b), vadd(x.c, y.c)};
+}
+template <typename T>
+__device__ __forceinline__ Tri<T> shfl_xor(Tri<T> v, int o) {
+  return Tri<T>{shfl_xor(v.a, o), shfl_xor(v.b, o), shfl_xor(v.c, o)};
+}
+template <typename T>
+__device__ __forceinline__ Tri<T> ld_cg(const Tri<T>* p) {
+  return Tri<T>{ld_cg(&p->a), ld_cg(&p->b), ld_cg(&p->c)};
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
