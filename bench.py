@@ -300,6 +300,7 @@ def gpu_arm(args, rank, world, local):
     if not args.no_extras:
         extras["batched_disorder_sweep"] = batched_sweep(ctx)
         extras["jump_trajectories"] = trajectory_ensemble(ctx, with_oracle=not args.no_cpu)
+        extras["serving_mix"] = serving_mix(args.serve_requests)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -438,16 +439,101 @@ def spmv_only(args, local):
     spec, ham = chains.xxz_chain(L)
     sec = q.Sector(spec.index, spec.constraints, ctx=ctx)
     H = sec.lower(ham)
-    kernels = sorted(A.SPMV_KERNELS) if args.spmv_only == 1 else [args.spmv_only]
+    kernels = sorted(A.SPMV_KERNELS) + [A.QD_SPMV_MATRIX_FREE] if args.spmv_only == 9999 else [args.spmv_only]
     hbm_peak, _ = peaks()
     for k in kernels:
         ms = C.c_double(0)
         nb = C.c_double(0)
         A.call("qd_ham_time_spmv", H.handle, k, args.iters, C.byref(ms), C.byref(nb))
         gbs = nb.value / (ms.value * 1e-3) / 1e9
-        print(json.dumps({"kernel": A.SPMV_KERNELS.get(k % 1000, "") + ("+dot" if 2000 <= k < 3000 else "") + ({3001: "lanczos_k2", 3002: "lanczos_k3"}.get(k, "")), "id": k, "ms": ms.value, "GBps": gbs,
+        print(json.dumps({"kernel": ("matrix_free" if k == A.QD_SPMV_MATRIX_FREE else "") + A.SPMV_KERNELS.get(k % 1000, "") + ("+dot" if 2000 <= k < 3000 else "") + ({3001: "lanczos_k2", 3002: "lanczos_k3"}.get(k, "")), "id": k, "ms": ms.value, "GBps": gbs,
                           "frac": gbs / hbm_peak, "matvecs_per_s": 1e3 / ms.value}))
     return 0
+
+
+def serving_requests(n_req, rate, seed):
+    """The serving mix: Poisson arrivals (mean `rate`/s), 70% ground states
+    (Lanczos k=100) and 30% real-time evolutions (T=5, dt=0.05: 100 Krylov
+    steps of dimension 16) on XXZ chains with L uniform in {12,...,22} (Sz=0),
+    Jz ~ U[0,2], and random fields h_i ~ U[-1,1] on half of them."""
+    from qudrip_gb300 import chains
+    rng = np.random.Generator(np.random.PCG64(seed))
+    t = 0.0
+    reqs = []
+    for i in range(n_req):
+        t += rng.exponential(1.0 / rate)
+        L = int(rng.choice([12, 14, 16, 18, 20, 22]))
+        Jz = float(rng.uniform(0.0, 2.0))
+        h = rng.uniform(-1.0, 1.0, size=L) if rng.uniform() < 0.5 else None
+        kind = "ground" if rng.uniform() < 0.7 else "evolve"
+        spec, ham = chains.xxz_chain(L, 1.0, Jz, periodic=True, fields=h)
+        reqs.append(dict(t=t, L=L, kind=kind, spec=spec, ham=ham, seed=int(rng.integers(1 << 62))))
+    return reqs
+
+
+def serve_stream(mode, reqs):
+    """Submits `reqs` at their arrival times; returns results by request index."""
+    import qudrip_gb300 as q
+    srv = q.Server(mode=mode)
+    try:
+        # warm-up: one request of each kind and size class
+        warm = [srv.submit_ground(r["spec"], r["ham"], 100, seed=1) for r in reqs[:4]]
+        warm += [srv.submit_evolve(r["spec"], r["ham"], 0.05, 2, m=16, seed=1) for r in reqs[:2]]
+        srv.wait_all(warm)
+        t0 = srv.now()
+        out = {}
+        ids = {}
+        i = 0
+        while i < len(reqs) or len(out) < len(reqs):
+            now = srv.now() - t0
+            while i < len(reqs) and reqs[i]["t"] <= now:
+                r = reqs[i]
+                if r["kind"] == "ground":
+                    rid = srv.submit_ground(r["spec"], r["ham"], 100, seed=r["seed"], tag=i)
+                else:
+                    rid = srv.submit_evolve(r["spec"], r["ham"], 0.05, 100, m=16, seed=r["seed"], tag=i)
+                ids[rid] = i
+                i += 1
+            wait_ms = 1 if i < len(reqs) else 50
+            for res in srv.poll(256, wait_ms):
+                out[res["tag"]] = res
+        st = srv.stats()
+    finally:
+        srv.close()
+    return out, st
+
+
+def serving_mix(n_req=400, rate=200.0, seed=77):
+    reqs = serving_requests(n_req, rate, seed)
+    summary = {"workload": f"Poisson {rate:.0f} req/s, {n_req} requests: 70% ground state (Lanczos k=100), "
+                           "30% evolution (T=5, dt=0.05, m=16); XXZ L in {12..22} Sz=0, Jz~U[0,2], "
+                           "fields h_i~U[-1,1] on half"}
+    results = {}
+    for mode in ("mixed", "plain"):
+        out, st = serve_stream(mode, reqs)
+        lat = np.array([out[i]["t_done"] - out[i]["t_submit"] for i in range(n_req)])
+        t_first = min(out[i]["t_submit"] for i in range(n_req))
+        t_last = max(out[i]["t_done"] for i in range(n_req))
+        bad = sum(1 for i in range(n_req) if out[i]["status"] != 0)
+        by_kind = {}
+        for kind in ("ground", "evolve"):
+            idx = [i for i in range(n_req) if reqs[i]["kind"] == kind]
+            lk = lat[idx]
+            by_kind[kind] = {"n": len(idx), "p50_ms": 1e3 * float(np.percentile(lk, 50)),
+                             "p99_ms": 1e3 * float(np.percentile(lk, 99))}
+        results[mode] = out
+        summary[mode] = {"solves_per_s": n_req / (t_last - t_first), "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+                         "p99_ms": 1e3 * float(np.percentile(lat, 99)), "failed": bad, "by_kind": by_kind,
+                         "batches": st["batches"], "batched": st["batched"], "max_active": st["max_active"],
+                         "bytes_peak": st["bytes_peak"], "budget": st["budget"]}
+    dE = [abs(results["mixed"][i]["energy"] - results["plain"][i]["energy"]) / abs(results["plain"][i]["energy"])
+          for i in range(n_req) if reqs[i]["kind"] == "ground"]
+    dEv = [abs(results["mixed"][i]["energy"] - results["plain"][i]["energy"]) / abs(results["plain"][i]["energy"])
+           for i in range(n_req) if reqs[i]["kind"] == "evolve"]
+    summary["max_rel_dE_ground_mixed_vs_plain"] = float(max(dE)) if dE else None
+    summary["max_rel_dE_evolved_mixed_vs_plain"] = float(max(dEv)) if dEv else None
+    summary["speedup_solves_per_s"] = summary["mixed"]["solves_per_s"] / summary["plain"]["solves_per_s"]
+    return summary
 
 
 def main():
@@ -459,14 +545,20 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-extras", action="store_true", help="skip the secondary workloads")
     ap.add_argument("--spmv-only", type=int, default=0, metavar="KERNEL",
-                    help="only time CSR product kernel KERNEL (100..105; 1 = all) on the L=24 matrix")
+                    help="only time product KERNEL on the L=24 matrix (100..111 CSR kernels, 1 matrix-free, "
+                         "9999 all)")
     ap.add_argument("--iters", type=int, default=50)
+    ap.add_argument("--serve-only", action="store_true", help="only run the serving mix")
+    ap.add_argument("--serve-requests", type=int, default=400)
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
         return reference_arm(args, rank, world)
     if args.spmv_only:
         return spmv_only(args, local)
+    if args.serve_only:
+        print(json.dumps(serving_mix(args.serve_requests)))
+        return 0
     return gpu_arm(args, rank, world, local)
 
 

@@ -167,6 +167,17 @@ qd_status qd_ham_lower(qd_sector *sec, const qd_term *terms, int nterms,
                        const qd_gate *gates, int ngates, qd_ham **out);
 qd_status qd_ham_destroy(qd_ham *ham);
 qd_status qd_ham_get_info(qd_ham *ham, qd_ham_info *info);
+
+/* Matrix-free form: replaces Operator::map_acc / OperatorSum::map_acc
+ * (operator.hpp:215-232, operator_abel.hpp:36-49).  Compiles the operator
+ * tree into per-support transitions (terms of at most 6 sites, at most 512
+ * state-changing transitions in all) and a stored diagonal; products then read
+ * only the basis, the diagonal and the vectors.  Solvers take it with
+ * qd_lanczos_opts.spmv = QD_SPMV_MATRIX_FREE (built on demand). */
+qd_status qd_ham_build_matrix_free(qd_ham *ham);
+/* y(:, t_out) = H x(:, t_in) through the matrix-free form (x != y). */
+qd_status qd_ham_apply_matrix_free(qd_ham *ham, qd_state *x, int t_in,
+                                   qd_state *y, int t_out);
 /* Reference layout: column pointers (dim+1), row indices sorted within each
  * column, complex values (2*nnz doubles). */
 qd_status qd_ham_download_csc(qd_ham *ham, int64_t *colptr, int32_t *rowidx,
@@ -335,6 +346,133 @@ qd_status qd_csr_expect_noalloc(const int64_t *d_rowptr, const int32_t *d_colidx
                                 const double *d_vals, int64_t dim,
                                 const double *d_psi, double *d_result,
                                 void *stream);
+
+/* ------------------------------------------------------------------ */
+/* Hermitian Lanczos ground state                                     */
+/*   replaces Hermitian::LanczosSolver::getGroundState                */
+/*   (sparse_algorithm.hpp:287-301) with getKrylovReprAd (:72-122)    */
+/*   and getKrylovGS (:206-238)                                       */
+/* Two-vector recurrence (no stored basis), stop once ||r||^2 <= 1e-10; */
+/* the ground-state vector is rebuilt by a second pass and written to    */
+/* psi(:, t).  evals_out (may be NULL) receives res->act_dim eigenvalues  */
+/* of the tridiagonal matrix; one product per step and pass.            */
+/* ------------------------------------------------------------------ */
+qd_status qd_hermitian_lanczos_ground(qd_ham *ham, qd_state *psi, int t, int kry_dim,
+                                      double *evals_out, qd_lanczos_result *res);
+
+/* ------------------------------------------------------------------ */
+/* Short-recurrence Krylov real-time step (Hermitian operators)       */
+/*   same result as qd_arnoldi_evolve (ArnoldiSolver<T,0>::evolve,    */
+/*   sparse_algorithm.hpp:548-562) up to rounding: for Hermitian H the */
+/*   Arnoldi projection is tridiagonal, so the three-term recurrence   */
+/*   builds the same Krylov space with two vector passes per product.  */
+/* m - 1 products, breakdown rule of expandBasis<0>; exp(-i h T) e_0 from  */
+/* the eigen-decomposition of T.  QD_ERR_NOT_HERMITIAN for other H.      */
+/* ------------------------------------------------------------------ */
+qd_status qd_lanczos_evolve(qd_ham *ham, qd_state *psi, int t_in, int t_out,
+                            double h, int m, int *act_dim);
+
+/* ------------------------------------------------------------------ */
+/* Seeded start vectors                                               */
+/* Element i = 2u - 1 with u the (i mod 2)-th uniform double of        */
+/* Philox4x32-10 (key = seed, counter = (i / 2, 0x53544152, 0, 0)).     */
+/* Host-only; the request loop draws the same vector on the device.   */
+/* ------------------------------------------------------------------ */
+qd_status qd_seeded_start(uint64_t seed, int64_t dim, double *host_out);
+
+/* ------------------------------------------------------------------ */
+/* Request loop (serving)                                             */
+/*   no counterpart in the reference, which runs one solve per        */
+/*   process (programs/*.cpp).  A server owns worker lanes on the      */
+/*   context's device, each a CUDA stream driven by a host thread.     */
+/* Requests carry an operator description (sector constraints, terms,  */
+/* gates -- what qd_sector_create / qd_ham_lower take) and are admitted */
+/* in arrival order as lanes free up and as their estimated device      */
+/* footprint fits the byte budget; the sector, the lowered Hamiltonian  */
+/* and the Krylov basis stay resident on the device for the request's   */
+/* lifetime, and requests on different lanes overlap on the GPU.        */
+/* Ground state: Lanczos (krylov_dim steps) from the start vector,      */
+/* result = Ritz vector.  Evolution: nsteps Krylov steps of length dt   */
+/* with dimension m = krylov_dim.                                      */
+/* QD_SERVE_PLAIN runs every request with the FP64 reference            */
+/* algorithms (qd_lanczos_ground, qd_arnoldi_evolve).  QD_SERVE_MIXED   */
+/* batches ground states with dim <= small_dim and a real start vector  */
+/* into one persistent launch per lane pass (qd_batch_lanczos: FP32     */
+/* products and basis, FP64 accumulation and refinement), and evolves   */
+/* Hermitian operators with qd_lanczos_evolve.                          */
+/* ------------------------------------------------------------------ */
+enum { QD_REQ_GROUND = 0, QD_REQ_EVOLVE = 1 };
+enum { QD_SERVE_PLAIN = 0, QD_SERVE_MIXED = 1 };
+enum { QD_PATH_GRID = 0, QD_PATH_BATCH = 1 };
+
+typedef struct qd_server qd_server;
+
+typedef struct qd_server_opts {
+  int32_t mode;         /* QD_SERVE_PLAIN or QD_SERVE_MIXED */
+  int32_t small_lanes;  /* lanes for requests with dim <= small_dim (default 4) */
+  int32_t large_lanes;  /* lanes for any request (default 3) */
+  int32_t batch_lanes;  /* QD_SERVE_MIXED: lanes for batched ground states (default 2) */
+  int32_t batch_max;    /* requests per batched launch (default 64) */
+  int32_t reserved0;
+  int64_t small_dim;    /* default 65536 */
+  int64_t hbm_budget;   /* bytes admitted requests may hold; 0 = 80% of free memory */
+  int32_t reserved[4];
+} qd_server_opts;
+
+typedef struct qd_request {
+  int32_t kind;                /* QD_REQ_GROUND or QD_REQ_EVOLVE */
+  int32_t nbits;
+  int32_t ncons;
+  int32_t tight;
+  const qd_constraint *cons;
+  const qd_term *terms;
+  const qd_gate *gates;
+  int32_t nterms;
+  int32_t ngates;
+  int32_t krylov_dim;          /* ground: Lanczos steps (1..256); evolve: m (2..33) */
+  int32_t nsteps;              /* evolve: number of steps of length dt */
+  double dt;
+  const double *psi0;          /* complex128[psi0_len] start state, copied at submit; NULL: seeded */
+  int64_t psi0_len;            /* must equal the sector dimension when psi0 is given */
+  uint64_t seed;               /* qd_seeded_start(seed, dim) when psi0 is NULL */
+  double *psi_out;             /* complex128 result state, written before the result is posted; or NULL */
+  int64_t psi_out_len;         /* capacity of psi_out in complex elements */
+  uint64_t tag;                /* returned unchanged in the result */
+} qd_request;
+
+typedef struct qd_result {
+  uint64_t id;
+  uint64_t tag;
+  int32_t status;              /* QD_OK or the failing status */
+  int32_t kind;
+  int32_t path;                /* QD_PATH_GRID or QD_PATH_BATCH */
+  int32_t act_dim;             /* Krylov dimension of the (last) solve */
+  int64_t dim;
+  int64_t nnz;
+  int64_t matvecs;
+  int64_t bytes;               /* device bytes the request held */
+  double energy;               /* Re <psi|H|psi> / <psi|psi> of the result state */
+  double ritz;                 /* ground: lowest Ritz value; evolve: 0 */
+  double norm;                 /* ||result state|| */
+  double t_submit, t_admit, t_done;  /* seconds on the server clock */
+} qd_result;
+
+typedef struct qd_server_stats {
+  int64_t submitted, completed, failed, queued, active, max_active;
+  int64_t batches, batched;    /* batched launches and the requests they carried */
+  int64_t bytes_in_use, bytes_peak, budget;
+} qd_server_stats;
+
+qd_status qd_server_create(qd_ctx *ctx, const qd_server_opts *opts, qd_server **out);
+/* Copies the request description and start state; psi_out must stay valid
+ * until the request's result has been polled. */
+qd_status qd_server_submit(qd_server *srv, const qd_request *req, uint64_t *id);
+/* Up to max finished results; waits up to timeout_ms for the first one. */
+qd_status qd_server_poll(qd_server *srv, qd_result *out, int max, int *n, int timeout_ms);
+qd_status qd_server_now(qd_server *srv, double *seconds);
+qd_status qd_server_get_stats(qd_server *srv, qd_server_stats *st);
+/* Finishes the running requests, drops the queued ones, joins the lanes. */
+qd_status qd_server_destroy(qd_server *srv);
 
 #ifdef __cplusplus
 }

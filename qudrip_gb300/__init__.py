@@ -10,5 +10,6 @@ from .operators import (II, id, pauli_x, pauli_y, pauli_z, getQbits, getNset, ge
                         getEmptyOperator, Operator, OperatorSum, QbitsIndex, SectorSpec)
 from .engine import (Context, default_context, Sector, Constrain, LooseConstrain, Hamiltonian,  # noqa: F401
                      State, getState, apply, start_vector, shuffle_state, LanczosSolver, ArnoldiSolver, Arnoldi,
-                     batch_lanczos, traj_run)
+                     batch_lanczos, traj_run, lanczos_evolve, seeded_start, Server, Hermitian,
+                     HermitianLanczosSolver)
 from . import _capi  # noqa: F401

@@ -89,6 +89,43 @@ class qd_traj_stats(C.Structure):
                 ("reserved", C.c_double)]
 
 
+QD_REQ_GROUND = 0
+QD_REQ_EVOLVE = 1
+QD_SERVE_PLAIN = 0
+QD_SERVE_MIXED = 1
+QD_PATH_GRID = 0
+QD_PATH_BATCH = 1
+
+
+class qd_server_opts(C.Structure):
+    _fields_ = [("mode", C.c_int32), ("small_lanes", C.c_int32), ("large_lanes", C.c_int32),
+                ("batch_lanes", C.c_int32), ("batch_max", C.c_int32), ("reserved0", C.c_int32),
+                ("small_dim", C.c_int64), ("hbm_budget", C.c_int64), ("reserved", C.c_int32 * 4)]
+
+
+class qd_request(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("nbits", C.c_int32), ("ncons", C.c_int32), ("tight", C.c_int32),
+                ("cons", C.POINTER(qd_constraint)), ("terms", C.POINTER(qd_term)),
+                ("gates", C.POINTER(qd_gate)), ("nterms", C.c_int32), ("ngates", C.c_int32),
+                ("krylov_dim", C.c_int32), ("nsteps", C.c_int32), ("dt", C.c_double),
+                ("psi0", C.POINTER(C.c_double)), ("psi0_len", C.c_int64), ("seed", C.c_uint64),
+                ("psi_out", C.POINTER(C.c_double)), ("psi_out_len", C.c_int64), ("tag", C.c_uint64)]
+
+
+class qd_result(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("tag", C.c_uint64), ("status", C.c_int32), ("kind", C.c_int32),
+                ("path", C.c_int32), ("act_dim", C.c_int32), ("dim", C.c_int64), ("nnz", C.c_int64),
+                ("matvecs", C.c_int64), ("bytes", C.c_int64), ("energy", C.c_double),
+                ("ritz", C.c_double), ("norm", C.c_double), ("t_submit", C.c_double),
+                ("t_admit", C.c_double), ("t_done", C.c_double)]
+
+
+class qd_server_stats(C.Structure):
+    _fields_ = [(k, C.c_int64) for k in ("submitted", "completed", "failed", "queued", "active",
+                                         "max_active", "batches", "batched", "bytes_in_use",
+                                         "bytes_peak", "budget")]
+
+
 class QDError(RuntimeError):
     def __init__(self, code: int, where: str, msg: str):
         super().__init__(f"{where}: status {code} ({msg})")
@@ -132,6 +169,8 @@ _SIGNATURES = {
     "qd_ham_lower": [_P, C.POINTER(qd_term), C.c_int, C.POINTER(qd_gate), C.c_int, _PP],
     "qd_ham_destroy": [_P],
     "qd_ham_get_info": [_P, C.POINTER(qd_ham_info)],
+    "qd_ham_build_matrix_free": [_P],
+    "qd_ham_apply_matrix_free": [_P, _P, C.c_int, _P, C.c_int],
     "qd_ham_download_csc": [_P, _I64P, C.POINTER(C.c_int32), _DP],
     "qd_ham_download_csr": [_P, _I64P, C.POINTER(C.c_int32), _DP],
     "qd_state_create": [_P, C.c_int64, C.c_int, _PP],
@@ -144,6 +183,15 @@ _SIGNATURES = {
     "qd_state_eval": [_P, C.c_int, _P, _DP],
     "qd_lanczos_ground": [_P, _P, C.c_int, C.POINTER(qd_lanczos_opts), _DP,
                           C.POINTER(qd_lanczos_result)],
+    "qd_hermitian_lanczos_ground": [_P, _P, C.c_int, C.c_int, _DP, C.POINTER(qd_lanczos_result)],
+    "qd_lanczos_evolve": [_P, _P, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int)],
+    "qd_seeded_start": [C.c_uint64, C.c_int64, _DP],
+    "qd_server_create": [_P, C.POINTER(qd_server_opts), _PP],
+    "qd_server_submit": [_P, C.POINTER(qd_request), C.POINTER(C.c_uint64)],
+    "qd_server_poll": [_P, C.POINTER(qd_result), C.c_int, C.POINTER(C.c_int), C.c_int],
+    "qd_server_now": [_P, _DP],
+    "qd_server_get_stats": [_P, C.POINTER(qd_server_stats)],
+    "qd_server_destroy": [_P],
 }
 _RESTYPES = {"qd_status_string": C.c_char_p, "qd_last_error": C.c_char_p,
              "qd_api_version": C.c_int}

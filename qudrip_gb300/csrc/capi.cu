@@ -273,6 +273,26 @@ qd_status qd_ham_get_info(qd_ham* ham, qd_ham_info* info) {
   });
 }
 
+qd_status qd_ham_build_matrix_free(qd_ham* ham) {
+  return guard([&] {
+    QD_REQUIRE(ham, QD_ERR_INVALID, "null argument");
+    DeviceGuard dg(ham->ctx->device);
+    ham_build_matrix_free(ham);
+  });
+}
+
+qd_status qd_ham_apply_matrix_free(qd_ham* ham, qd_state* x, int t_in, qd_state* y, int t_out) {
+  return guard([&] {
+    QD_REQUIRE(ham && x && y, QD_ERR_INVALID, "null argument");
+    QD_REQUIRE(x->dim == ham->dim && y->dim == ham->dim, QD_ERR_INVALID, "dimension mismatch");
+    QD_REQUIRE(t_in >= 0 && t_in < x->nt && t_out >= 0 && t_out < y->nt, QD_ERR_INVALID, "bad column");
+    QD_REQUIRE(x->col(t_in) != y->col(t_out), QD_ERR_INVALID, "in-place product");
+    DeviceGuard dg(ham->ctx->device);
+    mf_apply_c(ham, x->col(t_in), y->col(t_out));
+    QD_CUDA(cudaStreamSynchronize(ham->ctx->stream));
+  });
+}
+
 qd_status qd_ham_download_csr(qd_ham* ham, int64_t* rowptr, int32_t* colidx, double* vals) {
   return guard([&] {
     QD_REQUIRE(ham && rowptr, QD_ERR_INVALID, "null argument");
@@ -412,7 +432,6 @@ qd_status qd_lanczos_ground(qd_ham* ham, qd_state* psi, int t, const qd_lanczos_
     QD_REQUIRE(opts->spmv == QD_SPMV_CSR || opts->spmv == QD_SPMV_MATRIX_FREE, QD_ERR_INVALID, "bad spmv kind");
     QD_REQUIRE(opts->ritz == QD_RITZ_STORED_BASIS || opts->ritz == QD_RITZ_SECOND_PASS, QD_ERR_INVALID,
                "bad ritz mode");
-    QD_REQUIRE(opts->spmv == QD_SPMV_CSR, QD_ERR_UNSUPPORTED, "matrix-free Lanczos is not built yet");
     DeviceGuard dg(ham->ctx->device);
     std::memset(res, 0, sizeof(*res));
     lanczos_ground(ham, psi->col(t), *opts, evals_out, res);
@@ -422,7 +441,7 @@ qd_status qd_lanczos_ground(qd_ham* ham, qd_state* psi, int t, const qd_lanczos_
 qd_status qd_ham_time_spmv(qd_ham* ham, int spmv, int iters, double* avg_ms, double* bytes_per_launch) {
   return guard([&] {
     QD_REQUIRE(ham && avg_ms && bytes_per_launch && iters >= 1, QD_ERR_INVALID, "bad argument");
-    const bool plain = spmv == QD_SPMV_CSR || (spmv >= kSpmvTile && spmv <= kSpmvLast);
+    const bool plain = spmv == QD_SPMV_CSR || spmv == QD_SPMV_MATRIX_FREE || (spmv >= kSpmvTile && spmv <= kSpmvLast);
     const bool fused = spmv >= 2000 + kSpmvTile && spmv <= 2000 + kSpmvLast;
     const bool vec = spmv == 3001 || spmv == 3002;
     QD_REQUIRE(plain || fused || vec, QD_ERR_UNSUPPORTED, "qd_ham_time_spmv: unknown kernel code %d", spmv);
@@ -439,6 +458,29 @@ qd_status qd_arnoldi_evolve(qd_ham* ham, qd_state* psi, int t_in, int t_out, dou
     QD_REQUIRE(t_in >= 0 && t_in < psi->nt && t_out >= 0 && t_out < psi->nt, QD_ERR_INVALID, "bad column");
     DeviceGuard dg(ham->ctx->device);
     arnoldi_evolve(ham, psi->col(t_in), psi->col(t_out), h, m, act_dim);
+  });
+}
+
+qd_status qd_hermitian_lanczos_ground(qd_ham* ham, qd_state* psi, int t, int kry_dim, double* evals_out,
+                                      qd_lanczos_result* res) {
+  return guard([&] {
+    QD_REQUIRE(ham && psi && res, QD_ERR_INVALID, "null argument");
+    QD_REQUIRE(t >= 0 && t < psi->nt, QD_ERR_INVALID, "bad column");
+    QD_REQUIRE(psi->dim == ham->dim, QD_ERR_INVALID, "dimension mismatch");
+    DeviceGuard dg(ham->ctx->device);
+    std::memset(res, 0, sizeof(*res));
+    hermitian_lanczos_ground(ham, psi->col(t), kry_dim, evals_out, res);
+  });
+}
+
+qd_status qd_lanczos_evolve(qd_ham* ham, qd_state* psi, int t_in, int t_out, double h, int m, int* act_dim) {
+  return guard([&] {
+    QD_REQUIRE(ham && psi, QD_ERR_INVALID, "null argument");
+    QD_REQUIRE(psi->dim == ham->dim, QD_ERR_INVALID, "dimension mismatch");
+    QD_REQUIRE(t_in >= 0 && t_in < psi->nt && t_out >= 0 && t_out < psi->nt, QD_ERR_INVALID, "bad column");
+    QD_REQUIRE(m >= 2 && m <= 33, QD_ERR_UNSUPPORTED, "Krylov dimension m must be in 2..33");
+    DeviceGuard dg(ham->ctx->device);
+    lanczos_evolve(ham, psi->col(t_in), psi->col(t_out), h, m, act_dim);
   });
 }
 

@@ -65,26 +65,45 @@ qd_status guard(F&& f) {
 }
 
 // ---------------------------------------------------------------- device buffers
-// Owning device buffer (cudaMalloc / cudaFree); never copied.
+// Stream on which this thread's DBuf allocations are ordered.  Null (the
+// default) means cudaMalloc / cudaFree.  Request-loop worker threads set their
+// lane's stream, so their allocations come from the stream-ordered pool
+// (cudaMallocAsync / cudaFreeAsync), which does not serialise the other
+// lanes' kernels the way cudaMalloc / cudaFree do.
+inline cudaStream_t& alloc_stream() {
+  static thread_local cudaStream_t s = nullptr;
+  return s;
+}
+struct AllocStreamScope {
+  cudaStream_t prev;
+  explicit AllocStreamScope(cudaStream_t s) : prev(alloc_stream()) { alloc_stream() = s; }
+  ~AllocStreamScope() { alloc_stream() = prev; }
+};
+
+// Owning device buffer; never copied.
 template <typename T>
 struct DBuf {
   T* p = nullptr;
   size_t n = 0;
+  cudaStream_t s = nullptr;  // stream the buffer was allocated on (stream-ordered pool), or null
   DBuf() = default;
   explicit DBuf(size_t count) { alloc(count); }
   DBuf(const DBuf&) = delete;
   DBuf& operator=(const DBuf&) = delete;
-  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n) {
+  DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), s(o.s) {
     o.p = nullptr;
     o.n = 0;
+    o.s = nullptr;
   }
   DBuf& operator=(DBuf&& o) noexcept {
     if (this != &o) {
       release();
       p = o.p;
       n = o.n;
+      s = o.s;
       o.p = nullptr;
       o.n = 0;
+      o.s = nullptr;
     }
     return *this;
   }
@@ -92,13 +111,23 @@ struct DBuf {
   void alloc(size_t count) {
     release();
     if (count == 0) count = 1;
-    QD_CUDA(cudaMalloc((void**)&p, count * sizeof(T)));
+    s = alloc_stream();
+    if (s)
+      QD_CUDA(cudaMallocAsync((void**)&p, count * sizeof(T), s));
+    else
+      QD_CUDA(cudaMalloc((void**)&p, count * sizeof(T)));
     n = count;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (s)
+        cudaFreeAsync(p, s);
+      else
+        cudaFree(p);
+    }
     p = nullptr;
     n = 0;
+    s = nullptr;
   }
   size_t bytes() const { return n * sizeof(T); }
 };

@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(kEvThreads) ev_combine_kernel(int64_t n, const
   }
 }
 
-void ArnoldiBuffers::ensure(int64_t n_, int m_, int grid) {
+void ArnoldiBuffers::ensure(int64_t n_, int m_, int grid, cudaStream_t stream) {
   if (n_ == n && m_ == m && grid <= grid_cap) return;
   n = n_;
   m = m_;
@@ -164,7 +164,7 @@ void ArnoldiBuffers::ensure(int64_t n_, int m_, int grid) {
   partials.alloc((size_t)grid_cap * 32);
   rpart.alloc(kMaxGrid);
   tickets.alloc(4);
-  QD_CUDA(cudaMemset(tickets.p, 0, 4 * sizeof(unsigned)));
+  QD_CUDA(cudaMemsetAsync(tickets.p, 0, 4 * sizeof(unsigned), stream));
 }
 
 template <typename MV>
@@ -212,7 +212,7 @@ void arnoldi_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int 
   if (!H->arnoldi) H->arnoldi.reset(new ArnoldiBuffers());
   ArnoldiBuffers& B = *H->arnoldi;
   const int g = ev_grid(ctx, n);
-  B.ensure(n, m, g);
+  B.ensure(n, m, g, ctx->stream);
   // v_0 = psi / ||psi||
   ev_norm_only_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, psi_in, B.nrm2.p, GridRed<double>{B.rpart.p, B.tickets.p + 1});
   QD_CHECK_LAUNCH();

@@ -20,7 +20,7 @@ struct ArnoldiBuffers {
   DBuf<cplx> partials;  // grid x 32 multi-dot partials
   DBuf<double> rpart;
   DBuf<unsigned> tickets;
-  void ensure(int64_t n_, int m_, int grid);
+  void ensure(int64_t n_, int m_, int grid, cudaStream_t stream);
 };
 
 void arnoldi_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int m, int* act_out);

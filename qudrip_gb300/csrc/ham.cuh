@@ -5,7 +5,7 @@
 //   colidx  int32[nnz]     columns, ascending within each row
 //   vals_c  cplx[nnz]      complex128 values (bit-identical to the reference)
 //   vals_r  double[nnz]    real part, only when every imaginary part is 0
-//   diag_r  double[dim]    real diagonal (matrix-free path)
+//   diag_r  double[dim]    diagonal of the matrix-free form (diag_c if complex)
 // The reference's CSC layout is produced on demand by transposing.
 #pragma once
 
@@ -38,24 +38,34 @@ struct TermDev {
   int pad;
 };
 
-// Matrix-free description: the Hamiltonian split into a diagonal (stored)
-// and off-diagonal "flip" terms, each acting on a small support.
-struct MfTerm {
-  uint64_t support;   // bits the term changes or reads
-  uint64_t jw_mask;   // bits outside the support whose parity flips the sign
-  int nsup;           // number of support bits (<= kMfMaxSupport)
-  int ntrans;         // transitions stored at trans_offset
-  int trans_offset;
-  int pad;
+// Matrix-free form: the operator compiled into "entries", one per (term,
+// input pattern on the term's support) that changes the state.  Row r
+// (state s) receives amp * sign * x[rank(c)] from every entry with
+// (s & sup) == outb, where c = s ^ flip and sign = (-1)^popcount(c & jw)
+// (the Jordan-Wigner parity of the bits outside the support).  Entries that
+// keep the state are summed once into the stored diagonal.
+struct MfEntry {
+  uint64_t sup;   // support bits of the term
+  uint64_t outb;  // output pattern (support bits of the row state)
+  uint64_t flip;  // input ^ output
+  uint64_t jw;    // bits outside the support whose parity flips the sign
+  cplx amp;       // coefficient * leaf sum (sign from jw excluded)
 };
 
-struct MfTrans {
-  uint32_t in_local;   // local input configuration (support bits compressed)
-  uint32_t out_local;  // local output configuration
-  cplx amp;            // coefficient * product of gate amplitudes (sign from jw_mask excluded)
+// Ranking of a product sector by byte tables: for field f, byte b of its
+// value v, and cb set bits below that byte, tab[off_f + (b * 256 + byte) *
+// (k_f + 1) + cb] is the byte's share of the colex rank.
+struct MfRank {
+  int nf;
+  int pad;
+  int lo[4], width[4], k[4], is_free[4], nb[4];
+  int64_t stride[4];
+  int64_t off[4];
+  const int64_t* tab;
 };
 
 constexpr int kMfMaxSupport = 6;
+constexpr int kMfMaxEntries = 512;
 
 }  // namespace qd
 
@@ -73,13 +83,16 @@ struct qd_ham {
   qd::DBuf<double> vals_r;
   qd::DBuf<float> vals_f;  // fp32 copy of vals_r for the mixed-precision SpMV
   qd::DBuf<int32_t> row_order;  // rows by decreasing length inside 256-row windows (kernel 111)
-  // matrix-free form
+  // matrix-free form (qd_ham_build_matrix_free)
   bool has_mf = false;
-  qd::DBuf<double> diag_r;
-  qd::DBuf<qd::MfTerm> mf_terms;
-  qd::DBuf<qd::MfTrans> mf_trans;
-  int mf_nterms = 0;
-  double mf_uniform_amp = 0.0;  // when every off-diagonal transition has this real amplitude
+  bool mf_real = false;      // every amplitude and diagonal entry is real
+  bool mf_tables = false;    // product sector ranked by byte tables (else sector_rank)
+  int mf_nent = 0;
+  qd::DBuf<qd::MfEntry> mf_ent;
+  qd::DBuf<double> diag_r;   // real diagonal (mf_real)
+  qd::DBuf<cplx> diag_c;     // complex diagonal
+  qd::DBuf<int64_t> mf_tab;
+  qd::MfRank mf_rank{};
   std::vector<qd_term> host_terms;
   std::vector<qd_gate> host_gates;
   std::unique_ptr<qd::Workspace, qd::WorkspaceDeleter> ws;  // solver buffers, reused across calls
@@ -91,5 +104,6 @@ void ham_lower(qd_ham* H, const qd_term* terms, int nterms, const qd_gate* gates
 void ham_transpose(Ctx* ctx, int64_t n, const int64_t* ptr, const int32_t* idx, const cplx* vals,
                    int64_t nnz, int64_t* out_ptr, int32_t* out_idx, cplx* out_vals);
 void ham_build_matrix_free(qd_ham* H);
+void mf_apply_c(qd_ham* H, const cplx* x, cplx* y);
 void ham_ensure_row_order(qd_ham* H);
 }  // namespace qd

@@ -259,6 +259,17 @@ __global__ void __launch_bounds__(kVecThreads) ritz_kernel(int64_t n, const VV* 
   }
 }
 
+// psi = sum_k y_k V[k] with complex coefficients (the Krylov exponential).
+template <typename VV>
+__global__ void __launch_bounds__(kVecThreads) combine_kernel(int64_t n, const VV* V, int64_t ld, const cplx* y,
+                                                              int act, cplx* psi) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    cplx acc = vfma(y[0], V[i], mkc(0.0, 0.0));
+    for (int k = 1; k < act; ++k) acc = vfma(y[k], V[(int64_t)k * ld + i], acc);
+    psi[i] = acc;
+  }
+}
+
 // <a, b> over complex columns (a^dagger b).
 __global__ void __launch_bounds__(kVecThreads) cdot_kernel(int64_t n, const cplx* a, const cplx* b, cplx* out,
                                                            GridRed<cplx> red) {
@@ -318,6 +329,22 @@ cplx state_eval(qd_ham* H, const cplx* psi) {
   return h;
 }
 
+// ||psi||^2 on the Hamiltonian's stream.
+double state_norm2(qd_ham* H, const cplx* psi) {
+  Ctx* ctx = H->ctx;
+  Workspace& W = ham_workspace(H);
+  DBuf<double> nrm2(1);
+  DBuf<int> has_im(1);
+  QD_CUDA(cudaMemsetAsync(has_im.p, 0, sizeof(int), ctx->stream));
+  colnorm_kernel<<<vec_grid(ctx, H->dim), kVecThreads, 0, ctx->stream>>>(H->dim, psi, nrm2.p, W.red_d(0), has_im.p);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  double h = 0.0;
+  QD_CUDA(cudaMemcpyAsync(&h, nrm2.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  return h;
+}
+
 // The product the real Lanczos path launches, timed back to back.
 void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per_launch) {
   Ctx* ctx = H->ctx;
@@ -338,7 +365,16 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   const double one = 1.0;
   QD_CUDA(cudaMemcpyAsync(scal.p, &one, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   const double* s1 = (const double*)scal.p;
+  const bool mf = (spmv == QD_SPMV_MATRIX_FREE);
+  if (mf) ham_build_matrix_free(H);
   auto launch = [&]() {
+    if (mf) {
+      if (H->mf_real && real)
+        launch_mf<double>(ctx, H, (const double*)x.p, (double*)y.p, 1.0, nullptr, nullptr, 0);
+      else
+        launch_mf<cplx>(ctx, H, (const cplx*)x.p, (cplx*)y.p, 1.0, nullptr, nullptr, 0);
+      return;
+    }
     if (mode == 3) {
       QD_REQUIRE(real, QD_ERR_UNSUPPORTED, "vector-kernel timing is for real Hamiltonians");
       double* d = (double*)scal.p;
@@ -375,11 +411,13 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   *avg_ms = (double)ms / iters;
   const double mvb = real ? 8.0 : 16.0;
   *bytes_per_launch = (double)H->nnz * (mvb + 4.0) + (double)(n + 1) * 8.0 + (double)n * 2.0 * (double)vb;
+  if (mf)  // basis word, diagonal, x[r], y[r] per row (the gathered x comes from L2)
+    *bytes_per_launch = (double)n * (8.0 + (H->mf_real ? 8.0 : 16.0) + 2.0 * (double)vb);
 }
 
 // ---------------------------------------------------------------- Lanczos
 template <typename MV, typename VV>
-static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int kdim, Workspace& W) {
+static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int kdim, Workspace& W, bool mf) {
   Ctx* ctx = H->ctx;
   const int64_t n = H->dim;
   for (int k = 1; k <= kdim; ++k) {
@@ -388,9 +426,12 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int kd
     VV* Vk = B.V.p + (int64_t)k * B.ld;
     const double* s1 = B.scl.p + (k - 1);
     const double* s2 = (k >= 2) ? B.scl.p + (k - 2) : nullptr;
-    // K1: w = s1 * H V1
-    launch_spmv<MV, VV>(ctx, H, vals, V1, B.w.p, 1.0, nullptr, W.red_c_or_d<VV>(1), nullptr, B.stop.p, k, -1, s1,
-                        nullptr);
+    // K1: w = s1 * H V1 (CSR, or matrix-free)
+    if (mf)
+      launch_mf<VV>(ctx, H, V1, B.w.p, 1.0, s1, B.stop.p, k);
+    else
+      launch_spmv<MV, VV>(ctx, H, vals, V1, B.w.p, 1.0, nullptr, W.red_c_or_d<VV>(1), nullptr, B.stop.p, k, -1, s1,
+                          nullptr);
     // K2, K3
     lz_vector_passes<VV>(ctx, n, B.stop.p, k, B.w.p, V1, V2, s1, s2, B.beta.p + k, B.alpha.p + k, B.dots.p + k, Vk,
                          B.nrm2.p + k, B.nrm.p + k, B.scl.p + k, W.red_tri<VV>(2), W.red_d(3));
@@ -433,7 +474,12 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
   const bool timing = std::getenv("QD_TIMING") != nullptr;
   const auto host_t0 = std::chrono::steady_clock::now();
   if (timing) QD_CUDA(cudaEventRecord(ctx->events[12], ctx->stream));
-  B.run_graph(ctx, [&]() { lanczos_run<MV, VV>(H, vals, B, kdim, W); });
+  const bool mf = (o.spmv == QD_SPMV_MATRIX_FREE);
+  if (B.kind != (int)mf) {
+    B.drop_graph();
+    B.kind = (int)mf;
+  }
+  B.run_graph(ctx, [&]() { lanczos_run<MV, VV>(H, vals, B, kdim, W, mf); });
   if (timing) QD_CUDA(cudaEventRecord(ctx->events[13], ctx->stream));
   int matvecs = kdim;
 
@@ -463,7 +509,7 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
     QD_CHECK_LAUNCH();
     QD_LAUNCHED(ctx);
     QD_CUDA(cudaMemsetAsync(B.stop.p, 0, sizeof(int), ctx->stream));
-    lanczos_run<MV, VV>(H, vals, B, act, W);
+    lanczos_run<MV, VV>(H, vals, B, act, W, mf);
     matvecs += act;
   }
   // psi = sum_k y_k v_k = sum_k (y_k s_k) V[k]
@@ -511,13 +557,262 @@ void lanczos_ground(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, double* eval
   QD_CUDA(cudaMemcpyAsync(&hn, nrm2.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
   QD_REQUIRE(hn > 0.0 && std::isfinite(hn), QD_ERR_INVALID, "start vector has zero or non-finite norm");
-  const bool real_h = (H->flags & QD_HAM_REAL) != 0;
+  if (o.spmv == QD_SPMV_MATRIX_FREE) ham_build_matrix_free(H);
+  const bool real_h = (o.spmv == QD_SPMV_MATRIX_FREE) ? H->mf_real : (H->flags & QD_HAM_REAL) != 0;
   if (real_h && !him)
     lanczos_ground_impl<double, double>(H, psi, nrm2.p, o, evals_out, res);
   else if (real_h)
     lanczos_ground_impl<double, cplx>(H, psi, nrm2.p, o, evals_out, res);
   else
     lanczos_ground_impl<cplx, cplx>(H, psi, nrm2.p, o, evals_out, res);
+}
+
+// ---------------------------------------------------------------- Hermitian::LanczosSolver
+// Hermitian::LanczosSolver::getGroundState (sparse_algorithm.hpp:287-301):
+// getKrylovReprAd (:72-122) keeps two vectors v, w and alternates which one
+// is rebuilt; step i takes x (the newest vector) and p (the one before):
+//   a_i = <x, H x>,  p = H x - a_i x - sqrt(nn_{i-1}) p,  nn_i = ||p||^2,
+//   p /= sqrt(nn_i),  and stops once nn_i <= 1e-10 (qudrip.hpp:18).
+// The reference forms H x twice per step (once inside <x, H x>, once for the
+// update); here one product serves both, with the inner product fused into
+// it.  The lowest eigenvector z of tridiag(Re a, sqrt nn) is then expanded
+// by getKrylovGS (:206-238): a second pass regenerates the same vectors with
+// the same kernels (same bits) and accumulates psi = sum_i z_i x_i, so only
+// three vectors of the space are ever held.
+__device__ __forceinline__ double as_vv(double b, double) { return b; }
+__device__ __forceinline__ cplx as_vv(double b, cplx) { return mkc(b, 0.0); }
+
+__device__ __forceinline__ bool hstopped(const int* stop, int step) {
+  const int st = *stop;
+  return st != 0 && step >= st;
+}
+
+template <typename VV>
+__global__ void __launch_bounds__(kVecThreads) herm_update_kernel(int64_t n, int* stop, int step, const VV* h,
+                                                                  const VV* x, VV* p, const VV* a,
+                                                                  const double* nn_prev, double* nn_out,
+                                                                  GridRed<double> red) {
+  if (hstopped(stop, step)) return;
+  const VV ai = *a;
+  const double b = nn_prev ? sqrt(*nn_prev) : 0.0;
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    VV o = vsubmul(h[i], ai, x[i]);
+    if (nn_prev) o = vsubmul(o, as_vv(b, VV{}), p[i]);
+    p[i] = o;
+    acc += vnorm2(o);
+  }
+  if (grid_sum(acc, red, nn_out) && threadIdx.x == 0) {
+    if (!(*nn_out > 1e-10)) *stop = step + 1;
+  }
+}
+
+template <typename VV>
+__global__ void __launch_bounds__(kVecThreads) herm_scale_kernel(int64_t n, const int* stop, int step, VV* p,
+                                                                 const double* nn) {
+  if (hstopped(stop, step)) return;
+  const double inv = 1.0 / sqrt(*nn);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = vscale(inv, p[i]);
+}
+
+template <typename VV>
+__global__ void __launch_bounds__(kVecThreads) herm_accum_kernel(int64_t n, double z, const VV* x, cplx* psi,
+                                                                 int first) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const cplx xi = to_c(x[i]);
+    psi[i] = first ? mkc(z * xi.re, z * xi.im) : mkc(fma(z, xi.re, psi[i].re), fma(z, xi.im, psi[i].im));
+  }
+}
+
+template <typename MV, typename VV>
+static void herm_lanczos_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, int kdim, double* evals_out,
+                              qd_lanczos_result* res) {
+  Ctx* ctx = H->ctx;
+  const int64_t n = H->dim;
+  Workspace& W = ham_workspace(H);
+  const MV* vals = nullptr;
+  if constexpr (std::is_same<MV, double>::value) vals = H->vals_r.p;
+  else vals = H->vals_c.p;
+  const int vg = vec_grid(ctx, n);
+  DBuf<VV> v(n), w(n), h(n), a(kdim + 1);
+  DBuf<double> nn(kdim + 1);
+  DBuf<int> stop(1);
+  DBuf<cplx> start(n);
+  QD_CUDA(cudaMemcpyAsync(start.p, psi, n * sizeof(cplx), cudaMemcpyDeviceToDevice, ctx->stream));
+  int64_t matvecs = 0;
+  // one pass: steps 0..kdim-1 (accumulating psi += z_i x_i when z is given)
+  auto pass = [&](const std::vector<double>* z, int K) {
+    QD_CUDA(cudaMemsetAsync(stop.p, 0, sizeof(int), ctx->stream));
+    init_v0_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, start.p, psi_nrm2, v.p);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+    const int steps = z ? K : kdim;
+    for (int i = 0; i < steps; ++i) {
+      VV* x = (i % 2 == 0) ? v.p : w.p;
+      VV* pp = (i % 2 == 0) ? w.p : v.p;
+      if (z) {
+        herm_accum_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, (*z)[i], x, psi, i == 0);
+        QD_CHECK_LAUNCH();
+        QD_LAUNCHED(ctx);
+        if (i == K - 1) break;
+      }
+      launch_spmv<MV, VV>(ctx, H, vals, x, h.p, 1.0, x, W.red_c_or_d<VV>(1), a.p + i, stop.p, i + 1, -1);
+      ++matvecs;
+      herm_update_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, stop.p, i, h.p, x, pp, a.p + i,
+                                                                  i ? nn.p + i - 1 : nullptr, nn.p + i, W.red_d(3));
+      QD_CHECK_LAUNCH();
+      QD_LAUNCHED(ctx);
+      herm_scale_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, stop.p, i, pp, nn.p + i);
+      QD_CHECK_LAUNCH();
+      QD_LAUNCHED(ctx);
+    }
+  };
+  pass(nullptr, 0);
+  std::vector<VV> ha(kdim + 1);
+  std::vector<double> hnn(kdim + 1);
+  int st = 0;
+  QD_CUDA(cudaMemcpyAsync(ha.data(), a.p, (kdim + 1) * sizeof(VV), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(hnn.data(), nn.p, (kdim + 1) * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(&st, stop.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  const int K = st ? st : kdim;
+  std::vector<double> d(K), e(K), ev(K), z(K);
+  for (int i = 0; i < K; ++i) {
+    d[i] = real_part(ha[i]);
+    e[i] = (i + 1 < K) ? std::sqrt(hnn[i]) : 0.0;
+  }
+  QD_REQUIRE(tridiag_lowest<double>(K, d.data(), e.data(), ev.data(), z.data()) == 0, QD_ERR_INVALID,
+             "tridiagonal eigensolver did not converge");
+  pass(&z, K);
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (evals_out) std::memcpy(evals_out, ev.data(), K * sizeof(double));
+  res->act_dim = K;
+  res->breakdown = st ? 1 : 0;
+  (void)matvecs;
+  res->matvecs = 2 * K - 1;  // K products in the first pass, K - 1 in the second
+  res->ritz_value = ev[0];
+  res->err = std::sqrt(hnn[K - 1]);
+}
+
+void hermitian_lanczos_ground(qd_ham* H, cplx* psi, int kdim, double* evals_out, qd_lanczos_result* res) {
+  Ctx* ctx = H->ctx;
+  const int64_t n = H->dim;
+  QD_REQUIRE(kdim >= 1 && kdim <= 4096, QD_ERR_INVALID, "krylov_dim must be in 1..4096");
+  QD_REQUIRE(H->flags & QD_HAM_HERMITIAN, QD_ERR_NOT_HERMITIAN, "Hermitian::LanczosSolver needs a Hermitian operator");
+  Workspace& W = ham_workspace(H);
+  DBuf<double> nrm2(1);
+  DBuf<int> has_im(1);
+  QD_CUDA(cudaMemsetAsync(has_im.p, 0, sizeof(int), ctx->stream));
+  colnorm_kernel<<<vec_grid(ctx, n), kVecThreads, 0, ctx->stream>>>(n, psi, nrm2.p, W.red_d(0), has_im.p);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  int him = 0;
+  double hn = 0.0;
+  QD_CUDA(cudaMemcpyAsync(&him, has_im.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(&hn, nrm2.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  QD_REQUIRE(hn > 0.0 && std::isfinite(hn), QD_ERR_INVALID, "start vector has zero or non-finite norm");
+  const bool real_h = (H->flags & QD_HAM_REAL) != 0;
+  if (real_h && !him)
+    herm_lanczos_impl<double, double>(H, psi, nrm2.p, kdim, evals_out, res);
+  else if (real_h)
+    herm_lanczos_impl<double, cplx>(H, psi, nrm2.p, kdim, evals_out, res);
+  else
+    herm_lanczos_impl<cplx, cplx>(H, psi, nrm2.p, kdim, evals_out, res);
+}
+
+// ---------------------------------------------------------------- Hermitian Krylov exponential
+// psi_out = V exp(-i h T) e_0 with the Lanczos basis V of psi_in and its
+// tridiagonal projection T: for Hermitian H the Arnoldi projection of
+// ArnoldiSolver<T,0>::evolve (sparse_algorithm.hpp:548-562) is tridiagonal,
+// so the three-term recurrence reaches the same Krylov space with 2 vector
+// passes per product instead of a Gram-Schmidt sweep over the whole basis.
+// m - 1 products as the reference's expandBasis<0>; a breakdown at step s
+// keeps s basis vectors (the expandBasis<0> count, sparse_algorithm.hpp:
+// 387-390).  exp(-i h T) e_0 = Q exp(-i h Lambda) Q^T e_0 from the QL
+// eigen-decomposition of T.  The output has the input norm dropped.
+template <typename MV>
+static void lanczos_evolve_impl(qd_ham* H, const cplx* psi_in, cplx* psi_out, const double* psi_nrm2, double h,
+                                int m, int* act_out) {
+  Ctx* ctx = H->ctx;
+  const int64_t n = H->dim;
+  const int kdim = m - 1;
+  Workspace& W = ham_workspace(H);
+  LanczosBuffers<cplx>& B = buffers_for<cplx>(W, n, kdim);
+  const MV* vals = nullptr;
+  if constexpr (std::is_same<MV, double>::value) vals = H->vals_r.p;
+  else vals = H->vals_c.p;
+  const int vg = vec_grid(ctx, n);
+  QD_CUDA(cudaMemsetAsync(B.stop.p, 0, sizeof(int), ctx->stream));
+  const double one = 1.0;
+  QD_CUDA(cudaMemcpyAsync(B.scl.p, &one, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  init_v0_kernel<cplx><<<vg, kVecThreads, 0, ctx->stream>>>(n, psi_in, psi_nrm2, B.V.p);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  if (B.kind != 0) {
+    B.drop_graph();
+    B.kind = 0;
+  }
+  B.run_graph(ctx, [&]() { lanczos_run<MV, cplx>(H, vals, B, kdim, W, false); });
+  std::vector<cplx> alpha(kdim + 1);
+  std::vector<double> nrm(kdim + 1), scl(kdim + 1);
+  int stop = 0;
+  QD_CUDA(cudaMemcpyAsync(alpha.data(), B.alpha.p, (kdim + 1) * sizeof(cplx), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(nrm.data(), B.nrm.p, (kdim + 1) * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(scl.data(), B.scl.p, (kdim + 1) * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(&stop, B.stop.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  const int act = stop ? stop : kdim;
+  std::vector<double> d(act), e(act), z((size_t)act * act, 0.0);
+  for (int i = 0; i < act; ++i) {
+    d[i] = alpha[i + 1].re;
+    e[i] = (i + 1 < act) ? nrm[i + 1] : 0.0;
+    z[(size_t)i * act + i] = 1.0;
+  }
+  QD_REQUIRE(tridiag_ql<double>(act, d.data(), e.data(), z.data(), act) == 0, QD_ERR_INVALID,
+             "tridiagonal eigensolver did not converge");
+  // c_j = sum_l Q(j, l) exp(-i h lambda_l) Q(0, l); column l of Q is z[l * act ...]
+  std::vector<cplx> y(act);
+  for (int j = 0; j < act; ++j) {
+    double re = 0.0, im = 0.0;
+    for (int l = 0; l < act; ++l) {
+      const double w = z[(size_t)l * act + j] * z[(size_t)l * act + 0];
+      re += w * std::cos(h * d[l]);
+      im -= w * std::sin(h * d[l]);
+    }
+    y[j] = mkc(re * scl[j], im * scl[j]);
+  }
+  DBuf<cplx> dy(act);
+  QD_CUDA(cudaMemcpyAsync(dy.p, y.data(), act * sizeof(cplx), cudaMemcpyHostToDevice, ctx->stream));
+  combine_kernel<cplx><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, dy.p, act, psi_out);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (act_out) *act_out = act;
+}
+
+void lanczos_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int m, int* act_out) {
+  Ctx* ctx = H->ctx;
+  const int64_t n = H->dim;
+  QD_REQUIRE(m >= 2 && m <= 4097, QD_ERR_INVALID, "Krylov dimension must be in 2..4097");
+  QD_REQUIRE(H->flags & QD_HAM_HERMITIAN, QD_ERR_NOT_HERMITIAN,
+             "the short-recurrence Krylov exponential needs a Hermitian operator");
+  Workspace& W = ham_workspace(H);
+  DBuf<double> nrm2(1);
+  DBuf<int> has_im(1);
+  QD_CUDA(cudaMemsetAsync(has_im.p, 0, sizeof(int), ctx->stream));
+  colnorm_kernel<<<vec_grid(ctx, n), kVecThreads, 0, ctx->stream>>>(n, psi_in, nrm2.p, W.red_d(0), has_im.p);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  double hn = 0.0;
+  QD_CUDA(cudaMemcpyAsync(&hn, nrm2.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  QD_REQUIRE(hn > 0.0 && std::isfinite(hn), QD_ERR_INVALID, "input state has zero or non-finite norm");
+  if (H->flags & QD_HAM_REAL)
+    lanczos_evolve_impl<double>(H, psi_in, psi_out, nrm2.p, h, m, act_out);
+  else
+    lanczos_evolve_impl<cplx>(H, psi_in, psi_out, nrm2.p, h, m, act_out);
 }
 
 }  // namespace qd

@@ -27,6 +27,7 @@ struct LanczosBuffers {
   DBuf<double> nrm, nrm2, y, scl;  // scl[k] = 1 / ||V[k]|| (basis stored unnormalised)
   DBuf<int> stop;
   cudaGraphExec_t exec = nullptr;
+  int kind = 0;  // product the captured graph launches (0 CSR, 1 matrix-free)
   int64_t graph_kernels = 0;
 
   void ensure(int64_t n_, int kdim_) {
@@ -106,7 +107,13 @@ struct Workspace {
 Workspace& ham_workspace(qd_ham* H);
 void ham_apply_c(qd_ham* H, const cplx* x, cplx* y);
 cplx state_eval(qd_ham* H, const cplx* psi);
+double state_norm2(qd_ham* H, const cplx* psi);
 void lanczos_ground(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, double* evals_out, qd_lanczos_result* res);
 void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per_launch);
+void lanczos_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int m, int* act_out);
+void hermitian_lanczos_ground(qd_ham* H, cplx* psi, int kdim, double* evals_out, qd_lanczos_result* res);
+template <typename VV>
+void launch_mf(Ctx* ctx, qd_ham* H, const VV* x, VV* y, double scale, const double* scale_dev, const int* stop,
+               int step);
 
 }  // namespace qd

@@ -253,8 +253,10 @@ def getState(index: Sector, nt: int) -> State:
     return State(index, nt)
 
 
-def apply(ham: Hamiltonian, x: State, t_in: int, y: State, t_out: int) -> None:
-    A.call("qd_ham_apply", ham.handle, x.handle, t_in, y.handle, t_out)
+def apply(ham: Hamiltonian, x: State, t_in: int, y: State, t_out: int, matrix_free: bool = False) -> None:
+    """y(t_out) = H x(t_in) through the CSR form, or the matrix-free form."""
+    name = "qd_ham_apply_matrix_free" if matrix_free else "qd_ham_apply"
+    A.call(name, ham.handle, x.handle, t_in, y.handle, t_out)
 
 
 def start_vector(dim: int, seed: int) -> np.ndarray:
@@ -337,6 +339,32 @@ class ArnoldiSolver:
         return self._act
 
 
+class HermitianLanczosSolver:
+    """Hermitian::LanczosSolver(index, kry_dim): two-vector Lanczos ground state."""
+
+    def __init__(self, index: Sector, kry_dim: int):
+        self.index = index
+        self.kry_dim = kry_dim
+        self._evals = np.empty(0)
+        self.result = None
+
+    def getGroundState(self, H: Hamiltonian, psi: State, tstp: int):
+        evals = np.empty(self.kry_dim, dtype=np.float64)
+        res = A.qd_lanczos_result()
+        A.call("qd_hermitian_lanczos_ground", H.handle, psi.handle, tstp, self.kry_dim,
+               evals.ctypes.data_as(C.POINTER(C.c_double)), C.byref(res))
+        self._evals = evals[:res.act_dim].copy()
+        self.result = res
+        return res
+
+    def eigenvalues(self) -> np.ndarray:
+        return self._evals
+
+
+class Hermitian:
+    LanczosSolver = HermitianLanczosSolver
+
+
 class Arnoldi:
     @staticmethod
     def getLanczosSolver(index: Sector, kry_dim: int, **kw) -> LanczosSolver:
@@ -392,3 +420,136 @@ def traj_run(heff: Hamiltonian, psi0, ntraj: int, nsteps: int, dt: float, gamma:
     A.call("qd_traj_run", heff.handle, C.byref(d), psi0.ctypes.data_as(A._DP), mean.ctypes.data_as(A._DP),
            err.ctypes.data_as(A._DP), C.byref(st))
     return mean, err, st
+
+
+def lanczos_evolve(H: Hamiltonian, psi: State, t_in: int, t_out: int, h: float, m: int) -> int:
+    """psi(t_out) = exp(-i H h) psi(t_in) by the short-recurrence Krylov
+    exponential (Hermitian H); returns the Krylov dimension used."""
+    act = C.c_int(0)
+    A.call("qd_lanczos_evolve", H.handle, psi.handle, t_in, t_out, h, m, C.byref(act))
+    return act.value
+
+
+def seeded_start(seed: int, dim: int) -> np.ndarray:
+    """The start vector the request loop draws for `seed` (Philox4x32-10, host copy)."""
+    out = np.empty(dim)
+    A.call("qd_seeded_start", C.c_uint64(seed), dim, out.ctypes.data_as(A._DP))
+    return out
+
+
+class Server:
+    """The request loop (qd_server_*): submit ground-state and evolution
+    requests as operator descriptions, poll finished results.
+
+    mode "plain" runs every request with the FP64 reference algorithms;
+    "mixed" batches small real ground states (FP32 products, FP64 refinement)
+    and evolves Hermitian operators with the short-recurrence exponential.
+    """
+
+    def __init__(self, mode: str = "mixed", small_lanes: int = 4, large_lanes: int = 3, batch_lanes: int = 2,
+                 batch_max: int = 64, small_dim: int = 65536, hbm_budget: int = 0,
+                 ctx: Optional[Context] = None):
+        self.ctx = ctx or default_context()
+        o = A.qd_server_opts()
+        o.mode = A.QD_SERVE_MIXED if mode == "mixed" else A.QD_SERVE_PLAIN
+        o.small_lanes = small_lanes
+        o.large_lanes = large_lanes
+        o.batch_lanes = batch_lanes
+        o.batch_max = batch_max
+        o.small_dim = small_dim
+        o.hbm_budget = hbm_budget
+        self.handle = C.c_void_p()
+        A.call("qd_server_create", self.ctx.handle, C.byref(o), C.byref(self.handle))
+        self.mode = mode
+        self._keep = {}
+
+    def _submit(self, kind: int, spec: SectorSpec, opsum: OperatorSum, krylov_dim: int, nsteps: int,
+                dt: float, psi0, seed: int, want_state: bool, dim_hint: int, tag: int) -> int:
+        q = A.qd_request()
+        q.kind = kind
+        q.nbits = spec.nbits
+        cons, nc = spec.constraint_array()
+        q.ncons = nc
+        q.tight = spec.tight
+        q.cons = C.cast(cons, C.POINTER(A.qd_constraint))
+        terms, nt, gates, ng = opsum.pack()
+        q.terms = C.cast(terms, C.POINTER(A.qd_term))
+        q.gates = C.cast(gates, C.POINTER(A.qd_gate))
+        q.nterms = nt
+        q.ngates = ng
+        q.krylov_dim = krylov_dim
+        q.nsteps = nsteps
+        q.dt = dt
+        q.seed = seed
+        q.tag = tag
+        keep = [cons, terms, gates]
+        if psi0 is not None:
+            p0 = np.ascontiguousarray(np.asarray(psi0, dtype=np.complex128))
+            q.psi0 = p0.ctypes.data_as(A._DP)
+            q.psi0_len = len(p0)
+            keep.append(p0)
+        out = None
+        if want_state:
+            n = dim_hint if dim_hint else (len(psi0) if psi0 is not None else 0)
+            if n <= 0:
+                raise ValueError("want_state needs the sector dimension (dim_hint) or psi0")
+            out = np.zeros(n, dtype=np.complex128)
+            q.psi_out = out.ctypes.data_as(A._DP)
+            q.psi_out_len = n
+        rid = C.c_uint64()
+        A.call("qd_server_submit", self.handle, C.byref(q), C.byref(rid))
+        self._keep[rid.value] = out
+        return rid.value
+
+    def submit_ground(self, spec: SectorSpec, opsum: OperatorSum, krylov_dim: int = 100, psi0=None, seed: int = 0,
+                      want_state: bool = False, dim_hint: int = 0, tag: int = 0) -> int:
+        return self._submit(A.QD_REQ_GROUND, spec, opsum, krylov_dim, 0, 0.0, psi0, seed, want_state, dim_hint, tag)
+
+    def submit_evolve(self, spec: SectorSpec, opsum: OperatorSum, dt: float, nsteps: int, m: int = 16, psi0=None,
+                      seed: int = 0, want_state: bool = False, dim_hint: int = 0, tag: int = 0) -> int:
+        return self._submit(A.QD_REQ_EVOLVE, spec, opsum, m, nsteps, dt, psi0, seed, want_state, dim_hint, tag)
+
+    def poll(self, max_results: int = 256, timeout_ms: int = 0):
+        buf = (A.qd_result * max_results)()
+        n = C.c_int(0)
+        A.call("qd_server_poll", self.handle, buf, max_results, C.byref(n), timeout_ms)
+        out = []
+        for i in range(n.value):
+            r = buf[i]
+            d = {f: getattr(r, f) for f, _ in A.qd_result._fields_}
+            d["state"] = self._keep.pop(r.id, None)
+            out.append(d)
+        return out
+
+    def wait_all(self, ids, timeout_s: float = 600.0):
+        want = set(ids)
+        got = {}
+        import time as _t
+        t_end = _t.monotonic() + timeout_s
+        while want - set(got):
+            if _t.monotonic() > t_end:
+                raise TimeoutError(f"{len(want - set(got))} requests still pending")
+            for r in self.poll(256, 100):
+                got[r["id"]] = r
+        return got
+
+    def now(self) -> float:
+        t = C.c_double()
+        A.call("qd_server_now", self.handle, C.byref(t))
+        return t.value
+
+    def stats(self) -> dict:
+        st = A.qd_server_stats()
+        A.call("qd_server_get_stats", self.handle, C.byref(st))
+        return {f: getattr(st, f) for f, _ in A.qd_server_stats._fields_}
+
+    def close(self):
+        if getattr(self, "handle", None) and self.handle.value and not _SHUTDOWN[0]:
+            A.call("qd_server_destroy", self.handle)
+        self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -97,3 +97,36 @@ def test_library_exports_every_declared_symbol():
     missing = [n for n in _declared_functions() if not hasattr(lib, n)]
     assert not missing, missing
     assert lib.qd_api_version() == 1
+
+
+def _philox4x32_10(ctr, key):
+    """Philox4x32-10 (Salmon et al., SC11), restated for the check below."""
+    M0, M1, W0, W1 = 0xD2511F53, 0xCD9E8D57, 0x9E3779B9, 0xBB67AE85
+    c = list(ctr)
+    k0, k1 = key
+    for _ in range(10):
+        p0 = M0 * c[0]
+        p1 = M1 * c[2]
+        hi0, lo0 = p0 >> 32, p0 & 0xFFFFFFFF
+        hi1, lo1 = p1 >> 32, p1 & 0xFFFFFFFF
+        c = [hi1 ^ c[1] ^ k0, lo1, hi0 ^ c[3] ^ k1, lo0]
+        k0 = (k0 + W0) & 0xFFFFFFFF
+        k1 = (k1 + W1) & 0xFFFFFFFF
+    return c
+
+
+def test_seeded_start_follows_the_documented_generator():
+    # host-only entry point: needs the library, not a GPU
+    if not os.path.exists(A.LIB_PATH):
+        from qudrip_gb300 import build
+        build.build()
+    import qudrip_gb300 as q
+    seed = 0x1234_5678_9ABC
+    got = q.seeded_start(seed, 9)
+    for i in range(9):
+        c = _philox4x32_10([i // 2, 0x53544152, 0, 0], [seed & 0xFFFFFFFF, seed >> 32])
+        words = (c[0], c[1]) if i % 2 == 0 else (c[2], c[3])
+        u = ((words[0] >> 5) * 67108864.0 + (words[1] >> 6)) / 9007199254740992.0
+        assert got[i] == 2.0 * u - 1.0
+    assert np.all(np.abs(got) <= 1.0)
+    assert not np.array_equal(q.seeded_start(seed + 1, 9), got)
