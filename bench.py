@@ -522,7 +522,14 @@ def serving_mix(n_req=400, rate=200.0, seed=77):
             by_kind[kind] = {"n": len(idx), "p50_ms": 1e3 * float(np.percentile(lk, 50)),
                              "p99_ms": 1e3 * float(np.percentile(lk, 99))}
         results[mode] = out
-        summary[mode] = {"solves_per_s": n_req / (t_last - t_first), "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+        service = {}
+        for kind in ("ground", "evolve"):
+            for L in (12, 14, 16, 18, 20, 22):
+                idx = [i for i in range(n_req) if reqs[i]["kind"] == kind and reqs[i]["L"] == L]
+                if idx:
+                    sv = [out[i]["t_done"] - out[i]["t_admit"] for i in idx]
+                    service[f"{kind}_L{L}"] = round(1e3 * float(np.median(sv)), 2)
+        summary[mode] = {"service_p50_ms": service, "solves_per_s": n_req / (t_last - t_first), "p50_ms": 1e3 * float(np.percentile(lat, 50)),
                          "p99_ms": 1e3 * float(np.percentile(lat, 99)), "failed": bad, "by_kind": by_kind,
                          "batches": st["batches"], "batched": st["batched"], "max_active": st["max_active"],
                          "bytes_peak": st["bytes_peak"], "budget": st["budget"]}

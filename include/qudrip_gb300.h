@@ -317,18 +317,30 @@ qd_status qd_traj_run(qd_ham *heff, const qd_traj_desc *desc, const double *psi0
 /* Average device time of the sparse product kernel the solvers use on this
  * Hamiltonian (iters back-to-back launches on the context stream, timed with
  * CUDA events), and the kernel's algorithmic HBM bytes per launch:
- * CSR: nnz*(value + 4) + (dim+1)*8 + dim*(x + y) bytes.  Diagnostic codes:
+ * CSR: nnz*(value + 4) + (dim+1)*8 + dim*(x + y) bytes; 120: nnz_offdiag*4 +
+ * (dim+1)*4 + dim*(8 diagonal + 8 x + 16 fixed-point x + 8 y); 1 (matrix-free):
+ * dim*(8 basis + diagonal + x + y).  Code 0 times what the Lanczos path
+ * launches.  Diagnostic codes:
  * 2000 + kernel times the product with the fused Lanczos dot epilogue; 3001
  * and 3002 time the two Lanczos vector kernels alone (real Hamiltonians). */
 qd_status qd_ham_time_spmv(qd_ham *ham, int spmv, int iters, double *avg_ms,
                            double *bytes_per_launch);
 
-/* CSR product kernels: 100 warp tile (lane per row), 101 balanced warp tile
- * (equal nnz per lane), 102/103/104 two/four/eight lanes per row, 105 thread
- * per row.  All give the same products up to summation order. */
+/* Product kernels the Lanczos recurrence launches.  CSR: 100 warp tile (lane
+ * per row), 101 balanced warp tile (equal nnz per lane), 102/103/104 two/four/
+ * eight lanes per row, 105 thread per row, 106/107 thread per row with 4/8
+ * loads in flight (108/109 streaming loads), 110 thread per row with an
+ * exact-count tail (the default CSR kernel), 111 as 110 in length order.
+ * 120: the uniform-coupling form -- when every off-diagonal entry of a real
+ * operator has one value c, the diagonal and the columns are kept without
+ * values and each row's off-diagonal sum is accumulated exactly in 128-bit
+ * fixed point from a fixed-point copy of the vector, rounded once to FP64.
+ * It is the default wherever it applies (real start vector); choosing any
+ * other code turns it off.  All give the same products up to rounding. */
 qd_status qd_ham_set_spmv_kernel(qd_ham *ham, int kernel);
-/* Time every product kernel on this Hamiltonian and keep the fastest for the
- * solvers (the autotuner); returns the choice and its average ms. */
+/* Time every product kernel on this Hamiltonian (120 included where it
+ * applies) and keep the fastest for the solvers (the autotuner); returns the
+ * choice and its average ms. */
 qd_status qd_ham_autotune(qd_ham *ham, int iters, int *chosen, double *best_ms);
 
 /* <psi|H|psi> for a CSR Hamiltonian, with no device allocation at all.
@@ -354,8 +366,9 @@ qd_status qd_csr_expect_noalloc(const int64_t *d_rowptr, const int32_t *d_colidx
 /*   and getKrylovGS (:206-238)                                       */
 /* Two-vector recurrence (no stored basis), stop once ||r||^2 <= 1e-10; */
 /* the ground-state vector is rebuilt by a second pass and written to    */
-/* psi(:, t).  evals_out (may be NULL) receives res->act_dim eigenvalues  */
-/* of the tridiagonal matrix; one product per step and pass.            */
+/* psi(:, t).  Up to kry_dim + 1 Lanczos coefficients, as the reference's */
+/* loop; evals_out (NULL or kry_dim + 1 doubles) receives res->act_dim     */
+/* eigenvalues of the tridiagonal matrix; one product per step and pass. */
 /* ------------------------------------------------------------------ */
 qd_status qd_hermitian_lanczos_ground(qd_ham *ham, qd_state *psi, int t, int kry_dim,
                                       double *evals_out, qd_lanczos_result *res);
@@ -366,11 +379,14 @@ qd_status qd_hermitian_lanczos_ground(qd_ham *ham, qd_state *psi, int t, int kry
 /*   sparse_algorithm.hpp:548-562) up to rounding: for Hermitian H the */
 /*   Arnoldi projection is tridiagonal, so the three-term recurrence   */
 /*   builds the same Krylov space with two vector passes per product.  */
-/* m - 1 products, breakdown rule of expandBasis<0>; exp(-i h T) e_0 from  */
-/* the eigen-decomposition of T.  QD_ERR_NOT_HERMITIAN for other H.      */
+/* nsteps steps of length h from psi(:, t_in) into psi(:, t_out), each   */
+/* with m - 1 products and the breakdown rule of expandBasis<0>; the     */
+/* small exponential exp(-i h T) e_0 is evaluated on the device, so a     */
+/* step is one CUDA graph launch with no host round trip.  act_dim gets  */
+/* the last step's Krylov dimension.  QD_ERR_NOT_HERMITIAN for other H.  */
 /* ------------------------------------------------------------------ */
 qd_status qd_lanczos_evolve(qd_ham *ham, qd_state *psi, int t_in, int t_out,
-                            double h, int m, int *act_dim);
+                            double h, int m, int nsteps, int *act_dim);
 
 /* ------------------------------------------------------------------ */
 /* Seeded start vectors                                               */
@@ -396,7 +412,7 @@ qd_status qd_seeded_start(uint64_t seed, int64_t dim, double *host_out);
 /* with dimension m = krylov_dim.                                      */
 /* QD_SERVE_PLAIN runs every request with the FP64 reference            */
 /* algorithms (qd_lanczos_ground, qd_arnoldi_evolve).  QD_SERVE_MIXED   */
-/* batches ground states with dim <= small_dim and a real start vector  */
+/* batches ground states with dim <= batch_dim and a real start vector  */
 /* into one persistent launch per lane pass (qd_batch_lanczos: FP32     */
 /* products and basis, FP64 accumulation and refinement), and evolves   */
 /* Hermitian operators with qd_lanczos_evolve.                          */
@@ -416,7 +432,8 @@ typedef struct qd_server_opts {
   int32_t reserved0;
   int64_t small_dim;    /* default 65536 */
   int64_t hbm_budget;   /* bytes admitted requests may hold; 0 = 80% of free memory */
-  int32_t reserved[4];
+  int64_t batch_dim;    /* QD_SERVE_MIXED: ground states with dim <= batch_dim are batched (default 16384) */
+  int32_t reserved[2];
 } qd_server_opts;
 
 typedef struct qd_request {

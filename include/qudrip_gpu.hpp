@@ -462,10 +462,12 @@ namespace Arnoldi {
 class LanczosSolver {
  public:
   LanczosSolver(const SubIndex&, int kry_dim) : kry_dim_(kry_dim) {}
+  // products through the matrix-free form (qd_ham_build_matrix_free) instead of the CSR matrix
+  void setMatrixFree(bool on) { spmv_ = on ? QD_SPMV_MATRIX_FREE : QD_SPMV_CSR; }
   void getGroundState(const SpMatrix& H, State& psi, int tstp) {
     qd_lanczos_opts o{};
     o.krylov_dim = kry_dim_;
-    o.spmv = QD_SPMV_CSR;
+    o.spmv = spmv_;
     o.ritz = QD_RITZ_STORED_BASIS;
     evals_.assign((size_t)kry_dim_, 0.0);
     check(qd_lanczos_ground(H.handle(), psi.handle(), tstp, &o, evals_.data(), &res_), "getGroundState");
@@ -481,6 +483,7 @@ class LanczosSolver {
 
  private:
   int kry_dim_;
+  int spmv_ = QD_SPMV_CSR;
   qd_lanczos_result res_{};
   std::vector<double> evals_;
 };
@@ -505,4 +508,28 @@ inline LanczosSolver getLanczosSolver(const SubIndex& index, int kry_dim) { retu
 inline ArnoldiSolver getSolver(const SubIndex& index, int kry_dim) { return ArnoldiSolver(index, kry_dim); }
 
 }  // namespace Arnoldi
+
+// Hermitian::LanczosSolver (sparse_algorithm.hpp:287-301): two-vector Lanczos,
+// ground state rebuilt by a second pass.
+namespace Hermitian {
+
+class LanczosSolver {
+ public:
+  LanczosSolver(const SubIndex&, int kry_dim) : kry_dim_(kry_dim) {}
+  void getGroundState(const SpMatrix& H, State& psi, int tstp) {
+    evals_.assign((size_t)kry_dim_ + 1, 0.0);
+    check(qd_hermitian_lanczos_ground(H.handle(), psi.handle(), tstp, kry_dim_, evals_.data(), &res_),
+          "getGroundState");
+    evals_.resize((size_t)res_.act_dim);
+  }
+  double error() const { return res_.err; }
+  const std::vector<double>& eigenvalues() const { return evals_; }
+
+ private:
+  int kry_dim_;
+  qd_lanczos_result res_{};
+  std::vector<double> evals_;
+};
+
+}  // namespace Hermitian
 }  // namespace qudrip_gpu

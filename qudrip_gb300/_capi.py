@@ -100,7 +100,8 @@ QD_PATH_BATCH = 1
 class qd_server_opts(C.Structure):
     _fields_ = [("mode", C.c_int32), ("small_lanes", C.c_int32), ("large_lanes", C.c_int32),
                 ("batch_lanes", C.c_int32), ("batch_max", C.c_int32), ("reserved0", C.c_int32),
-                ("small_dim", C.c_int64), ("hbm_budget", C.c_int64), ("reserved", C.c_int32 * 4)]
+                ("small_dim", C.c_int64), ("hbm_budget", C.c_int64), ("batch_dim", C.c_int64),
+                ("reserved", C.c_int32 * 2)]
 
 
 class qd_request(C.Structure):
@@ -184,7 +185,7 @@ _SIGNATURES = {
     "qd_lanczos_ground": [_P, _P, C.c_int, C.POINTER(qd_lanczos_opts), _DP,
                           C.POINTER(qd_lanczos_result)],
     "qd_hermitian_lanczos_ground": [_P, _P, C.c_int, C.c_int, _DP, C.POINTER(qd_lanczos_result)],
-    "qd_lanczos_evolve": [_P, _P, C.c_int, C.c_int, C.c_double, C.c_int, C.POINTER(C.c_int)],
+    "qd_lanczos_evolve": [_P, _P, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_int)],
     "qd_seeded_start": [C.c_uint64, C.c_int64, _DP],
     "qd_server_create": [_P, C.POINTER(qd_server_opts), _PP],
     "qd_server_submit": [_P, C.POINTER(qd_request), C.POINTER(C.c_uint64)],

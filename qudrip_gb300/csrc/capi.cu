@@ -441,7 +441,8 @@ qd_status qd_lanczos_ground(qd_ham* ham, qd_state* psi, int t, const qd_lanczos_
 qd_status qd_ham_time_spmv(qd_ham* ham, int spmv, int iters, double* avg_ms, double* bytes_per_launch) {
   return guard([&] {
     QD_REQUIRE(ham && avg_ms && bytes_per_launch && iters >= 1, QD_ERR_INVALID, "bad argument");
-    const bool plain = spmv == QD_SPMV_CSR || spmv == QD_SPMV_MATRIX_FREE || (spmv >= kSpmvTile && spmv <= kSpmvLast);
+    const bool plain = spmv == QD_SPMV_CSR || spmv == QD_SPMV_MATRIX_FREE || spmv == kSpmvFx ||
+                       (spmv >= kSpmvTile && spmv <= kSpmvLast);
     const bool fused = spmv >= 2000 + kSpmvTile && spmv <= 2000 + kSpmvLast;
     const bool vec = spmv == 3001 || spmv == 3002;
     QD_REQUIRE(plain || fused || vec, QD_ERR_UNSUPPORTED, "qd_ham_time_spmv: unknown kernel code %d", spmv);
@@ -473,14 +474,16 @@ qd_status qd_hermitian_lanczos_ground(qd_ham* ham, qd_state* psi, int t, int kry
   });
 }
 
-qd_status qd_lanczos_evolve(qd_ham* ham, qd_state* psi, int t_in, int t_out, double h, int m, int* act_dim) {
+qd_status qd_lanczos_evolve(qd_ham* ham, qd_state* psi, int t_in, int t_out, double h, int m, int nsteps,
+                            int* act_dim) {
   return guard([&] {
     QD_REQUIRE(ham && psi, QD_ERR_INVALID, "null argument");
     QD_REQUIRE(psi->dim == ham->dim, QD_ERR_INVALID, "dimension mismatch");
     QD_REQUIRE(t_in >= 0 && t_in < psi->nt && t_out >= 0 && t_out < psi->nt, QD_ERR_INVALID, "bad column");
     QD_REQUIRE(m >= 2 && m <= 33, QD_ERR_UNSUPPORTED, "Krylov dimension m must be in 2..33");
     DeviceGuard dg(ham->ctx->device);
-    lanczos_evolve(ham, psi->col(t_in), psi->col(t_out), h, m, act_dim);
+    QD_REQUIRE(nsteps >= 1, QD_ERR_INVALID, "nsteps must be positive");
+    lanczos_evolve(ham, psi->col(t_in), psi->col(t_out), h, m, nsteps, act_dim, nullptr);
   });
 }
 
@@ -526,10 +529,17 @@ qd_status qd_traj_run(qd_ham* heff, const qd_traj_desc* desc, const double* psi0
 
 qd_status qd_ham_set_spmv_kernel(qd_ham* ham, int kernel) {
   return guard([&] {
-    QD_REQUIRE(ham && kernel >= kSpmvTile && kernel <= kSpmvLast, QD_ERR_INVALID, "unknown product kernel");
+    QD_REQUIRE(ham && ((kernel >= kSpmvTile && kernel <= kSpmvLast) || kernel == kSpmvFx), QD_ERR_INVALID,
+               "unknown product kernel");
     DeviceGuard dg(ham->ctx->device);
+    if (kernel == kSpmvFx) {
+      QD_REQUIRE(ham_build_fx(ham), QD_ERR_UNSUPPORTED, "the fixed-point form does not apply to this operator");
+      ham->fx_allowed = true;
+      return;
+    }
     if (kernel == kSpmvRowSorted) ham_ensure_row_order(ham);
     ham->spmv_variant = kernel;
+    ham->fx_allowed = false;
   });
 }
 
@@ -549,6 +559,16 @@ qd_status qd_ham_autotune(qd_ham* ham, int iters, int* chosen, double* best_ms) 
       }
     }
     ham->spmv_variant = pick;
+    ham->fx_allowed = false;
+    if ((ham->flags & QD_HAM_REAL) && ham_build_fx(ham)) {
+      double ms = 0;
+      time_spmv(ham, kSpmvFx, iters, &ms, &bytes);
+      if (ms < best) {
+        best = ms;
+        pick = kSpmvFx;
+        ham->fx_allowed = true;
+      }
+    }
     if (chosen) *chosen = pick;
     if (best_ms) *best_ms = best;
   });

@@ -1,0 +1,176 @@
+// fxsum.cu -- building the uniform-coupling form and its product (fxsum.cuh).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "fxsum.cuh"
+#include "ham.cuh"
+#include "scan.cuh"
+
+namespace qd {
+
+constexpr unsigned long long kNoValue = ~0ull;
+
+// The first nonzero off-diagonal value any row meets (its bits).
+__global__ void fx_probe_kernel(int64_t n, const int64_t* rowptr, const int32_t* colidx, const double* vals,
+                                unsigned long long* cand) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+      const double v = vals[k];
+      if (colidx[k] != (int32_t)r && v != 0.0) {
+        atomicCAS(cand, kNoValue, (unsigned long long)__double_as_longlong(v));
+        break;
+      }
+    }
+  }
+}
+
+// Per row: off-diagonal count, diagonal value, |row| sum; flags any
+// off-diagonal value other than c.
+__global__ void fx_count_kernel(int64_t n, const int64_t* rowptr, const int32_t* colidx, const double* vals, double c,
+                                int64_t* counts, double* diag, int* mismatch, unsigned long long* rowmax) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    int64_t cnt = 0;
+    double d = 0.0, abs_sum = 0.0;
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+      const double v = vals[k];
+      if (colidx[k] == (int32_t)r) {
+        d = v;
+      } else if (v != 0.0) {
+        if (v != c) *mismatch = 1;
+        ++cnt;
+        abs_sum += fabs(v);
+      }
+    }
+    abs_sum += fabs(d);
+    counts[r] = cnt;
+    diag[r] = d;
+    atomicMax(rowmax, (unsigned long long)__double_as_longlong(abs_sum));
+  }
+}
+
+__global__ void fx_fill_kernel(int64_t n, const int64_t* rowptr, const int32_t* colidx, const double* vals,
+                               const int64_t* off, int32_t* rowptr32, int32_t* colidx_fx) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r <= n; r += (int64_t)gridDim.x * blockDim.x) {
+    rowptr32[r] = (int32_t)off[r];
+    if (r == n) break;
+    int64_t o = off[r];
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k)
+      if (colidx[k] != (int32_t)r && vals[k] != 0.0) colidx_fx[o++] = colidx[k];
+  }
+}
+
+static int fx_grid(Ctx* ctx, int64_t n) {
+  return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)ctx->num_sms * 8));
+}
+
+bool ham_build_fx(qd_ham* H) {
+  if (H->fx_state != 0) return H->fx_state > 0;
+  H->fx_state = -1;
+  if (!(H->flags & QD_HAM_REAL) || H->dim < 1 || H->dim >= (1ll << 31)) return false;
+  Ctx* ctx = H->ctx;
+  const int64_t n = H->dim;
+  DBuf<unsigned long long> cand(2);
+  DBuf<int> mismatch(1);
+  QD_CUDA(cudaMemsetAsync(cand.p, 0xff, sizeof(unsigned long long), ctx->stream));
+  QD_CUDA(cudaMemsetAsync(cand.p + 1, 0, sizeof(unsigned long long), ctx->stream));
+  QD_CUDA(cudaMemsetAsync(mismatch.p, 0, sizeof(int), ctx->stream));
+  fx_probe_kernel<<<fx_grid(ctx, n), 256, 0, ctx->stream>>>(n, H->rowptr.p, H->colidx.p, H->vals_r.p, cand.p);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  unsigned long long cbits = kNoValue;
+  QD_CUDA(cudaMemcpyAsync(&cbits, cand.p, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  double c = 0.0;
+  if (cbits != kNoValue) std::memcpy(&c, &cbits, 8);
+  std::unique_ptr<FxForm> fx(new FxForm());
+  DBuf<int64_t> counts(n + 1), off(n + 1);
+  fx->diag.alloc(n);
+  fx_count_kernel<<<fx_grid(ctx, n), 256, 0, ctx->stream>>>(n, H->rowptr.p, H->colidx.p, H->vals_r.p, c, counts.p,
+                                                            fx->diag.p, mismatch.p, cand.p + 1);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  QD_CUDA(cudaMemsetAsync(counts.p + n, 0, sizeof(int64_t), ctx->stream));
+  exclusive_scan_i64(ctx, counts.p, off.p, n + 1);
+  int mm = 0;
+  unsigned long long rbits = 0;
+  int64_t total = 0;
+  QD_CUDA(cudaMemcpyAsync(&mm, mismatch.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(&rbits, cand.p + 1, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(&total, off.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (mm || total >= (1ll << 31) || H->max_row_nnz > 128) return false;
+  double rowmax = 0.0;
+  std::memcpy(&rowmax, &rbits, 8);
+  if (!std::isfinite(rowmax)) return false;
+  const double bound = std::max(1.0, rowmax);
+  const int eb = (int)std::ceil(std::log2(bound)) + 1;  // one bit of margin
+  fx->F = 119 - eb;
+  fx->c = c;
+  fx->nnz = total;
+  fx->rowptr.alloc(n + 1);
+  fx->colidx.alloc(std::max<int64_t>(total, 1) + 16);
+  QD_CUDA(cudaMemsetAsync(fx->colidx.p, 0, fx->colidx.bytes(), ctx->stream));
+  fx_fill_kernel<<<fx_grid(ctx, n + 1), 256, 0, ctx->stream>>>(n, H->rowptr.p, H->colidx.p, H->vals_r.p, off.p,
+                                                               fx->rowptr.p, fx->colidx.p);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  H->fx = std::move(fx);
+  H->fx_state = 1;
+  return true;
+}
+
+// ---------------------------------------------------------------- product
+// w_r = s * (d_r x_r + c 2^-F sum_k X_k): thread per row, columns and the
+// 16-byte fixed-point gathers four at a time, one FP64 rounding of the sum.
+__global__ void __launch_bounds__(256) spmv_fx_kernel(int64_t n, const int32_t* __restrict__ rowptr,
+                                                      const int32_t* __restrict__ colidx,
+                                                      const double* __restrict__ diag,
+                                                      const double* __restrict__ x, const __int128* __restrict__ X,
+                                                      double* __restrict__ y, double cF, const double* scale_dev,
+                                                      const int* stop, int step) {
+  if (stop) {
+    const int st = *stop;
+    if (st != 0 && st < step) return;
+  }
+  const double sc = scale_dev ? *scale_dev : 1.0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    const int b = __ldg(rowptr + r), e = __ldg(rowptr + r + 1);
+    __int128 acc = 0;
+    int k = b;
+    for (; k + 4 <= e; k += 4) {
+      const int c0 = __ldcs(colidx + k), c1 = __ldcs(colidx + k + 1), c2 = __ldcs(colidx + k + 2),
+                c3 = __ldcs(colidx + k + 3);
+      const __int128 x0 = X[c0], x1 = X[c1], x2 = X[c2], x3 = X[c3];
+      acc += (x0 + x1) + (x2 + x3);
+    }
+    for (; k < e; ++k) acc += X[__ldcs(colidx + k)];
+    y[r] = sc * fma(cF, (double)acc, __ldg(diag + r) * __ldg(x + r));
+  }
+}
+
+// X = fixed-point copy of x (v_0 of a Lanczos run).
+__global__ void fx_shadow_kernel(int64_t n, const double* x, __int128* X, int F, int* ovf) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    X[i] = fx_from_double(x[i], F, ovf);
+}
+
+void launch_fx(Ctx* ctx, const qd_ham* H, const double* x, const __int128* X, double* y, const double* scale_dev,
+               const int* stop, int step) {
+  const FxForm& f = *H->fx;
+  const double cF = std::ldexp(f.c, -f.F);
+  spmv_fx_kernel<<<(unsigned)std::max<int64_t>(1, ceil_div(H->dim, 256)), 256, 0, ctx->stream>>>(
+      H->dim, f.rowptr.p, f.colidx.p, f.diag.p, x, X, y, cF, scale_dev, stop, step);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+}
+
+void launch_fx_shadow(Ctx* ctx, int64_t n, const double* x, __int128* X, int F, int* ovf) {
+  fx_shadow_kernel<<<fx_grid(ctx, n), 256, 0, ctx->stream>>>(n, x, X, F, ovf);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+}
+
+}  // namespace qd

@@ -12,6 +12,7 @@
 #include <memory>
 
 #include "common.cuh"
+#include "fxsum.cuh"
 #include "sector.cuh"
 
 namespace qd {
@@ -83,6 +84,10 @@ struct qd_ham {
   qd::DBuf<double> vals_r;
   qd::DBuf<float> vals_f;  // fp32 copy of vals_r for the mixed-precision SpMV
   qd::DBuf<int32_t> row_order;  // rows by decreasing length inside 256-row windows (kernel 111)
+  // uniform-coupling form with exact fixed-point sums (fxsum.cuh)
+  int fx_state = 0;          // 0 not tried, 1 built, -1 not applicable
+  bool fx_allowed = true;    // the Lanczos product uses it when built (kernel code 120)
+  std::unique_ptr<qd::FxForm> fx;
   // matrix-free form (qd_ham_build_matrix_free)
   bool has_mf = false;
   bool mf_real = false;      // every amplitude and diagonal entry is real
@@ -105,5 +110,9 @@ void ham_transpose(Ctx* ctx, int64_t n, const int64_t* ptr, const int32_t* idx, 
                    int64_t nnz, int64_t* out_ptr, int32_t* out_idx, cplx* out_vals);
 void ham_build_matrix_free(qd_ham* H);
 void mf_apply_c(qd_ham* H, const cplx* x, cplx* y);
+bool ham_build_fx(qd_ham* H);
+void launch_fx(Ctx* ctx, const qd_ham* H, const double* x, const __int128* X, double* y, const double* scale_dev,
+               const int* stop, int step);
+void launch_fx_shadow(Ctx* ctx, int64_t n, const double* x, __int128* X, int F, int* ovf);
 void ham_ensure_row_order(qd_ham* H);
 }  // namespace qd

@@ -69,6 +69,10 @@ struct LzPack<double> {
   __device__ static double dot(T a, T b, double acc) { return fma(a.y, b.y, fma(a.x, b.x, acc)); }
   __device__ static double nrm(T a, double acc) { return fma(a.y, a.y, fma(a.x, a.x, acc)); }
   __device__ static T submul(T x, double a, T y) { return make_double2(fma(-a, y.x, x.x), fma(-a, y.y, x.y)); }
+  __device__ static void shadow(__int128* X, int64_t p, T v, int F, int* ovf) {
+    X[2 * p] = fx_from_double(v.x, F, ovf);
+    X[2 * p + 1] = fx_from_double(v.y, F, ovf);
+  }
 };
 template <>
 struct LzPack<cplx> {
@@ -83,7 +87,13 @@ struct LzPack<cplx> {
   __device__ static cplx dot(T a, T b, cplx acc) { return vdotfma(a, b, acc); }
   __device__ static double nrm(T a, double acc) { return acc + vnorm2(a); }
   __device__ static T submul(T x, cplx a, T y) { return vsubmul(x, a, y); }
+  __device__ static void shadow(__int128*, int64_t, T, int, int*) {}
 };
+
+__device__ __forceinline__ void shadow_one(__int128* X, int64_t i, double v, int F, int* ovf) {
+  X[i] = fx_from_double(v, F, ovf);
+}
+__device__ __forceinline__ void shadow_one(__int128*, int64_t, cplx, int, int*) {}
 
 // K2: the three inner products of step k from one read of w, V1, V2:
 //   d1 = <V2, w>,  d2 = <V1, w>,  d3 = <V1, V2>
@@ -146,7 +156,7 @@ __global__ void __launch_bounds__(kLzThreads, kLzBlocksPerSm)
     lz_update_kernel(int64_t n, int* stop, int step, const VV* __restrict__ w, const VV* __restrict__ V1,
                      const VV* __restrict__ V2, const double* s1, const double* s2, const VV* alpha,
                      const VV* beta, VV* __restrict__ Vk, double* nrm2, double* nrm, double* sk,
-                     GridRed<double> red) {
+                     GridRed<double> red, __int128* Xk, int F, int* ovf) {
   if (stopped(stop, step)) return;
   using P = LzPack<VV>;
   const VV a = vscale(*s1, *alpha);
@@ -167,6 +177,10 @@ __global__ void __launch_bounds__(kLzThreads, kLzBlocksPerSm)
     o1 = P::submul(o1, a, a1);
     P::store(Vk, p, o0);
     P::store(Vk, p + stride, o1);
+    if (Xk) {
+      P::shadow(Xk, p, o0, F, ovf);
+      P::shadow(Xk, p + stride, o1, F, ovf);
+    }
     acc0 = P::nrm(o0, acc0);
     acc1 = P::nrm(o1, acc1);
   }
@@ -175,6 +189,7 @@ __global__ void __launch_bounds__(kLzThreads, kLzBlocksPerSm)
     if (kHas2) o0 = P::submul(o0, b, P::load_last(V2, p));
     o0 = P::submul(o0, a, P::load(V1, p));
     P::store(Vk, p, o0);
+    if (Xk) P::shadow(Xk, p, o0, F, ovf);
     acc0 = P::nrm(o0, acc0);
   }
   if (P::kPer == 2 && (n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -182,6 +197,7 @@ __global__ void __launch_bounds__(kLzThreads, kLzBlocksPerSm)
     if (kHas2) o = vsubmul(o, b, V2[n - 1]);
     o = vsubmul(o, a, V1[n - 1]);
     Vk[n - 1] = o;
+    if (Xk) shadow_one(Xk, n - 1, o, F, ovf);
     acc0 += vnorm2(o);
   }
   if (grid_sum(acc0 + acc1, red, nrm2) && threadIdx.x == 0) {
@@ -196,7 +212,8 @@ __global__ void __launch_bounds__(kLzThreads, kLzBlocksPerSm)
 template <typename VV>
 static void lz_vector_passes(Ctx* ctx, int64_t n, int* stop, int step, const VV* w, const VV* V1, const VV* V2,
                              const double* s1, const double* s2, VV* beta, VV* alpha, Tri<VV>* dots, VV* Vk,
-                             double* nrm2, double* nrm, double* sk, GridRed<Tri<VV>> rt, GridRed<double> rd) {
+                             double* nrm2, double* nrm, double* sk, GridRed<Tri<VV>> rt, GridRed<double> rd,
+                             __int128* Xk = nullptr, int F = 0, int* ovf = nullptr) {
   const int g = lz_grid(ctx, n / LzPack<VV>::kPer + 1);
   if (V2) {
     lz_dots_kernel<VV, true><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V2, s1, s2, beta, alpha, dots,
@@ -204,14 +221,14 @@ static void lz_vector_passes(Ctx* ctx, int64_t n, int* stop, int step, const VV*
     QD_CHECK_LAUNCH();
     QD_LAUNCHED(ctx);
     lz_update_kernel<VV, true><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V2, s1, s2, alpha, beta, Vk,
-                                                                  nrm2, nrm, sk, rd);
+                                                                  nrm2, nrm, sk, rd, Xk, F, ovf);
   } else {
     lz_dots_kernel<VV, false><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V1, s1, s1, beta, alpha,
                                                                  dots, rt);
     QD_CHECK_LAUNCH();
     QD_LAUNCHED(ctx);
     lz_update_kernel<VV, false><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V1, s1, s1, alpha, beta,
-                                                                   Vk, nrm2, nrm, sk, rd);
+                                                                   Vk, nrm2, nrm, sk, rd, Xk, F, ovf);
   }
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
@@ -256,17 +273,6 @@ __global__ void __launch_bounds__(kVecThreads) ritz_kernel(int64_t n, const VV* 
     VV acc = vscale(y[0], V[i]);
     for (int k = 1; k < act; ++k) acc = vfma(y[k], V[(int64_t)k * ld + i], acc);
     psi[i] = to_c(acc);
-  }
-}
-
-// psi = sum_k y_k V[k] with complex coefficients (the Krylov exponential).
-template <typename VV>
-__global__ void __launch_bounds__(kVecThreads) combine_kernel(int64_t n, const VV* V, int64_t ld, const cplx* y,
-                                                              int act, cplx* psi) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    cplx acc = vfma(y[0], V[i], mkc(0.0, 0.0));
-    for (int k = 1; k < act; ++k) acc = vfma(y[k], V[(int64_t)k * ld + i], acc);
-    psi[i] = acc;
   }
 }
 
@@ -367,7 +373,16 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   const double* s1 = (const double*)scal.p;
   const bool mf = (spmv == QD_SPMV_MATRIX_FREE);
   if (mf) ham_build_matrix_free(H);
+  // code 0: the product the real Lanczos path launches (the fixed-point form when it applies)
+  const bool fx = real && (spmv == kSpmvFx || (spmv == QD_SPMV_CSR && H->fx_allowed)) && ham_build_fx(H);
+  QD_REQUIRE(spmv != kSpmvFx || fx, QD_ERR_UNSUPPORTED, "the fixed-point form does not apply to this operator");
+  DBuf<__int128> X(fx ? n + 32 : 1);
+  if (fx) QD_CUDA(cudaMemsetAsync(X.p, 0, X.bytes(), ctx->stream));
   auto launch = [&]() {
+    if (fx) {
+      launch_fx(ctx, H, (const double*)x.p, X.p, (double*)y.p, nullptr, nullptr, 0);
+      return;
+    }
     if (mf) {
       if (H->mf_real && real)
         launch_mf<double>(ctx, H, (const double*)x.p, (double*)y.p, 1.0, nullptr, nullptr, 0);
@@ -386,7 +401,7 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
       else
         lz_update_kernel<double, true><<<g, kLzThreads, 0, ctx->stream>>>(
             n, nullptr, 0, (const double*)y.p, (const double*)x.p, (const double*)z.p, s1, s1, d + 1, d + 2,
-            (double*)t.p, d + 3, d + 4, d + 5, W.red_d(3));
+            (double*)t.p, d + 3, d + 4, d + 5, W.red_d(3), nullptr, 0, nullptr);
       QD_CHECK_LAUNCH();
       QD_LAUNCHED(ctx);
       return;
@@ -413,11 +428,14 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   *bytes_per_launch = (double)H->nnz * (mvb + 4.0) + (double)(n + 1) * 8.0 + (double)n * 2.0 * (double)vb;
   if (mf)  // basis word, diagonal, x[r], y[r] per row (the gathered x comes from L2)
     *bytes_per_launch = (double)n * (8.0 + (H->mf_real ? 8.0 : 16.0) + 2.0 * (double)vb);
+  if (fx)  // columns, row pointers (int32), diagonal, x, its fixed-point copy, y
+    *bytes_per_launch = (double)H->fx->nnz * 4.0 + (double)(n + 1) * 4.0 + (double)n * (8.0 + 8.0 + 16.0 + 8.0);
 }
 
 // ---------------------------------------------------------------- Lanczos
 template <typename MV, typename VV>
-static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int kdim, Workspace& W, bool mf) {
+static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int kdim, Workspace& W, bool mf,
+                        bool fx = false) {
   Ctx* ctx = H->ctx;
   const int64_t n = H->dim;
   for (int k = 1; k <= kdim; ++k) {
@@ -426,15 +444,21 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int kd
     VV* Vk = B.V.p + (int64_t)k * B.ld;
     const double* s1 = B.scl.p + (k - 1);
     const double* s2 = (k >= 2) ? B.scl.p + (k - 2) : nullptr;
-    // K1: w = s1 * H V1 (CSR, or matrix-free)
+    // K1: w = s1 * H V1 (CSR, fixed-point uniform-coupling form, or matrix-free)
+    __int128* Xprev = fx ? B.X.p + (int64_t)((k - 1) & 1) * B.ld : nullptr;
+    __int128* Xnext = fx ? B.X.p + (int64_t)(k & 1) * B.ld : nullptr;
+    if constexpr (std::is_same<VV, double>::value) {
+      if (fx) launch_fx(ctx, H, V1, Xprev, B.w.p, s1, B.stop.p, k);
+    }
     if (mf)
       launch_mf<VV>(ctx, H, V1, B.w.p, 1.0, s1, B.stop.p, k);
-    else
+    else if (!fx)
       launch_spmv<MV, VV>(ctx, H, vals, V1, B.w.p, 1.0, nullptr, W.red_c_or_d<VV>(1), nullptr, B.stop.p, k, -1, s1,
                           nullptr);
-    // K2, K3
+    // K2, K3 (K3 also writes the fixed-point copy of v_k for the next product)
     lz_vector_passes<VV>(ctx, n, B.stop.p, k, B.w.p, V1, V2, s1, s2, B.beta.p + k, B.alpha.p + k, B.dots.p + k, Vk,
-                         B.nrm2.p + k, B.nrm.p + k, B.scl.p + k, W.red_tri<VV>(2), W.red_d(3));
+                         B.nrm2.p + k, B.nrm.p + k, B.scl.p + k, W.red_tri<VV>(2), W.red_d(3), Xnext,
+                         fx ? H->fx->F : 0, fx ? B.ovf.p : nullptr);
   }
 }
 
@@ -475,11 +499,30 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
   const auto host_t0 = std::chrono::steady_clock::now();
   if (timing) QD_CUDA(cudaEventRecord(ctx->events[12], ctx->stream));
   const bool mf = (o.spmv == QD_SPMV_MATRIX_FREE);
-  if (B.kind != (int)mf) {
+  bool fx = false;
+  if constexpr (std::is_same<VV, double>::value) fx = !mf && H->fx_allowed && ham_build_fx(H);
+  const int kind = mf ? 1 : (fx ? 2 : 0);
+  if (B.kind != kind) {
     B.drop_graph();
-    B.kind = (int)mf;
+    B.kind = kind;
   }
-  B.run_graph(ctx, [&]() { lanczos_run<MV, VV>(H, vals, B, kdim, W, mf); });
+  if (fx) {
+    B.ensure_fx();
+    QD_CUDA(cudaMemsetAsync(B.ovf.p, 0, sizeof(int), ctx->stream));
+    if constexpr (std::is_same<VV, double>::value) launch_fx_shadow(ctx, n, B.V.p, B.X.p, H->fx->F, B.ovf.p);
+  }
+  B.run_graph(ctx, [&]() { lanczos_run<MV, VV>(H, vals, B, kdim, W, mf, fx); });
+  if (fx) {
+    int ov = 0;
+    QD_CUDA(cudaMemcpyAsync(&ov, B.ovf.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    QD_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (ov) {  // a vector left the fixed-point range: redo the solve on the FP64 CSR product
+      H->fx_allowed = false;
+      lanczos_ground_impl<MV, VV>(H, psi, psi_nrm2, o, evals_out, res);
+      H->fx_allowed = true;
+      return;
+    }
+  }
   if (timing) QD_CUDA(cudaEventRecord(ctx->events[13], ctx->stream));
   int matvecs = kdim;
 
@@ -509,7 +552,11 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
     QD_CHECK_LAUNCH();
     QD_LAUNCHED(ctx);
     QD_CUDA(cudaMemsetAsync(B.stop.p, 0, sizeof(int), ctx->stream));
-    lanczos_run<MV, VV>(H, vals, B, act, W, mf);
+    if (fx) {
+      QD_CUDA(cudaMemsetAsync(B.ovf.p, 0, sizeof(int), ctx->stream));
+      if constexpr (std::is_same<VV, double>::value) launch_fx_shadow(ctx, n, B.V.p, B.X.p, H->fx->F, B.ovf.p);
+    }
+    lanczos_run<MV, VV>(H, vals, B, act, W, mf, fx);
     matvecs += act;
   }
   // psi = sum_k y_k v_k = sum_k (y_k s_k) V[k]
@@ -635,8 +682,8 @@ static void herm_lanczos_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, int 
   if constexpr (std::is_same<MV, double>::value) vals = H->vals_r.p;
   else vals = H->vals_c.p;
   const int vg = vec_grid(ctx, n);
-  DBuf<VV> v(n), w(n), h(n), a(kdim + 1);
-  DBuf<double> nn(kdim + 1);
+  DBuf<VV> v(n), w(n), h(n), a(kdim + 2);
+  DBuf<double> nn(kdim + 2);
   DBuf<int> stop(1);
   DBuf<cplx> start(n);
   QD_CUDA(cudaMemcpyAsync(start.p, psi, n * sizeof(cplx), cudaMemcpyDeviceToDevice, ctx->stream));
@@ -647,7 +694,7 @@ static void herm_lanczos_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, int 
     init_v0_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, start.p, psi_nrm2, v.p);
     QD_CHECK_LAUNCH();
     QD_LAUNCHED(ctx);
-    const int steps = z ? K : kdim;
+    const int steps = z ? K : kdim + 1;  // a_0 and kdim more (the reference's idx runs 1..kdim)
     for (int i = 0; i < steps; ++i) {
       VV* x = (i % 2 == 0) ? v.p : w.p;
       VV* pp = (i % 2 == 0) ? w.p : v.p;
@@ -669,14 +716,14 @@ static void herm_lanczos_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, int 
     }
   };
   pass(nullptr, 0);
-  std::vector<VV> ha(kdim + 1);
-  std::vector<double> hnn(kdim + 1);
+  std::vector<VV> ha(kdim + 2);
+  std::vector<double> hnn(kdim + 2);
   int st = 0;
-  QD_CUDA(cudaMemcpyAsync(ha.data(), a.p, (kdim + 1) * sizeof(VV), cudaMemcpyDeviceToHost, ctx->stream));
-  QD_CUDA(cudaMemcpyAsync(hnn.data(), nn.p, (kdim + 1) * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(ha.data(), a.p, (kdim + 2) * sizeof(VV), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(hnn.data(), nn.p, (kdim + 2) * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   QD_CUDA(cudaMemcpyAsync(&st, stop.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
-  const int K = st ? st : kdim;
+  const int K = st ? st : kdim + 1;
   std::vector<double> d(K), e(K), ev(K), z(K);
   for (int i = 0; i < K; ++i) {
     d[i] = real_part(ha[i]);
@@ -732,9 +779,90 @@ void hermitian_lanczos_ground(qd_ham* H, cplx* psi, int kdim, double* evals_out,
 // keeps s basis vectors (the expandBasis<0> count, sparse_algorithm.hpp:
 // 387-390).  exp(-i h T) e_0 = Q exp(-i h Lambda) Q^T e_0 from the QL
 // eigen-decomposition of T.  The output has the input norm dropped.
+// exp(-i h T) e_0 for T = tridiag(Re alpha_1.., n_1..) of dimension act on
+// one warp (lane j holds component j): Taylor series with scaling (N. J.
+// Higham and A. H. Al-Mohy, SIAM J. Sci. Comput. 33 (2011) 488-511), each
+// term a tridiagonal product through shuffles, cut once a term falls below
+// 1e-17 of the sum.  Writes y_j = c_j s_j (the stored basis is unnormalised)
+// and act; adds act to *matvecs.
+__global__ void __launch_bounds__(32) texp_kernel(int kdim, double h, const cplx* alpha, const double* nrm,
+                                                  const double* scl, const int* stop, cplx* y, int* act_out,
+                                                  long long* matvecs) {
+  const int lane = threadIdx.x;
+  const int st = *stop;
+  const int act = st ? st : kdim;
+  const bool on = lane < act;
+  const double d = on ? alpha[lane + 1].re : 0.0;
+  const double e = (lane + 1 < act) ? nrm[lane + 1] : 0.0;  // T(lane, lane+1)
+  double em = __shfl_up_sync(0xffffffffu, e, 1);           // T(lane, lane-1)
+  if (lane == 0) em = 0.0;
+  double rowsum = fabs(d) + e + em;
+  for (int o = 16; o > 0; o >>= 1) rowsum = fmax(rowsum, __shfl_xor_sync(0xffffffffu, rowsum, o));
+  const int steps = max(1, (int)ceil(rowsum * fabs(h) / 0.5));
+  const double hs = h / steps;
+  double yr = (lane == 0) ? 1.0 : 0.0, yi = 0.0;
+  for (int sstep = 0; sstep < steps; ++sstep) {
+    double tr = yr, ti = yi;
+    for (int p = 1; p <= 60; ++p) {
+      const double tr_dn = __shfl_down_sync(0xffffffffu, tr, 1), ti_dn = __shfl_down_sync(0xffffffffu, ti, 1);
+      const double tr_up = __shfl_up_sync(0xffffffffu, tr, 1), ti_up = __shfl_up_sync(0xffffffffu, ti, 1);
+      double kr = d * tr + e * tr_dn + (lane ? em * tr_up : 0.0);
+      double ki = d * ti + e * ti_dn + (lane ? em * ti_up : 0.0);
+      if (!on) kr = ki = 0.0;
+      const double f = hs / p;  // t <- (-i f) K t
+      tr = f * ki;
+      ti = -f * kr;
+      yr += tr;
+      yi += ti;
+      double tn = tr * tr + ti * ti, yn = yr * yr + yi * yi;
+      for (int o = 16; o > 0; o >>= 1) {
+        tn += __shfl_xor_sync(0xffffffffu, tn, o);
+        yn += __shfl_xor_sync(0xffffffffu, yn, o);
+      }
+      if (tn <= 1e-34 * yn) break;
+    }
+  }
+  if (on) y[lane] = mkc(yr * scl[lane], yi * scl[lane]);
+  if (lane == 0) {
+    *act_out = act;
+    if (matvecs) *matvecs += act;
+  }
+}
+
+// psi = sum_{k < *act} y_k V[k]
+__global__ void __launch_bounds__(kVecThreads) combine_dev_kernel(int64_t n, const cplx* V, int64_t ld, const cplx* y,
+                                                                  const int* act_dev, cplx* psi) {
+  const int act = *act_dev;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    cplx acc = vfma(y[0], V[i], mkc(0.0, 0.0));
+    for (int k = 1; k < act; ++k) acc = vfma(y[k], V[(int64_t)k * ld + i], acc);
+    psi[i] = acc;
+  }
+}
+
+// One Krylov step psi <- V exp(-i h T) e_0 on the device, as one CUDA graph
+// (norm, v_0, the m - 1 Lanczos steps, the small exponential, the
+// combination): no host round trip, so nsteps steps are nsteps graph launches.
+struct EvolveGraph {
+  cudaGraphExec_t exec = nullptr;
+  const cplx* psi = nullptr;
+  double h = 0.0;
+  int m = 0, mv_kind = 0;
+  int64_t kernels = 0;
+  DBuf<double> nrm2;
+  DBuf<int> has_im, act;
+  DBuf<cplx> y;
+  DBuf<long long> matvecs;
+  ~EvolveGraph() {
+    if (exec) cudaGraphExecDestroy(exec);
+  }
+};
+
+void EvolveGraphDeleter::operator()(EvolveGraph* g) const { delete g; }
+
 template <typename MV>
-static void lanczos_evolve_impl(qd_ham* H, const cplx* psi_in, cplx* psi_out, const double* psi_nrm2, double h,
-                                int m, int* act_out) {
+static void lanczos_evolve_steps(qd_ham* H, cplx* psi, double h, int m, int nsteps, int* act_out,
+                                 int64_t* matvecs_out) {
   Ctx* ctx = H->ctx;
   const int64_t n = H->dim;
   const int kdim = m - 1;
@@ -743,76 +871,103 @@ static void lanczos_evolve_impl(qd_ham* H, const cplx* psi_in, cplx* psi_out, co
   const MV* vals = nullptr;
   if constexpr (std::is_same<MV, double>::value) vals = H->vals_r.p;
   else vals = H->vals_c.p;
-  const int vg = vec_grid(ctx, n);
-  QD_CUDA(cudaMemsetAsync(B.stop.p, 0, sizeof(int), ctx->stream));
+  const int mv_kind = std::is_same<MV, double>::value ? 1 : 2;
+  if (!W.evolve) W.evolve.reset(new EvolveGraph());
+  EvolveGraph& G = *W.evolve;
+  if (!G.nrm2.p) {
+    G.nrm2.alloc(1);
+    G.has_im.alloc(1);
+    G.act.alloc(1);
+    G.y.alloc(64);
+    G.matvecs.alloc(1);
+  }
   const double one = 1.0;
   QD_CUDA(cudaMemcpyAsync(B.scl.p, &one, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  init_v0_kernel<cplx><<<vg, kVecThreads, 0, ctx->stream>>>(n, psi_in, psi_nrm2, B.V.p);
-  QD_CHECK_LAUNCH();
-  QD_LAUNCHED(ctx);
+  QD_CUDA(cudaMemsetAsync(G.matvecs.p, 0, sizeof(long long), ctx->stream));
   if (B.kind != 0) {
     B.drop_graph();
     B.kind = 0;
   }
-  B.run_graph(ctx, [&]() { lanczos_run<MV, cplx>(H, vals, B, kdim, W, false); });
-  std::vector<cplx> alpha(kdim + 1);
-  std::vector<double> nrm(kdim + 1), scl(kdim + 1);
-  int stop = 0;
-  QD_CUDA(cudaMemcpyAsync(alpha.data(), B.alpha.p, (kdim + 1) * sizeof(cplx), cudaMemcpyDeviceToHost, ctx->stream));
-  QD_CUDA(cudaMemcpyAsync(nrm.data(), B.nrm.p, (kdim + 1) * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-  QD_CUDA(cudaMemcpyAsync(scl.data(), B.scl.p, (kdim + 1) * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-  QD_CUDA(cudaMemcpyAsync(&stop, B.stop.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-  QD_CUDA(cudaStreamSynchronize(ctx->stream));
-  const int act = stop ? stop : kdim;
-  std::vector<double> d(act), e(act), z((size_t)act * act, 0.0);
-  for (int i = 0; i < act; ++i) {
-    d[i] = alpha[i + 1].re;
-    e[i] = (i + 1 < act) ? nrm[i + 1] : 0.0;
-    z[(size_t)i * act + i] = 1.0;
-  }
-  QD_REQUIRE(tridiag_ql<double>(act, d.data(), e.data(), z.data(), act) == 0, QD_ERR_INVALID,
-             "tridiagonal eigensolver did not converge");
-  // c_j = sum_l Q(j, l) exp(-i h lambda_l) Q(0, l); column l of Q is z[l * act ...]
-  std::vector<cplx> y(act);
-  for (int j = 0; j < act; ++j) {
-    double re = 0.0, im = 0.0;
-    for (int l = 0; l < act; ++l) {
-      const double w = z[(size_t)l * act + j] * z[(size_t)l * act + 0];
-      re += w * std::cos(h * d[l]);
-      im -= w * std::sin(h * d[l]);
+  if (!G.exec || G.psi != psi || G.h != h || G.m != m || G.mv_kind != mv_kind) {
+    if (G.exec) cudaGraphExecDestroy(G.exec);
+    G.exec = nullptr;
+    const int vg = vec_grid(ctx, n);
+    cudaGraph_t g = nullptr;
+    const int64_t before = ctx->launches;
+    QD_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      QD_CUDA(cudaMemsetAsync(B.stop.p, 0, sizeof(int), ctx->stream));
+      colnorm_kernel<<<vg, kVecThreads, 0, ctx->stream>>>(n, psi, G.nrm2.p, W.red_d(0), G.has_im.p);
+      QD_CHECK_LAUNCH();
+      QD_LAUNCHED(ctx);
+      init_v0_kernel<cplx><<<vg, kVecThreads, 0, ctx->stream>>>(n, psi, G.nrm2.p, B.V.p);
+      QD_CHECK_LAUNCH();
+      QD_LAUNCHED(ctx);
+      lanczos_run<MV, cplx>(H, vals, B, kdim, W, false);
+      texp_kernel<<<1, 32, 0, ctx->stream>>>(kdim, h, B.alpha.p, B.nrm.p, B.scl.p, B.stop.p, G.y.p, G.act.p,
+                                             G.matvecs.p);
+      QD_CHECK_LAUNCH();
+      QD_LAUNCHED(ctx);
+      combine_dev_kernel<<<vg, kVecThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, G.y.p, G.act.p, psi);
+      QD_CHECK_LAUNCH();
+      QD_LAUNCHED(ctx);
+    } catch (...) {
+      cudaStreamEndCapture(ctx->stream, &g);
+      if (g) cudaGraphDestroy(g);
+      ctx->launches = before;
+      throw;
     }
-    y[j] = mkc(re * scl[j], im * scl[j]);
+    QD_CUDA(cudaStreamEndCapture(ctx->stream, &g));
+    G.kernels = ctx->launches - before;
+    ctx->launches = before;
+    const cudaError_t e = cudaGraphInstantiate(&G.exec, g, 0);
+    cudaGraphDestroy(g);
+    QD_CUDA(e);
+    G.psi = psi;
+    G.h = h;
+    G.m = m;
+    G.mv_kind = mv_kind;
   }
-  DBuf<cplx> dy(act);
-  QD_CUDA(cudaMemcpyAsync(dy.p, y.data(), act * sizeof(cplx), cudaMemcpyHostToDevice, ctx->stream));
-  combine_kernel<cplx><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, dy.p, act, psi_out);
-  QD_CHECK_LAUNCH();
-  QD_LAUNCHED(ctx);
+  for (int s = 0; s < nsteps; ++s) {
+    QD_CUDA(cudaGraphLaunch(G.exec, ctx->stream));
+    ctx->launches += G.kernels;
+  }
+  int act = 0;
+  long long mv = 0;
+  QD_CUDA(cudaMemcpyAsync(&act, G.act.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(&mv, G.matvecs.p, sizeof(long long), cudaMemcpyDeviceToHost, ctx->stream));
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
   if (act_out) *act_out = act;
+  if (matvecs_out) *matvecs_out = mv;
 }
 
-void lanczos_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int m, int* act_out) {
+void lanczos_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int m, int nsteps, int* act_out,
+                    int64_t* matvecs_out) {
   Ctx* ctx = H->ctx;
   const int64_t n = H->dim;
-  QD_REQUIRE(m >= 2 && m <= 4097, QD_ERR_INVALID, "Krylov dimension must be in 2..4097");
+  QD_REQUIRE(m >= 2 && m <= 33, QD_ERR_INVALID, "Krylov dimension must be in 2..33");
+  QD_REQUIRE(nsteps >= 1, QD_ERR_INVALID, "nsteps must be positive");
   QD_REQUIRE(H->flags & QD_HAM_HERMITIAN, QD_ERR_NOT_HERMITIAN,
              "the short-recurrence Krylov exponential needs a Hermitian operator");
   Workspace& W = ham_workspace(H);
-  DBuf<double> nrm2(1);
-  DBuf<int> has_im(1);
-  QD_CUDA(cudaMemsetAsync(has_im.p, 0, sizeof(int), ctx->stream));
-  colnorm_kernel<<<vec_grid(ctx, n), kVecThreads, 0, ctx->stream>>>(n, psi_in, nrm2.p, W.red_d(0), has_im.p);
-  QD_CHECK_LAUNCH();
-  QD_LAUNCHED(ctx);
-  double hn = 0.0;
-  QD_CUDA(cudaMemcpyAsync(&hn, nrm2.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-  QD_CUDA(cudaStreamSynchronize(ctx->stream));
-  QD_REQUIRE(hn > 0.0 && std::isfinite(hn), QD_ERR_INVALID, "input state has zero or non-finite norm");
+  {
+    DBuf<double> nrm2(1);
+    DBuf<int> has_im(1);
+    QD_CUDA(cudaMemsetAsync(has_im.p, 0, sizeof(int), ctx->stream));
+    colnorm_kernel<<<vec_grid(ctx, n), kVecThreads, 0, ctx->stream>>>(n, psi_in, nrm2.p, W.red_d(0), has_im.p);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+    double hn = 0.0;
+    QD_CUDA(cudaMemcpyAsync(&hn, nrm2.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    QD_CUDA(cudaStreamSynchronize(ctx->stream));
+    QD_REQUIRE(hn > 0.0 && std::isfinite(hn), QD_ERR_INVALID, "input state has zero or non-finite norm");
+  }
+  if (psi_out != psi_in)
+    QD_CUDA(cudaMemcpyAsync(psi_out, psi_in, n * sizeof(cplx), cudaMemcpyDeviceToDevice, ctx->stream));
   if (H->flags & QD_HAM_REAL)
-    lanczos_evolve_impl<double>(H, psi_in, psi_out, nrm2.p, h, m, act_out);
+    lanczos_evolve_steps<double>(H, psi_out, h, m, nsteps, act_out, matvecs_out);
   else
-    lanczos_evolve_impl<cplx>(H, psi_in, psi_out, nrm2.p, h, m, act_out);
+    lanczos_evolve_steps<cplx>(H, psi_out, h, m, nsteps, act_out, matvecs_out);
 }
 
 }  // namespace qd

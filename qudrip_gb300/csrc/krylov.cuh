@@ -26,8 +26,16 @@ struct LanczosBuffers {
   DBuf<Tri<VV>> dots;  // per step: <V2, w>, <V1, w>, <V1, V2>
   DBuf<double> nrm, nrm2, y, scl;  // scl[k] = 1 / ||V[k]|| (basis stored unnormalised)
   DBuf<int> stop;
+  DBuf<__int128> X;  // fixed-point copies of the two newest basis vectors (uniform-coupling product)
+  DBuf<int> ovf;
   cudaGraphExec_t exec = nullptr;
-  int kind = 0;  // product the captured graph launches (0 CSR, 1 matrix-free)
+  int kind = 0;  // product the captured graph launches (0 CSR, 1 matrix-free, 2 fixed-point)
+  void ensure_fx() {
+    if (!X.p) {
+      X.alloc((size_t)2 * ld);
+      ovf.alloc(1);
+    }
+  }
   int64_t graph_kernels = 0;
 
   void ensure(int64_t n_, int kdim_) {
@@ -46,6 +54,7 @@ struct LanczosBuffers {
     y.alloc(kdim + 2);
     scl.alloc(kdim + 2);
     stop.alloc(1);
+    X = DBuf<__int128>();
   }
   void drop_graph() {
     if (exec) cudaGraphExecDestroy(exec);
@@ -78,8 +87,14 @@ struct LanczosBuffers {
   ~LanczosBuffers() { drop_graph(); }
 };
 
+struct EvolveGraph;
+struct EvolveGraphDeleter {
+  void operator()(EvolveGraph* g) const;
+};
+
 struct Workspace {
   Ctx* ctx;
+  std::unique_ptr<EvolveGraph, EvolveGraphDeleter> evolve;  // cached Krylov-step graph
   DBuf<double> partials_d, gpart_d;
   DBuf<cplx> partials_c, gpart_c;
   DBuf<Tri<double>> partials_td, gpart_td;
@@ -110,7 +125,8 @@ cplx state_eval(qd_ham* H, const cplx* psi);
 double state_norm2(qd_ham* H, const cplx* psi);
 void lanczos_ground(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, double* evals_out, qd_lanczos_result* res);
 void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per_launch);
-void lanczos_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int m, int* act_out);
+void lanczos_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int m, int nsteps, int* act_out,
+                    int64_t* matvecs_out);
 void hermitian_lanczos_ground(qd_ham* H, cplx* psi, int kdim, double* evals_out, qd_lanczos_result* res);
 template <typename VV>
 void launch_mf(Ctx* ctx, qd_ham* H, const VV* x, VV* y, double scale, const double* scale_dev, const int* stop,

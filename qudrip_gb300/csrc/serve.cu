@@ -27,6 +27,8 @@
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <memory>
@@ -169,7 +171,7 @@ struct qd_server {
 namespace qd {
 
 static bool batchable(const qd_server* S, const ServeReq* r) {
-  return S->has_batch && r->d.kind == QD_REQ_GROUND && r->dim_est <= S->o.small_dim && r->d.psi_out == nullptr &&
+  return S->has_batch && r->d.kind == QD_REQ_GROUND && r->dim_est <= S->o.batch_dim && r->d.psi_out == nullptr &&
          r->real_start && r->d.krylov_dim <= 256;
 }
 
@@ -263,15 +265,26 @@ static void build_request(Ctx* ctx, ServeReq* r, Built& b) {
 }
 
 // One request with the grid-wide solvers on this lane's stream.
+static bool trace_on() {
+  static const bool on = std::getenv("QD_SERVE_TRACE") != nullptr;
+  return on;
+}
+
 static void run_single(qd_server* S, Lane* L, ServeReq* r, Built* prebuilt) {
   qd_result res;
   std::memset(&res, 0, sizeof(res));
   res.path = QD_PATH_GRID;
   Ctx* ctx = &L->ctx;
+  const double t0 = S->now();
+  double t_built = t0, t_solved = t0;
   try {
     Built own;
     Built& b = prebuilt ? *prebuilt : own;
     if (!b.H) build_request(ctx, r, b);
+    if (trace_on()) {
+      QD_CUDA(cudaStreamSynchronize(ctx->stream));
+      t_built = S->now();
+    }
     qd_ham* H = b.H;
     const int64_t n = H->dim;
     res.dim = n;
@@ -300,14 +313,21 @@ static void run_single(qd_server* S, Lane* L, ServeReq* r, Built* prebuilt) {
     } else {
       const bool fast = (S->o.mode == QD_SERVE_MIXED) && (H->flags & QD_HAM_HERMITIAN);
       int act = 0;
-      for (int s = 0; s < r->d.nsteps; ++s) {
-        if (fast)
-          lanczos_evolve(H, psi.p, psi.p, r->d.dt, r->d.krylov_dim, &act);
-        else
+      if (fast) {
+        int64_t mv = 0;
+        lanczos_evolve(H, psi.p, psi.p, r->d.dt, r->d.krylov_dim, r->d.nsteps, &act, &mv);
+        res.matvecs += mv;
+      } else {
+        for (int s = 0; s < r->d.nsteps; ++s) {
           arnoldi_evolve(H, psi.p, psi.p, r->d.dt, r->d.krylov_dim, &act);
-        res.matvecs += act;
+          res.matvecs += act;
+        }
       }
       res.act_dim = act;
+    }
+    if (trace_on()) {
+      QD_CUDA(cudaStreamSynchronize(ctx->stream));
+      t_solved = S->now();
     }
     recharge(S, r, held_bytes(b.sec, H) + (int64_t)psi.bytes());
     const double n2 = state_norm2(H, psi.p);
@@ -329,6 +349,10 @@ static void run_single(qd_server* S, Lane* L, ServeReq* r, Built* prebuilt) {
     res.status = QD_ERR_INVALID;
     cudaStreamSynchronize(ctx->stream);
   }
+  if (trace_on())
+    std::fprintf(stderr, "[qd serve] id=%llu kind=%d lane=%d dim=%lld build=%.2fms solve=%.2fms rest=%.2fms\n",
+                 (unsigned long long)r->id, r->d.kind, (int)L->kind, (long long)res.dim, 1e3 * (t_built - t0),
+                 1e3 * (t_solved - t_built), 1e3 * (S->now() - t_solved));
   finish(S, r, res);
 }
 
@@ -358,6 +382,7 @@ static void run_batch(qd_server* S, Lane* L, std::vector<ServeReq*>& rs) {
     }
   }
   if (ok.empty()) return;
+  const double t_built = S->now();
   std::vector<qd_ham*> hams;
   std::vector<std::vector<double>> v0(ok.size());
   std::vector<const double*> v0p;
@@ -386,6 +411,9 @@ static void run_batch(qd_server* S, Lane* L, std::vector<ServeReq*>& rs) {
     S->batches++;
     S->batched += (int64_t)ok.size();
   }
+  if (trace_on())
+    std::fprintf(stderr, "[qd serve] batch of %zu: builds done at %.2fms, solved at %.2fms\n", ok.size(),
+                 1e3 * t_built, 1e3 * S->now());
   for (size_t q = 0; q < ok.size(); ++q) {
     qd_result res;
     std::memset(&res, 0, sizeof(res));
@@ -452,6 +480,7 @@ qd_status qd_server_create(qd_ctx* ctx_, const qd_server_opts* opts, qd_server**
     if (o.mode == QD_SERVE_PLAIN) o.batch_lanes = 0;
     if (o.batch_max <= 0) o.batch_max = 64;
     if (o.small_dim <= 0) o.small_dim = 65536;
+    if (o.batch_dim <= 0) o.batch_dim = 16384;
     QD_REQUIRE(o.small_lanes + o.large_lanes + o.batch_lanes <= 64, QD_ERR_INVALID, "at most 64 lanes");
     if (o.hbm_budget <= 0) {
       size_t fr = 0, tot = 0;

@@ -31,6 +31,7 @@ enum SpmvVariant {
   kSpmvRowExact = 110,  // thread per row, groups of 4 loads, exact-count tail
   kSpmvRowSorted = 111, // as 110, rows taken in length order within 256-row windows
   kSpmvLast = 111,
+  kSpmvFx = 120,        // uniform-coupling form, exact fixed-point sums (fxsum.cuh)
 };
 
 constexpr int kSpmvWarps = 4;  // warps per block

@@ -349,7 +349,7 @@ class HermitianLanczosSolver:
         self.result = None
 
     def getGroundState(self, H: Hamiltonian, psi: State, tstp: int):
-        evals = np.empty(self.kry_dim, dtype=np.float64)
+        evals = np.empty(self.kry_dim + 1, dtype=np.float64)
         res = A.qd_lanczos_result()
         A.call("qd_hermitian_lanczos_ground", H.handle, psi.handle, tstp, self.kry_dim,
                evals.ctypes.data_as(C.POINTER(C.c_double)), C.byref(res))
@@ -422,11 +422,11 @@ def traj_run(heff: Hamiltonian, psi0, ntraj: int, nsteps: int, dt: float, gamma:
     return mean, err, st
 
 
-def lanczos_evolve(H: Hamiltonian, psi: State, t_in: int, t_out: int, h: float, m: int) -> int:
-    """psi(t_out) = exp(-i H h) psi(t_in) by the short-recurrence Krylov
-    exponential (Hermitian H); returns the Krylov dimension used."""
+def lanczos_evolve(H: Hamiltonian, psi: State, t_in: int, t_out: int, h: float, m: int, nsteps: int = 1) -> int:
+    """psi(t_out) = exp(-i H h)^nsteps psi(t_in) by the short-recurrence Krylov
+    exponential (Hermitian H); returns the last step's Krylov dimension."""
     act = C.c_int(0)
-    A.call("qd_lanczos_evolve", H.handle, psi.handle, t_in, t_out, h, m, C.byref(act))
+    A.call("qd_lanczos_evolve", H.handle, psi.handle, t_in, t_out, h, m, nsteps, C.byref(act))
     return act.value
 
 
@@ -447,7 +447,7 @@ class Server:
     """
 
     def __init__(self, mode: str = "mixed", small_lanes: int = 4, large_lanes: int = 3, batch_lanes: int = 2,
-                 batch_max: int = 64, small_dim: int = 65536, hbm_budget: int = 0,
+                 batch_max: int = 64, small_dim: int = 65536, hbm_budget: int = 0, batch_dim: int = 16384,
                  ctx: Optional[Context] = None):
         self.ctx = ctx or default_context()
         o = A.qd_server_opts()
@@ -458,6 +458,7 @@ class Server:
         o.batch_max = batch_max
         o.small_dim = small_dim
         o.hbm_budget = hbm_budget
+        o.batch_dim = batch_dim
         self.handle = C.c_void_p()
         A.call("qd_server_create", self.ctx.handle, C.byref(o), C.byref(self.handle))
         self.mode = mode

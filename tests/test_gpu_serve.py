@@ -75,6 +75,11 @@ def test_lanczos_evolve_matches_arnoldi_and_expm(ctx, complex_h):
     Hs = H.scipy()
     ex = sla.expm_multiply(-1j * dt * nsteps * Hs, x / np.linalg.norm(x))
     assert np.linalg.norm(got - ex) < 1e-9
+    # all steps in one call (one graph launch per step) give the same bits
+    psi.set(1, x)
+    act = q.lanczos_evolve(H, psi, 1, 1, dt, m, nsteps=nsteps)
+    assert act == m - 1
+    assert np.array_equal(psi.get(1), got)
 
 
 def test_lanczos_evolve_breakdown_keeps_the_reference_count(ctx):
