@@ -51,14 +51,19 @@ def dist_env():
 
 
 class Dist:
-    def __init__(self, world, local):
+    """Replica bookkeeping across ranks: a barrier and max/sum of per-rank
+    numbers (NCCL between GPUs; gloo on CPU for the host-side tests)."""
+
+    def __init__(self, world, local, backend="nccl"):
         self.world = world
         self.pg = None
+        self.device = "cuda" if backend == "nccl" else "cpu"
         if world > 1:
             import torch
             import torch.distributed as dist
-            torch.cuda.set_device(local)
-            dist.init_process_group("nccl")
+            if backend == "nccl":
+                torch.cuda.set_device(local)
+            dist.init_process_group(backend)
             self.dist = dist
             self.torch = torch
 
@@ -66,19 +71,16 @@ class Dist:
         if self.world > 1:
             self.dist.barrier()
 
-    def max(self, x: float) -> float:
-        if self.world == 1:
-            return x
-        t = self.torch.tensor([x], dtype=self.torch.float64, device="cuda")
-        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+    def _reduce(self, x: float, op) -> float:
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=op)
         return float(t.item())
 
+    def max(self, x: float) -> float:
+        return x if self.world == 1 else self._reduce(x, self.dist.ReduceOp.MAX)
+
     def sum(self, x: float) -> float:
-        if self.world == 1:
-            return x
-        t = self.torch.tensor([x], dtype=self.torch.float64, device="cuda")
-        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
-        return float(t.item())
+        return x if self.world == 1 else self._reduce(x, self.dist.ReduceOp.SUM)
 
     def close(self):
         if self.world > 1:
@@ -185,24 +187,49 @@ def run_cpu_steps(H, v0, kry, steps):
     return mv, dt
 
 
+def run_cpu_threads(H, v0, kry, steps, nthreads):
+    """`nthreads` host threads each run `steps` oracle Lanczos solves on the
+    shared read-only Hamiltonian (ctypes releases the GIL inside the oracle)."""
+    import threading
+    counts = [0] * nthreads
+
+    def work(i):
+        counts[i] = run_cpu_steps(H, v0, kry, steps)[0]
+
+    th = [threading.Thread(target=work, args=(i,)) for i in range(nthreads)]
+    t0 = time.perf_counter()
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    return sum(counts), time.perf_counter() - t0
+
+
 def reference_arm(args, rank, world):
     if rank != 0:
         return 0
     H, v0 = cpu_sample(4, 0)
     kry = 4  # bounded sample: 2*4 products per solve (first pass + getState pass)
-    run_cpu_steps(H, v0, kry, args.warmup)
-    mv, dt = run_cpu_steps(H, v0, kry, args.steps)
-    value = mv / dt
+    nthreads = max(1, len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count() or 1)
+    run_cpu_threads(H, v0, kry, 1, nthreads)
+    t_all = 0.0
+    mv_all = 0
+    for _ in range(args.steps):
+        mv, dt = run_cpu_threads(H, v0, kry, 1, nthreads)
+        mv_all += mv
+        t_all += dt
+    value = mv_all / t_all
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_all / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
         "data": "synthetic (seeded uniform[-1,1] start vector)",
         "config": {"workload": "xxz_chain_L24_periodic_Sz0_lanczos", "L": L, "dim": H.dim, "nnz": H.nnz,
-                   "krylov_dim_sample": kry, "spmv": "csc_column_push_complex128"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": f"{args.steps} Lanczos solves with krylov_dim={kry} at L=24 "
-                                   "(CPU restatement of the reference; the reference is single-threaded)"},
+                   "krylov_dim_sample": kry, "spmv": "csc_column_push_complex128", "threads": nthreads},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": f"each step: {nthreads} concurrent Lanczos solves (one per host thread) with "
+                                   f"krylov_dim={kry} at L=24 on one shared CSC matrix (CPU restatement of the "
+                                   "reference, which is single-threaded per solve)"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -262,7 +289,14 @@ def gpu_arm(args, rank, world, local):
     A.call("qd_ham_time_spmv", H.handle, A.QD_SPMV_CSR, 50, C.byref(avg_ms), C.byref(nbytes))
     hbm_peak, peak_kind = peaks()
     achieved = nbytes.value / (avg_ms.value * 1e-3) / 1e9
-    traffic = profile_traffic("spmv_csr_f64_xxz_L24")
+    info = A.qd_ham_info()
+    A.call("qd_ham_get_info", H.handle, C.byref(info))
+    if info.product_kernel == 120:
+        kernel_name, spmv_name = "spmv_fx_dots_kernel<true>", "uniform_coupling_fixed_point_sums_fused_dots"
+        traffic = profile_traffic("spmv_fx_dots_xxz_L24")
+    else:
+        kernel_name, spmv_name = "spmv_rowexact_kernel<double,double>", "csr_row_exact_fp64"
+        traffic = profile_traffic("spmv_csr_f64_xxz_L24")
 
     # end to end through the public API with pinned host buffers
     hb = C.c_void_p()
@@ -298,6 +332,7 @@ def gpu_arm(args, rank, world, local):
 
     extras = {}
     if not args.no_extras:
+        extras["matrix_free_L24"] = matrix_free_leg(ctx, H, sec, psi, ritz)
         extras["batched_disorder_sweep"] = batched_sweep(ctx)
         extras["jump_trajectories"] = trajectory_ensemble(ctx, with_oracle=not args.no_cpu)
         extras["serving_mix"] = serving_mix(args.serve_requests)
@@ -317,7 +352,7 @@ def gpu_arm(args, rank, world, local):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded uniform[-1,1] start vector; Hamiltonian built from the operator tree)",
             "config": {"workload": "xxz_chain_L24_periodic_Sz0_lanczos_k100", "L": L, "Jxy": 1.0, "Jz": 1.0,
-                       "dim": dim, "nnz": H.nnz, "krylov_dim": KRY, "spmv": "csr_row_exact_fp64",
+                       "dim": dim, "nnz": H.nnz, "krylov_dim": KRY, "spmv": spmv_name,
                        "ritz": "stored_basis", "parallelism": f"replicas{world}",
                        "l2": "inputs larger than L2 (CSR 493 MB); no flush",
                        "ritz_value": ritz, "psi_eval": energy.real if energy is not None else None},
@@ -326,7 +361,7 @@ def gpu_arm(args, rank, world, local):
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "traffic": traffic,
-                         "kernel": "spmv_rowexact_kernel<double,double>", "peak_kind": peak_kind,
+                         "kernel": kernel_name, "peak_kind": peak_kind,
                          "bytes_per_launch": nbytes.value, "launch_ms": avg_ms.value},
             "cpu_baseline": cpu,
             "clocks": clk,
@@ -335,6 +370,40 @@ def gpu_arm(args, rank, world, local):
         print(json.dumps(line))
     dist.close()
     return 0
+
+
+def matrix_free_leg(ctx, H, sec, psi, ritz_csr):
+    """Config 2's second product: the same L=24 Lanczos solve through the
+    matrix-free form (no stored matrix), timed, and checked against the FP64
+    reference energy (scipy eigsh, tests/golden) and the CSR-path Ritz value."""
+    import qudrip_gb300 as q
+    from qudrip_gb300 import _capi as A
+    solver = q.LanczosSolver(sec, KRY, spmv=A.QD_SPMV_MATRIX_FREE)
+
+    def solve():
+        A.call("qd_state_copy", psi.handle, 1, psi.handle, 0)
+        return solver.getGroundState(H, psi(0), 0)
+
+    solve()
+    ctx.sync()
+    A.call("qd_ctx_record", ctx.handle, 2)
+    mv = 0
+    n = 2
+    for _ in range(n):
+        r = solve()
+        mv += r.matvecs
+    A.call("qd_ctx_record", ctx.handle, 3)
+    ms = C.c_float(0)
+    A.call("qd_ctx_elapsed", ctx.handle, 2, 3, C.byref(ms))
+    pm, pb = C.c_double(), C.c_double()
+    A.call("qd_ham_time_spmv", H.handle, A.QD_SPMV_MATRIX_FREE, 20, C.byref(pm), C.byref(pb))
+    with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
+        e0 = json.load(f)["heisenberg_periodic_e0"]["24"]["e0"]
+    return {"matvecs_per_s": mv / (ms.value * 1e-3), "ms_per_solve": ms.value / n, "product_ms": pm.value,
+            "bytes_per_product": pb.value, "ritz_value": r.ritz_value,
+            "rel_dE_vs_reference_E0": abs(r.ritz_value - e0) / abs(e0),
+            "rel_dE_vs_csr_path": abs(r.ritz_value - ritz_csr) / abs(ritz_csr),
+            "device_bytes_of_the_operator": "basis 8 B/row + diagonal 8 B/row (no CSR)"}
 
 
 def batched_sweep(ctx, n_inst=512, steps=80, seed=2024):
@@ -551,7 +620,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--no-extras", action="store_true", help="skip the secondary workloads")
-    ap.add_argument("--spmv-only", type=int, default=0, metavar="KERNEL",
+    ap.add_argument("--spmv-only", type=int, default=None, metavar="KERNEL",
                     help="only time product KERNEL on the L=24 matrix (100..111 CSR kernels, 1 matrix-free, "
                          "9999 all)")
     ap.add_argument("--iters", type=int, default=50)
@@ -561,7 +630,7 @@ def main():
     rank, world, local = dist_env()
     if args.impl == "reference":
         return reference_arm(args, rank, world)
-    if args.spmv_only:
+    if args.spmv_only is not None:
         return spmv_only(args, local)
     if args.serve_only:
         print(json.dumps(serving_mix(args.serve_requests)))

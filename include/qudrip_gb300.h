@@ -150,7 +150,11 @@ typedef struct {
 /* The result is bit-identical to the reference's Eigen CSC matrix:    */
 /* same sparsity pattern (explicit zeros from cross-term cancellation   */
 /* kept, leaves with |value| <= 1e-10 dropped before duplicate sums)    */
-/* and the same complex128 values.  It is held on the device as CSR.   */
+/* and the same complex128 values.  It is held on the device as CSR,    */
+/* built row by row from transitions compiled per term when every term  */
+/* acts on at most 6 sites, else by walking each column's operator tree  */
+/* (environment QD_LOWER_TREE=1 forces the tree walk; both give the same */
+/* matrix).                                                            */
 /* ------------------------------------------------------------------ */
 enum { QD_HAM_REAL = 1, QD_HAM_HERMITIAN = 2 };
 
@@ -160,7 +164,7 @@ typedef struct {
   int32_t flags;       /* QD_HAM_REAL | QD_HAM_HERMITIAN */
   int32_t max_row_nnz;
   int32_t has_matrix_free; /* 1 if qd_ham_build_matrix_free succeeded */
-  int32_t reserved;
+  int32_t product_kernel;  /* product the real Lanczos path launches (codes of qd_ham_set_spmv_kernel) */
 } qd_ham_info;
 
 qd_status qd_ham_lower(qd_sector *sec, const qd_term *terms, int nterms,
@@ -415,7 +419,9 @@ qd_status qd_seeded_start(uint64_t seed, int64_t dim, double *host_out);
 /* batches ground states with dim <= batch_dim and a real start vector  */
 /* into one persistent launch per lane pass (qd_batch_lanczos: FP32     */
 /* products and basis, FP64 accumulation and refinement), and evolves   */
-/* Hermitian operators with qd_lanczos_evolve.                          */
+/* Hermitian operators to T = nsteps * dt with qd_lanczos_evolve and its */
+/* own step: m = 32, h = T / ceil(T ||H||_inf / 8) (Krylov error bound    */
+/* below 1e-15 per step), or the requested (dt, m) when that is coarser. */
 /* ------------------------------------------------------------------ */
 enum { QD_REQ_GROUND = 0, QD_REQ_EVOLVE = 1 };
 enum { QD_SERVE_PLAIN = 0, QD_SERVE_MIXED = 1 };

@@ -270,6 +270,8 @@ qd_status qd_ham_get_info(qd_ham* ham, qd_ham_info* info) {
     info->flags = ham->flags;
     info->max_row_nnz = ham->max_row_nnz;
     info->has_matrix_free = ham->has_mf ? 1 : 0;
+    info->product_kernel = ((ham->flags & QD_HAM_REAL) && ham->fx_allowed && ham_build_fx(ham)) ? kSpmvFx
+                                                                                                 : ham->spmv_variant;
   });
 }
 

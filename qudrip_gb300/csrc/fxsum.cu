@@ -6,6 +6,8 @@
 #include "fxsum.cuh"
 #include "ham.cuh"
 #include "scan.cuh"
+#include "spmv.cuh"
+#include "vec.cuh"
 
 namespace qd {
 
@@ -147,8 +149,87 @@ __global__ void __launch_bounds__(256) spmv_fx_kernel(int64_t n, const int32_t* 
       acc += (x0 + x1) + (x2 + x3);
     }
     for (; k < e; ++k) acc += X[__ldcs(colidx + k)];
-    y[r] = sc * fma(cF, (double)acc, __ldg(diag + r) * __ldg(x + r));
+    y[r] = sc * fma(cF, (double)acc, __ldcs(diag + r) * __ldg(x + r));
   }
+}
+
+// The product fused with the Lanczos step's three inner products (K1 + K2):
+// w = s1 H V1 with V1 = x, then d1 = <V2, w>, d2 = <V1, w>, d3 = <V1, V2>,
+// beta = s2 d1 and alpha = s1 (d2 - beta s2 d3), as lz_dots_kernel forms
+// them.  V1[r] is already loaded for the diagonal term and the FP64 pipe is
+// idle while the fixed-point gathers run, so the dots cost one extra 8-byte
+// read per row.  Grid-stride rows on a resident grid, one block reduction per
+// block, two-level grid reduction of the three sums.
+template <bool kHas2>
+__global__ void __launch_bounds__(256) spmv_fx_dots_kernel(
+    int64_t n, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colidx,
+    const double* __restrict__ diag, const double* __restrict__ x, const __int128* __restrict__ X,
+    const double* __restrict__ V2, double* __restrict__ y, double cF, const double* s1, const double* s2,
+    const int* stop, int step, double* beta, double* alpha, Tri<double>* dots, GridRed<Tri<double>> red) {
+  if (stop) {
+    const int st = *stop;
+    if (st != 0 && st < step) return;
+  }
+  const double sc = *s1;
+  Tri<double> acc = vzero(Tri<double>{});
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    const int b = __ldg(rowptr + r), e = __ldg(rowptr + r + 1);
+    __int128 s = 0;
+    int k = b;
+    for (; k + 4 <= e; k += 4) {
+      const int c0 = __ldcs(colidx + k), c1 = __ldcs(colidx + k + 1), c2 = __ldcs(colidx + k + 2),
+                c3 = __ldcs(colidx + k + 3);
+      const __int128 x0 = X[c0], x1 = X[c1], x2 = X[c2], x3 = X[c3];
+      s += (x0 + x1) + (x2 + x3);
+    }
+    for (; k < e; ++k) s += X[__ldcs(colidx + k)];
+    const double xr = __ldg(x + r);
+    const double w = sc * fma(cF, (double)s, __ldcs(diag + r) * xr);
+    y[r] = w;
+    acc.b = fma(xr, w, acc.b);
+    if (kHas2) {
+      const double v2 = __ldg(V2 + r);
+      acc.a = fma(v2, w, acc.a);
+      acc.c = fma(xr, v2, acc.c);
+    }
+  }
+  if (grid_sum(acc, red, dots) && threadIdx.x == 0) {
+    const Tri<double> d = *dots;
+    const double bt = kHas2 ? (*s2) * d.a : 0.0;
+    double t = d.b;
+    if (kHas2) t = fma(-(bt * (*s2)), d.c, t);
+    *beta = bt;
+    *alpha = (*s1) * t;
+  }
+}
+
+static int fx_dots_grid(Ctx* ctx, int64_t n) {
+  static thread_local int per_sm = 0;
+  if (!per_sm) {
+    int a = 0, b = 0;
+    QD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, spmv_fx_dots_kernel<true>, 256, 0));
+    QD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, spmv_fx_dots_kernel<false>, 256, 0));
+    per_sm = std::max(1, std::min(a, b));
+  }
+  return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)ctx->num_sms * per_sm));
+}
+
+void launch_fx_dots(Ctx* ctx, const qd_ham* H, const double* x, const __int128* X, const double* V2, double* y,
+                    const double* s1, const double* s2, const int* stop, int step, double* beta, double* alpha,
+                    Tri<double>* dots, GridRed<Tri<double>> red) {
+  const FxForm& f = *H->fx;
+  const double cF = std::ldexp(f.c, -f.F);
+  const int g = fx_dots_grid(ctx, H->dim);
+  QD_REQUIRE(g <= kMaxGrid, QD_ERR_UNSUPPORTED, "reduction grid exceeds its partials buffer");
+  if (V2)
+    spmv_fx_dots_kernel<true><<<g, 256, 0, ctx->stream>>>(H->dim, f.rowptr.p, f.colidx.p, f.diag.p, x, X, V2, y, cF,
+                                                           s1, s2, stop, step, beta, alpha, dots, red);
+  else
+    spmv_fx_dots_kernel<false><<<g, 256, 0, ctx->stream>>>(H->dim, f.rowptr.p, f.colidx.p, f.diag.p, x, X, x, y,
+                                                            cF, s1, s1, stop, step, beta, alpha, dots, red);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
 }
 
 // X = fixed-point copy of x (v_0 of a Lanczos run).

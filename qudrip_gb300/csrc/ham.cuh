@@ -77,6 +77,7 @@ struct qd_ham {
   int64_t nnz = 0;
   int flags = 0;
   int max_row_nnz = 0;
+  double norm_inf = -1.0;  // max row sum of |H| (ham_norm_inf), -1 until computed
   int spmv_variant = 110;  // CSR product kernel the solvers launch (krylov.cuh SpmvVariant)
   qd::DBuf<int64_t> rowptr;
   qd::DBuf<int32_t> colidx;
@@ -109,10 +110,12 @@ void ham_lower(qd_ham* H, const qd_term* terms, int nterms, const qd_gate* gates
 void ham_transpose(Ctx* ctx, int64_t n, const int64_t* ptr, const int32_t* idx, const cplx* vals,
                    int64_t nnz, int64_t* out_ptr, int32_t* out_idx, cplx* out_vals);
 void ham_build_matrix_free(qd_ham* H);
+bool ham_lower_pull(qd_ham* H);
 void mf_apply_c(qd_ham* H, const cplx* x, cplx* y);
 bool ham_build_fx(qd_ham* H);
 void launch_fx(Ctx* ctx, const qd_ham* H, const double* x, const __int128* X, double* y, const double* scale_dev,
                const int* stop, int step);
 void launch_fx_shadow(Ctx* ctx, int64_t n, const double* x, __int128* X, int F, int* ovf);
 void ham_ensure_row_order(qd_ham* H);
+double ham_norm_inf(qd_ham* H);
 }  // namespace qd

@@ -213,20 +213,24 @@ template <typename VV>
 static void lz_vector_passes(Ctx* ctx, int64_t n, int* stop, int step, const VV* w, const VV* V1, const VV* V2,
                              const double* s1, const double* s2, VV* beta, VV* alpha, Tri<VV>* dots, VV* Vk,
                              double* nrm2, double* nrm, double* sk, GridRed<Tri<VV>> rt, GridRed<double> rd,
-                             __int128* Xk = nullptr, int F = 0, int* ovf = nullptr) {
+                             __int128* Xk = nullptr, int F = 0, int* ovf = nullptr, bool dots_done = false) {
   const int g = lz_grid(ctx, n / LzPack<VV>::kPer + 1);
   if (V2) {
-    lz_dots_kernel<VV, true><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V2, s1, s2, beta, alpha, dots,
-                                                                rt);
-    QD_CHECK_LAUNCH();
-    QD_LAUNCHED(ctx);
+    if (!dots_done) {
+      lz_dots_kernel<VV, true><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V2, s1, s2, beta, alpha,
+                                                                  dots, rt);
+      QD_CHECK_LAUNCH();
+      QD_LAUNCHED(ctx);
+    }
     lz_update_kernel<VV, true><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V2, s1, s2, alpha, beta, Vk,
                                                                   nrm2, nrm, sk, rd, Xk, F, ovf);
   } else {
-    lz_dots_kernel<VV, false><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V1, s1, s1, beta, alpha,
-                                                                 dots, rt);
-    QD_CHECK_LAUNCH();
-    QD_LAUNCHED(ctx);
+    if (!dots_done) {
+      lz_dots_kernel<VV, false><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V1, s1, s1, beta, alpha,
+                                                                   dots, rt);
+      QD_CHECK_LAUNCH();
+      QD_LAUNCHED(ctx);
+    }
     lz_update_kernel<VV, false><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V1, s1, s1, alpha, beta,
                                                                    Vk, nrm2, nrm, sk, rd, Xk, F, ovf);
   }
@@ -379,6 +383,12 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   DBuf<__int128> X(fx ? n + 32 : 1);
   if (fx) QD_CUDA(cudaMemsetAsync(X.p, 0, X.bytes(), ctx->stream));
   auto launch = [&]() {
+    if (fx && spmv == QD_SPMV_CSR) {  // what the recurrence launches: the product fused with its dots
+      double* d = (double*)scal.p;
+      launch_fx_dots(ctx, H, (const double*)x.p, X.p, (const double*)z.p, (double*)y.p, s1, s1, nullptr, 0, d + 1,
+                     d + 2, reinterpret_cast<Tri<double>*>(d + 6), W.red_tri<double>(2));
+      return;
+    }
     if (fx) {
       launch_fx(ctx, H, (const double*)x.p, X.p, (double*)y.p, nullptr, nullptr, 0);
       return;
@@ -428,8 +438,9 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   *bytes_per_launch = (double)H->nnz * (mvb + 4.0) + (double)(n + 1) * 8.0 + (double)n * 2.0 * (double)vb;
   if (mf)  // basis word, diagonal, x[r], y[r] per row (the gathered x comes from L2)
     *bytes_per_launch = (double)n * (8.0 + (H->mf_real ? 8.0 : 16.0) + 2.0 * (double)vb);
-  if (fx)  // columns, row pointers (int32), diagonal, x, its fixed-point copy, y
-    *bytes_per_launch = (double)H->fx->nnz * 4.0 + (double)(n + 1) * 4.0 + (double)n * (8.0 + 8.0 + 16.0 + 8.0);
+  if (fx)  // columns, row pointers (int32), diagonal, x, its fixed-point copy, y (+ v2 for the fused dots)
+    *bytes_per_launch = (double)H->fx->nnz * 4.0 + (double)(n + 1) * 4.0 +
+                        (double)n * (8.0 + 8.0 + 16.0 + 8.0 + (spmv == QD_SPMV_CSR ? 8.0 : 0.0));
 }
 
 // ---------------------------------------------------------------- Lanczos
@@ -447,8 +458,10 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int kd
     // K1: w = s1 * H V1 (CSR, fixed-point uniform-coupling form, or matrix-free)
     __int128* Xprev = fx ? B.X.p + (int64_t)((k - 1) & 1) * B.ld : nullptr;
     __int128* Xnext = fx ? B.X.p + (int64_t)(k & 1) * B.ld : nullptr;
-    if constexpr (std::is_same<VV, double>::value) {
-      if (fx) launch_fx(ctx, H, V1, Xprev, B.w.p, s1, B.stop.p, k);
+    if constexpr (std::is_same<VV, double>::value) {  // product fused with the step's inner products
+      if (fx)
+        launch_fx_dots(ctx, H, V1, Xprev, V2, B.w.p, s1, s2, B.stop.p, k, B.beta.p + k, B.alpha.p + k, B.dots.p + k,
+                       W.red_tri<double>(2));
     }
     if (mf)
       launch_mf<VV>(ctx, H, V1, B.w.p, 1.0, s1, B.stop.p, k);
@@ -458,7 +471,7 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int kd
     // K2, K3 (K3 also writes the fixed-point copy of v_k for the next product)
     lz_vector_passes<VV>(ctx, n, B.stop.p, k, B.w.p, V1, V2, s1, s2, B.beta.p + k, B.alpha.p + k, B.dots.p + k, Vk,
                          B.nrm2.p + k, B.nrm.p + k, B.scl.p + k, W.red_tri<VV>(2), W.red_d(3), Xnext,
-                         fx ? H->fx->F : 0, fx ? B.ovf.p : nullptr);
+                         fx ? H->fx->F : 0, fx ? B.ovf.p : nullptr, fx);
   }
 }
 

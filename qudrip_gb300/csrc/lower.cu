@@ -18,6 +18,7 @@
 // pointers, pass 1 writes rows (sorted) and values.  The CSC result is then
 // transposed into the CSR compute layout.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 
 #include "ham.cuh"
@@ -322,50 +323,55 @@ void ham_lower(qd_ham* H, const qd_term* terms, int nterms, const qd_gate* gates
   QD_CUDA(cudaMemcpyAsync(dterms.p, ht.data(), ht.size() * sizeof(TermDev), cudaMemcpyHostToDevice, ctx->stream));
   QD_CUDA(cudaMemcpyAsync(dgates.p, hg.data(), hg.size() * sizeof(GateDev), cudaMemcpyHostToDevice, ctx->stream));
 
-  LowerParams P;
-  std::memset(&P, 0, sizeof(P));
-  P.S = S->view;
-  P.terms = dterms.p;
-  P.gates = dgates.p;
-  P.nterms = nterms;
+  // Row-wise lowering from compiled transitions when every term is a
+  // product on at most 6 sites (mfree.cu); the tree walk per column otherwise.
+  const bool tree_only = std::getenv("QD_LOWER_TREE") != nullptr;
+  if (tree_only || !ham_lower_pull(H)) {
+    LowerParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.S = S->view;
+    P.terms = dterms.p;
+    P.gates = dgates.p;
+    P.nterms = nterms;
 
-  // Start with the smallest column capacity that the leaf count allows and
-  // grow it only if a column overflows (most operators have short columns).
-  int cap = 0;
-  const int64_t cap_bound = std::min<int64_t>(leaf_total, std::max<int64_t>(dim, 1));
-  DBuf<int> overflow(1);
-  DBuf<int64_t> colptr(dim + 1);
-  LowerFn fn = nullptr;
-  for (int64_t try_cap = 32;; try_cap *= 4) {
-    fn = pick_lower(std::min<int64_t>(std::min<int64_t>(try_cap, cap_bound), 512), max_leaves, cap);
-    QD_REQUIRE(fn != nullptr, QD_ERR_UNSUPPORTED, "lowering: products with %d leaves are not supported",
-               max_leaves);
-    QD_CUDA(cudaMemsetAsync(overflow.p, 0, sizeof(int), ctx->stream));
-    QD_CUDA(cudaMemsetAsync(colptr.p, 0, (dim + 1) * 8, ctx->stream));
-    if (dim > 0) fn(ctx, P, 0, colptr.p, nullptr, nullptr, nullptr, overflow.p);
-    int ovf = 0;
-    QD_CUDA(cudaMemcpyAsync(&ovf, overflow.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    // Start with the smallest column capacity that the leaf count allows and
+    // grow it only if a column overflows (most operators have short columns).
+    int cap = 0;
+    const int64_t cap_bound = std::min<int64_t>(leaf_total, std::max<int64_t>(dim, 1));
+    DBuf<int> overflow(1);
+    DBuf<int64_t> colptr(dim + 1);
+    LowerFn fn = nullptr;
+    for (int64_t try_cap = 32;; try_cap *= 4) {
+      fn = pick_lower(std::min<int64_t>(std::min<int64_t>(try_cap, cap_bound), 512), max_leaves, cap);
+      QD_REQUIRE(fn != nullptr, QD_ERR_UNSUPPORTED, "lowering: products with %d leaves are not supported",
+                 max_leaves);
+      QD_CUDA(cudaMemsetAsync(overflow.p, 0, sizeof(int), ctx->stream));
+      QD_CUDA(cudaMemsetAsync(colptr.p, 0, (dim + 1) * 8, ctx->stream));
+      if (dim > 0) fn(ctx, P, 0, colptr.p, nullptr, nullptr, nullptr, overflow.p);
+      int ovf = 0;
+      QD_CUDA(cudaMemcpyAsync(&ovf, overflow.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+      QD_CUDA(cudaStreamSynchronize(ctx->stream));
+      if (!ovf) break;
+      QD_REQUIRE(cap < 512 && cap < cap_bound, QD_ERR_OVERFLOW, "lowering: a column has more than %d entries", cap);
+    }
+    exclusive_scan_i64(ctx, colptr.p, colptr.p, dim + 1);
+    int64_t nnz = 0;
+    QD_CUDA(cudaMemcpyAsync(&nnz, colptr.p + dim, 8, cudaMemcpyDeviceToHost, ctx->stream));
     QD_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (!ovf) break;
-    QD_REQUIRE(cap < 512 && cap < cap_bound, QD_ERR_OVERFLOW, "lowering: a column has more than %d entries", cap);
-  }
-  exclusive_scan_i64(ctx, colptr.p, colptr.p, dim + 1);
-  int64_t nnz = 0;
-  QD_CUDA(cudaMemcpyAsync(&nnz, colptr.p + dim, 8, cudaMemcpyDeviceToHost, ctx->stream));
-  QD_CUDA(cudaStreamSynchronize(ctx->stream));
-  QD_REQUIRE(nnz < (int64_t)INT32_MAX * 8, QD_ERR_UNSUPPORTED, "nnz too large");
-  H->nnz = nnz;
-  DBuf<int32_t> rowidx(nnz + 1);
-  DBuf<cplx> cvals(nnz + 1);
-  if (dim > 0 && nnz > 0) fn(ctx, P, 1, nullptr, colptr.p, rowidx.p, cvals.p, overflow.p);
+    QD_REQUIRE(nnz < (int64_t)INT32_MAX * 8, QD_ERR_UNSUPPORTED, "nnz too large");
+    H->nnz = nnz;
+    DBuf<int32_t> rowidx(nnz + 1);
+    DBuf<cplx> cvals(nnz + 1);
+    if (dim > 0 && nnz > 0) fn(ctx, P, 1, nullptr, colptr.p, rowidx.p, cvals.p, overflow.p);
 
-  // CSC -> CSR (rows of H); pad the arrays so vector loads past the end stay inside
-  H->rowptr.alloc(dim + 2);
-  H->colidx.alloc(nnz + 16);
-  H->vals_c.alloc(nnz + 16);
-  QD_CUDA(cudaMemsetAsync(H->colidx.p, 0, (nnz + 16) * sizeof(int32_t), ctx->stream));
-  QD_CUDA(cudaMemsetAsync(H->vals_c.p, 0, (nnz + 16) * sizeof(cplx), ctx->stream));
-  ham_transpose(ctx, dim, colptr.p, rowidx.p, cvals.p, nnz, H->rowptr.p, H->colidx.p, H->vals_c.p);
+    // CSC -> CSR (rows of H); pad the arrays so vector loads past the end stay inside
+    H->rowptr.alloc(dim + 2);
+    H->colidx.alloc(nnz + 16);
+    H->vals_c.alloc(nnz + 16);
+    QD_CUDA(cudaMemsetAsync(H->colidx.p, 0, (nnz + 16) * sizeof(int32_t), ctx->stream));
+    QD_CUDA(cudaMemsetAsync(H->vals_c.p, 0, (nnz + 16) * sizeof(cplx), ctx->stream));
+    ham_transpose(ctx, dim, colptr.p, rowidx.p, cvals.p, nnz, H->rowptr.p, H->colidx.p, H->vals_c.p);
+  }
 
   DBuf<int> flags(3);
   QD_CUDA(cudaMemsetAsync(flags.p, 0, 3 * sizeof(int), ctx->stream));
@@ -380,6 +386,7 @@ void ham_lower(qd_ham* H, const qd_term* terms, int nterms, const qd_gate* gates
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
   H->flags = (hf[0] ? 0 : QD_HAM_REAL) | (hf[1] ? 0 : QD_HAM_HERMITIAN);
   H->max_row_nnz = hf[2];
+  const int64_t nnz = H->nnz;
   if (H->flags & QD_HAM_REAL) {
     H->vals_r.alloc(nnz + 16);
     H->vals_f.alloc(nnz + 16);
@@ -393,6 +400,35 @@ void ham_lower(qd_ham* H, const qd_term* terms, int nterms, const qd_gate* gates
     }
   }
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+__global__ void row_abs_max_kernel(int64_t n, const int64_t* rowptr, const cplx* vals, unsigned long long* out) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) s += hypot(vals[k].re, vals[k].im);
+    atomicMax(out, (unsigned long long)__double_as_longlong(s));
+  }
+}
+
+// max_r sum_c |H(r, c)| (cached): bounds the spectral radius.
+double ham_norm_inf(qd_ham* H) {
+  if (H->norm_inf >= 0.0) return H->norm_inf;
+  Ctx* ctx = H->ctx;
+  DBuf<unsigned long long> m(1);
+  QD_CUDA(cudaMemsetAsync(m.p, 0, sizeof(unsigned long long), ctx->stream));
+  if (H->dim > 0) {
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(H->dim, 256), (int64_t)ctx->num_sms * 8));
+    row_abs_max_kernel<<<g, 256, 0, ctx->stream>>>(H->dim, H->rowptr.p, H->vals_c.p, m.p);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+  }
+  unsigned long long bits = 0;
+  QD_CUDA(cudaMemcpyAsync(&bits, m.p, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  double v = 0.0;
+  std::memcpy(&v, &bits, 8);
+  H->norm_inf = v;
+  return v;
 }
 
 void ham_ensure_row_order(qd_ham* H) {

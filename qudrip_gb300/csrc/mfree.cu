@@ -27,6 +27,7 @@
 
 #include "ham.cuh"
 #include "krylov.cuh"
+#include "scan.cuh"
 #include "spmv.cuh"
 
 namespace qd {
@@ -406,6 +407,169 @@ void launch_mf(Ctx* ctx, qd_ham* H, const VV* x, VV* y, double scale, const doub
 
 template void launch_mf<double>(Ctx*, qd_ham*, const double*, double*, double, const double*, const int*, int);
 template void launch_mf<cplx>(Ctx*, qd_ham*, const cplx*, cplx*, double, const double*, const int*, int);
+
+// ---------------------------------------------------------------- row-wise lowering
+// The CSR matrix built from the compiled entries, one thread per row: the
+// row state s takes every entry whose output pattern it carries; entries that
+// land on the same column add in entry order, which is term order, starting
+// from 0 + p -- the union sum of OperatorSum::operator>> (operator_abel.hpp:
+// 25-34) with explicit zeros kept.  Leaf sums inside a term, the 1e-10 leaf
+// filter and every rounding are those of the tree lowering (compile_terms
+// walks the same leaves), so the values equal the tree lowering's; a row
+// pulls ~50 pattern tests instead of a column walking every term's tree.
+struct PullArgs {
+  int64_t dim;
+  const uint64_t* basis;
+  const MfEntry* ent;
+  int nent;
+  int use_tables;
+  MfRank rk;
+  SectorView S;
+};
+
+__device__ __forceinline__ int64_t pull_rank(const PullArgs& A, uint64_t c) {
+  if (!A.use_tables) return sector_rank(A.S, c);
+  int64_t r = 0;
+  for (int f = 0; f < A.rk.nf; ++f) {
+    const int w = A.rk.width[f];
+    const uint64_t v = (c >> A.rk.lo[f]) & ((w >= 64) ? ~0ull : ((1ull << w) - 1));
+    if (A.rk.is_free[f]) {
+      r += (int64_t)v * A.rk.stride[f];
+      continue;
+    }
+    const int k = A.rk.k[f];
+    if (__popcll(v) != k) return A.dim;
+    const int64_t* T = A.rk.tab + A.rk.off[f];
+    int64_t acc = 0;
+    int cb = 0;
+    for (int b = 0; b < A.rk.nb[f]; ++b) {
+      const unsigned byte = (unsigned)(v >> (8 * b)) & 255u;
+      acc += __ldg(T + ((int64_t)b * 256 + byte) * (k + 1) + cb);
+      cb += __popc(byte);
+    }
+    r += acc * A.rk.stride[f];
+  }
+  return r;
+}
+
+constexpr int kPullCap = 64;
+
+__global__ void __launch_bounds__(128) pull_lower_kernel(PullArgs A, int pass, int64_t* counts,
+                                                         const int64_t* rowptr, int32_t* colidx, cplx* vals,
+                                                         int* overflow) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= A.dim) return;
+  const uint64_t s = A.basis[r];
+  int n = 0;
+  int cols[kPullCap];
+  cplx acc[kPullCap];
+  for (int e = 0; e < A.nent; ++e) {
+    const MfEntry E = A.ent[e];
+    if ((s & E.sup) != E.outb) continue;
+    const uint64_t c = s ^ E.flip;
+    const int64_t col = pull_rank(A, c);
+    if (col >= A.dim) continue;  // outside the sector (operator.hpp:196-199)
+    cplx v = E.amp;
+    if (__popcll(c & E.jw) & 1) v = mkc(-v.re, -v.im);
+    int lo = 0, hi = n;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (cols[mid] < (int)col) lo = mid + 1;
+      else hi = mid;
+    }
+    if (lo < n && cols[lo] == (int)col) {
+      acc[lo] = cadd_rn(acc[lo], v);
+    } else {
+      if (n >= kPullCap) {
+        atomicExch(overflow, 1);
+        return;
+      }
+      for (int q = n; q > lo; --q) {
+        cols[q] = cols[q - 1];
+        acc[q] = acc[q - 1];
+      }
+      cols[lo] = (int)col;
+      acc[lo] = cadd_rn(mkc(0.0, 0.0), v);
+      ++n;
+    }
+  }
+  if (pass == 0) {
+    counts[r] = n;
+  } else {
+    const int64_t o = rowptr[r];
+    for (int q = 0; q < n; ++q) {
+      colidx[o + q] = cols[q];
+      vals[o + q] = acc[q];
+    }
+  }
+}
+
+bool ham_lower_pull(qd_ham* H) {
+  std::vector<MfEntry> off, dia;
+  try {
+    compile_terms(H, off, dia);
+  } catch (const Error&) {
+    clear_error();
+    return false;
+  }
+  off.insert(off.end(), dia.begin(), dia.end());
+  if (off.size() > 4096) return false;
+  Ctx* ctx = H->ctx;
+  const qd_sector* S = H->sec;
+  const int64_t dim = S->view.dim;
+  DBuf<MfEntry> dent(std::max<size_t>(off.size(), 1));
+  if (!off.empty())
+    QD_CUDA(cudaMemcpyAsync(dent.p, off.data(), off.size() * sizeof(MfEntry), cudaMemcpyHostToDevice, ctx->stream));
+  PullArgs A;
+  std::memset(&A, 0, sizeof(A));
+  A.dim = dim;
+  A.basis = S->basis.p;
+  A.ent = dent.p;
+  A.nent = (int)off.size();
+  A.S = S->view;
+  A.use_tables = (S->view.rank_kind == 1 && S->view.nfields <= 4) ? 1 : 0;
+  DBuf<int64_t> tab;
+  if (A.use_tables) {
+    std::vector<int64_t> ht;
+    build_tables(S, A.rk, ht);
+    tab.alloc(std::max<size_t>(ht.size(), 1));
+    if (!ht.empty())
+      QD_CUDA(cudaMemcpyAsync(tab.p, ht.data(), ht.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    A.rk.tab = tab.p;
+  }
+  DBuf<int> overflow(1);
+  QD_CUDA(cudaMemsetAsync(overflow.p, 0, sizeof(int), ctx->stream));
+  DBuf<int64_t> rowptr(dim + 2);
+  QD_CUDA(cudaMemsetAsync(rowptr.p, 0, (dim + 2) * 8, ctx->stream));
+  const unsigned g = (unsigned)std::max<int64_t>(1, ceil_div(dim, 128));
+  if (dim > 0) {
+    pull_lower_kernel<<<g, 128, 0, ctx->stream>>>(A, 0, rowptr.p, nullptr, nullptr, nullptr, overflow.p);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+  }
+  int ovf = 0;
+  QD_CUDA(cudaMemcpyAsync(&ovf, overflow.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (ovf) return false;
+  exclusive_scan_i64(ctx, rowptr.p, rowptr.p, dim + 1);
+  int64_t nnz = 0;
+  QD_CUDA(cudaMemcpyAsync(&nnz, rowptr.p + dim, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  QD_REQUIRE(nnz < (int64_t)INT32_MAX * 8, QD_ERR_UNSUPPORTED, "nnz too large");
+  H->nnz = nnz;
+  H->rowptr = std::move(rowptr);
+  H->colidx.alloc(nnz + 16);
+  H->vals_c.alloc(nnz + 16);
+  QD_CUDA(cudaMemsetAsync(H->colidx.p, 0, (nnz + 16) * sizeof(int32_t), ctx->stream));
+  QD_CUDA(cudaMemsetAsync(H->vals_c.p, 0, (nnz + 16) * sizeof(cplx), ctx->stream));
+  if (dim > 0 && nnz > 0) {
+    pull_lower_kernel<<<g, 128, 0, ctx->stream>>>(A, 1, nullptr, H->rowptr.p, H->colidx.p, H->vals_c.p, overflow.p);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+  }
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  return true;
+}
 
 void mf_apply_c(qd_ham* H, const cplx* x, cplx* y) {
   ham_build_matrix_free(H);

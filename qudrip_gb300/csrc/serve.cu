@@ -314,8 +314,23 @@ static void run_single(qd_server* S, Lane* L, ServeReq* r, Built* prebuilt) {
       const bool fast = (S->o.mode == QD_SERVE_MIXED) && (H->flags & QD_HAM_HERMITIAN);
       int act = 0;
       if (fast) {
+        // Integrate to T = nsteps * dt with the mixed form's own Krylov step:
+        // m = 32 and h = T / n with n = ceil(T ||H||_inf / 8), so that
+        // ||H h|| <= 8 = m / 4 and the Krylov error bound (e ||Hh|| / 2m)^m
+        // stays below 1e-15 per step; the requested (dt, m) is kept when it is
+        // the coarser of the two.
+        const double T = r->d.dt * r->d.nsteps;
+        const double hn = ham_norm_inf(H);
+        int nint = std::max(1, (int)std::ceil(std::fabs(T) * hn / 8.0));
+        double h = r->d.dt;
+        int m = r->d.krylov_dim, steps = r->d.nsteps;
+        if (nint < r->d.nsteps && std::isfinite(hn)) {
+          h = T / nint;
+          m = 32;
+          steps = nint;
+        }
         int64_t mv = 0;
-        lanczos_evolve(H, psi.p, psi.p, r->d.dt, r->d.krylov_dim, r->d.nsteps, &act, &mv);
+        lanczos_evolve(H, psi.p, psi.p, h, m, steps, &act, &mv);
         res.matvecs += mv;
       } else {
         for (int s = 0; s < r->d.nsteps; ++s) {

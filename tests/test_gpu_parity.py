@@ -86,8 +86,11 @@ def test_sector_kinds(ctx):
     assert empty.dim == 0
 
 
+@pytest.mark.parametrize("path", ["rows", "tree"])
 @pytest.mark.parametrize("name", sorted(SYSTEMS))
-def test_lowering_bit_exact(ctx, name):
+def test_lowering_bit_exact(ctx, name, path, monkeypatch):
+    if path == "tree":  # the per-column tree walk instead of the compiled row-wise pull
+        monkeypatch.setenv("QD_LOWER_TREE", "1")
     spec, ham = SYSTEMS[name]()
     osec = O.Sector(spec)
     oh = O.Ham(osec, ham)
