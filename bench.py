@@ -540,10 +540,10 @@ def serving_requests(n_req, rate, seed):
     return reqs
 
 
-def serve_stream(mode, reqs):
+def serve_stream(mode, reqs, **opts):
     """Submits `reqs` at their arrival times; returns results by request index."""
     import qudrip_gb300 as q
-    srv = q.Server(mode=mode)
+    srv = q.Server(mode=mode, **opts)
     try:
         # warm-up: one request of each kind and size class
         warm = [srv.submit_ground(r["spec"], r["ham"], 100, seed=1) for r in reqs[:4]]
@@ -572,14 +572,14 @@ def serve_stream(mode, reqs):
     return out, st
 
 
-def serving_mix(n_req=400, rate=200.0, seed=77):
+def serving_mix(n_req=400, rate=200.0, seed=77, **opts):
     reqs = serving_requests(n_req, rate, seed)
     summary = {"workload": f"Poisson {rate:.0f} req/s, {n_req} requests: 70% ground state (Lanczos k=100), "
                            "30% evolution (T=5, dt=0.05, m=16); XXZ L in {12..22} Sz=0, Jz~U[0,2], "
                            "fields h_i~U[-1,1] on half"}
     results = {}
     for mode in ("mixed", "plain"):
-        out, st = serve_stream(mode, reqs)
+        out, st = serve_stream(mode, reqs, **opts)
         lat = np.array([out[i]["t_done"] - out[i]["t_submit"] for i in range(n_req)])
         t_first = min(out[i]["t_submit"] for i in range(n_req))
         t_last = max(out[i]["t_done"] for i in range(n_req))

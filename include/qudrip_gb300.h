@@ -438,7 +438,7 @@ typedef struct qd_server_opts {
   int32_t reserved0;
   int64_t small_dim;    /* default 65536 */
   int64_t hbm_budget;   /* bytes admitted requests may hold; 0 = 80% of free memory */
-  int64_t batch_dim;    /* QD_SERVE_MIXED: ground states with dim <= batch_dim are batched (default 16384) */
+  int64_t batch_dim;    /* QD_SERVE_MIXED: ground states with dim <= batch_dim are batched (default 3432) */
   int32_t reserved[2];
 } qd_server_opts;
 

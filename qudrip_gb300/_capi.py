@@ -36,6 +36,7 @@ QD_SPMV_CSR = 0
 QD_SPMV_MATRIX_FREE = 1
 QD_RITZ_STORED_BASIS = 0
 QD_RITZ_SECOND_PASS = 1
+QD_SPMV_FX = 120  # uniform-coupling form with exact fixed-point row sums
 SPMV_KERNELS = {100: "tile", 101: "balanced", 102: "vector2", 103: "vector4", 104: "vector8",
                 105: "scalar", 106: "row4", 107: "row8", 108: "row4_stream", 109: "row8_stream",
                 110: "row_exact", 111: "row_sorted"}

@@ -159,7 +159,9 @@ __global__ void __launch_bounds__(256) spmv_fx_kernel(int64_t n, const int32_t* 
 // them.  V1[r] is already loaded for the diagonal term and the FP64 pipe is
 // idle while the fixed-point gathers run, so the dots cost one extra 8-byte
 // read per row.  Grid-stride rows on a resident grid, one block reduction per
-// block, two-level grid reduction of the three sums.
+// block, two-level grid reduction of the three sums.  Everything but the
+// gathered fixed-point vector is loaded and stored with evict-first hints so
+// that the 16-byte-per-row vector X stays in L2 for the gathers.
 template <bool kHas2>
 __global__ void __launch_bounds__(256) spmv_fx_dots_kernel(
     int64_t n, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colidx,
@@ -174,7 +176,7 @@ __global__ void __launch_bounds__(256) spmv_fx_dots_kernel(
   Tri<double> acc = vzero(Tri<double>{});
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-    const int b = __ldg(rowptr + r), e = __ldg(rowptr + r + 1);
+    const int b = __ldcs(rowptr + r), e = __ldcs(rowptr + r + 1);
     __int128 s = 0;
     int k = b;
     for (; k + 4 <= e; k += 4) {
@@ -184,12 +186,12 @@ __global__ void __launch_bounds__(256) spmv_fx_dots_kernel(
       s += (x0 + x1) + (x2 + x3);
     }
     for (; k < e; ++k) s += X[__ldcs(colidx + k)];
-    const double xr = __ldg(x + r);
+    const double xr = __ldcs(x + r);
     const double w = sc * fma(cF, (double)s, __ldcs(diag + r) * xr);
-    y[r] = w;
+    __stcs(y + r, w);
     acc.b = fma(xr, w, acc.b);
     if (kHas2) {
-      const double v2 = __ldg(V2 + r);
+      const double v2 = __ldcs(V2 + r);
       acc.a = fma(v2, w, acc.a);
       acc.c = fma(xr, v2, acc.c);
     }

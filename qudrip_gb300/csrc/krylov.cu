@@ -66,6 +66,7 @@ struct LzPack<double> {
   __device__ static T load(const double* p, int64_t i) { return reinterpret_cast<const double2*>(p)[i]; }
   __device__ static T load_last(const double* p, int64_t i) { return __ldcs(reinterpret_cast<const double2*>(p) + i); }
   __device__ static void store(double* p, int64_t i, T v) { reinterpret_cast<double2*>(p)[i] = v; }
+  __device__ static void store_stream(double* p, int64_t i, T v) { __stcs(reinterpret_cast<double2*>(p) + i, v); }
   __device__ static double dot(T a, T b, double acc) { return fma(a.y, b.y, fma(a.x, b.x, acc)); }
   __device__ static double nrm(T a, double acc) { return fma(a.y, a.y, fma(a.x, a.x, acc)); }
   __device__ static T submul(T x, double a, T y) { return make_double2(fma(-a, y.x, x.x), fma(-a, y.y, x.y)); }
@@ -84,6 +85,7 @@ struct LzPack<cplx> {
     return mkc(d.x, d.y);
   }
   __device__ static void store(cplx* p, int64_t i, T v) { p[i] = v; }
+  __device__ static void store_stream(cplx* p, int64_t i, T v) { p[i] = v; }
   __device__ static cplx dot(T a, T b, cplx acc) { return vdotfma(a, b, acc); }
   __device__ static double nrm(T a, double acc) { return acc + vnorm2(a); }
   __device__ static T submul(T x, cplx a, T y) { return vsubmul(x, a, y); }
@@ -175,11 +177,14 @@ __global__ void __launch_bounds__(kLzThreads, kLzBlocksPerSm)
     }
     o0 = P::submul(o0, a, a0);
     o1 = P::submul(o1, a, a1);
-    P::store(Vk, p, o0);
-    P::store(Vk, p + stride, o1);
-    if (Xk) {
+    if (Xk) {  // the next product gathers X, not v_k: keep X in L2
+      P::store_stream(Vk, p, o0);
+      P::store_stream(Vk, p + stride, o1);
       P::shadow(Xk, p, o0, F, ovf);
       P::shadow(Xk, p + stride, o1, F, ovf);
+    } else {
+      P::store(Vk, p, o0);
+      P::store(Vk, p + stride, o1);
     }
     acc0 = P::nrm(o0, acc0);
     acc1 = P::nrm(o1, acc1);

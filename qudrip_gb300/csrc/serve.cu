@@ -495,7 +495,7 @@ qd_status qd_server_create(qd_ctx* ctx_, const qd_server_opts* opts, qd_server**
     if (o.mode == QD_SERVE_PLAIN) o.batch_lanes = 0;
     if (o.batch_max <= 0) o.batch_max = 64;
     if (o.small_dim <= 0) o.small_dim = 65536;
-    if (o.batch_dim <= 0) o.batch_dim = 16384;
+    if (o.batch_dim <= 0) o.batch_dim = 3432;
     QD_REQUIRE(o.small_lanes + o.large_lanes + o.batch_lanes <= 64, QD_ERR_INVALID, "at most 64 lanes");
     if (o.hbm_budget <= 0) {
       size_t fr = 0, tot = 0;

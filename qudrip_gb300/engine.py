@@ -447,7 +447,7 @@ class Server:
     """
 
     def __init__(self, mode: str = "mixed", small_lanes: int = 4, large_lanes: int = 3, batch_lanes: int = 2,
-                 batch_max: int = 64, small_dim: int = 65536, hbm_budget: int = 0, batch_dim: int = 16384,
+                 batch_max: int = 64, small_dim: int = 65536, hbm_budget: int = 0, batch_dim: int = 3432,
                  ctx: Optional[Context] = None):
         self.ctx = ctx or default_context()
         o = A.qd_server_opts()

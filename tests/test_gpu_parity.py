@@ -277,4 +277,5 @@ def test_every_product_kernel(ctx, name):
     chosen = C.c_int(0)
     ms = C.c_double(0)
     A.call("qd_ham_autotune", gh.handle, 3, C.byref(chosen), C.byref(ms))
-    assert chosen.value in A.SPMV_KERNELS and ms.value > 0
+    # 120 (the uniform-coupling fixed-point form) competes where it applies
+    assert (chosen.value in A.SPMV_KERNELS or chosen.value == A.QD_SPMV_FX) and ms.value > 0
