@@ -98,6 +98,7 @@ struct qd_ham {
   qd::DBuf<double> diag_r;   // real diagonal (mf_real)
   qd::DBuf<cplx> diag_c;     // complex diagonal
   qd::DBuf<int64_t> mf_tab;
+  qd::DBuf<uint32_t> mf_tab32;  // the tables in 32 bits (registers of at most 32 bits)
   qd::MfRank mf_rank{};
   std::vector<qd_term> host_terms;
   std::vector<qd_gate> host_gates;

@@ -450,8 +450,10 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
 
 // ---------------------------------------------------------------- Lanczos
 template <typename MV, typename VV>
+// fxk: 0 the product alone (CSR or matrix-free), then K2; 1 the uniform-
+// coupling form with fixed-point sums fused with the step's inner products.
 static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int kdim, Workspace& W, bool mf,
-                        bool fx = false) {
+                        int fxk = 0) {
   Ctx* ctx = H->ctx;
   const int64_t n = H->dim;
   for (int k = 1; k <= kdim; ++k) {
@@ -461,22 +463,24 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int kd
     const double* s1 = B.scl.p + (k - 1);
     const double* s2 = (k >= 2) ? B.scl.p + (k - 2) : nullptr;
     // K1: w = s1 * H V1 (CSR, fixed-point uniform-coupling form, or matrix-free)
-    __int128* Xprev = fx ? B.X.p + (int64_t)((k - 1) & 1) * B.ld : nullptr;
-    __int128* Xnext = fx ? B.X.p + (int64_t)(k & 1) * B.ld : nullptr;
+    __int128* Xprev = (fxk == 1) ? B.X.p + (int64_t)((k - 1) & 1) * B.ld : nullptr;
+    __int128* Xnext = (fxk == 1) ? B.X.p + (int64_t)(k & 1) * B.ld : nullptr;
     if constexpr (std::is_same<VV, double>::value) {  // product fused with the step's inner products
-      if (fx)
+      if (fxk == 1)
         launch_fx_dots(ctx, H, V1, Xprev, V2, B.w.p, s1, s2, B.stop.p, k, B.beta.p + k, B.alpha.p + k, B.dots.p + k,
                        W.red_tri<double>(2));
     }
-    if (mf)
-      launch_mf<VV>(ctx, H, V1, B.w.p, 1.0, s1, B.stop.p, k);
-    else if (!fx)
-      launch_spmv<MV, VV>(ctx, H, vals, V1, B.w.p, 1.0, nullptr, W.red_c_or_d<VV>(1), nullptr, B.stop.p, k, -1, s1,
-                          nullptr);
+    if (fxk == 0) {
+      if (mf)
+        launch_mf<VV>(ctx, H, V1, B.w.p, 1.0, s1, B.stop.p, k);
+      else
+        launch_spmv<MV, VV>(ctx, H, vals, V1, B.w.p, 1.0, nullptr, W.red_c_or_d<VV>(1), nullptr, B.stop.p, k, -1,
+                            s1, nullptr);
+    }
     // K2, K3 (K3 also writes the fixed-point copy of v_k for the next product)
     lz_vector_passes<VV>(ctx, n, B.stop.p, k, B.w.p, V1, V2, s1, s2, B.beta.p + k, B.alpha.p + k, B.dots.p + k, Vk,
                          B.nrm2.p + k, B.nrm.p + k, B.scl.p + k, W.red_tri<VV>(2), W.red_d(3), Xnext,
-                         fx ? H->fx->F : 0, fx ? B.ovf.p : nullptr, fx);
+                         fxk == 1 ? H->fx->F : 0, fxk == 1 ? B.ovf.p : nullptr, fxk != 0);
   }
 }
 
@@ -517,9 +521,13 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
   const auto host_t0 = std::chrono::steady_clock::now();
   if (timing) QD_CUDA(cudaEventRecord(ctx->events[12], ctx->stream));
   const bool mf = (o.spmv == QD_SPMV_MATRIX_FREE);
-  bool fx = false;
-  if constexpr (std::is_same<VV, double>::value) fx = !mf && H->fx_allowed && ham_build_fx(H);
-  const int kind = mf ? 1 : (fx ? 2 : 0);
+  int fxk = 0;  // 1: the fixed-point uniform-coupling CSR form fused with the dots (fxsum.cuh)
+  if constexpr (std::is_same<VV, double>::value) {
+    if (!mf && H->fx_allowed && ham_build_fx(H)) fxk = 1;
+  }
+  const bool fx = fxk == 1;
+  const int fxF = fx ? H->fx->F : 0;
+  const int kind = (mf ? 1 : 0) + 2 * fxk;
   if (B.kind != kind) {
     B.drop_graph();
     B.kind = kind;
@@ -527,9 +535,9 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
   if (fx) {
     B.ensure_fx();
     QD_CUDA(cudaMemsetAsync(B.ovf.p, 0, sizeof(int), ctx->stream));
-    if constexpr (std::is_same<VV, double>::value) launch_fx_shadow(ctx, n, B.V.p, B.X.p, H->fx->F, B.ovf.p);
+    if constexpr (std::is_same<VV, double>::value) launch_fx_shadow(ctx, n, B.V.p, B.X.p, fxF, B.ovf.p);
   }
-  B.run_graph(ctx, [&]() { lanczos_run<MV, VV>(H, vals, B, kdim, W, mf, fx); });
+  B.run_graph(ctx, [&]() { lanczos_run<MV, VV>(H, vals, B, kdim, W, mf, fxk); });
   if (fx) {
     int ov = 0;
     QD_CUDA(cudaMemcpyAsync(&ov, B.ovf.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -572,9 +580,9 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
     QD_CUDA(cudaMemsetAsync(B.stop.p, 0, sizeof(int), ctx->stream));
     if (fx) {
       QD_CUDA(cudaMemsetAsync(B.ovf.p, 0, sizeof(int), ctx->stream));
-      if constexpr (std::is_same<VV, double>::value) launch_fx_shadow(ctx, n, B.V.p, B.X.p, H->fx->F, B.ovf.p);
+      if constexpr (std::is_same<VV, double>::value) launch_fx_shadow(ctx, n, B.V.p, B.X.p, fxF, B.ovf.p);
     }
-    lanczos_run<MV, VV>(H, vals, B, act, W, mf, fx);
+    lanczos_run<MV, VV>(H, vals, B, act, W, mf, fxk);
     matvecs += act;
   }
   // psi = sum_k y_k v_k = sum_k (y_k s_k) V[k]

@@ -22,6 +22,7 @@
 // search).  The amplitudes keep the JW sign of the bits outside the support
 // apart (the parity of c & jw), which multiplies exactly.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -358,12 +359,125 @@ void ham_build_matrix_free(qd_ham* H) {
     if (!tab.empty())
       QD_CUDA(cudaMemcpyAsync(H->mf_tab.p, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
     H->mf_rank.tab = H->mf_tab.p;
+    if (S->view.nbits <= 32 && n < (1ll << 31)) {  // 32-bit copy for the 32-bit product
+      std::vector<uint32_t> t32(std::max<size_t>(tab.size(), 1), 0u);
+      for (size_t i = 0; i < tab.size(); ++i) t32[i] = (uint32_t)tab[i];
+      H->mf_tab32.alloc(t32.size());
+      QD_CUDA(cudaMemcpyAsync(H->mf_tab32.p, t32.data(), t32.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    }
   }
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
   H->mf_real = real && !has_im;
   if (H->mf_real) H->diag_c = DBuf<cplx>();
   else H->diag_r = DBuf<double>();
   H->has_mf = true;
+}
+
+// 32-bit form of the product for registers of at most 32 bits ranked by
+// tables (every model of the configurations): states, masks and table entries
+// in 32-bit integers, the fields unrolled, so a row costs about half the
+// integer instructions of the 64-bit form.
+struct Mf32 {
+  int nf;
+  int lo[2], k[2], nb[2];
+  uint32_t wmask[2];
+  uint32_t stride[2];
+  int off[2];
+  const uint32_t* tab;
+};
+
+template <typename AV, typename VV, int NF>
+__global__ void __launch_bounds__(256) mf_spmv32_kernel(int64_t dim, const uint64_t* __restrict__ basis,
+                                                        const AV* __restrict__ diag, const MfEntry* __restrict__ ent,
+                                                        int nent, Mf32 R, const VV* __restrict__ x, VV* __restrict__ y,
+                                                        double scale, const double* scale_dev, const int* stop,
+                                                        int step) {
+  extern __shared__ __align__(16) unsigned char mf_smem32[];
+  uint32_t* s_sup = reinterpret_cast<uint32_t*>(mf_smem32);
+  uint32_t* s_out = s_sup + nent;
+  uint32_t* s_flip = s_out + nent;
+  uint32_t* s_jw = s_flip + nent;
+  AV* s_amp = reinterpret_cast<AV*>(mf_smem32 + (((size_t)4 * nent * sizeof(uint32_t) + 15) & ~(size_t)15));
+  if (stop) {
+    const int st = *stop;
+    if (st != 0 && st < step) return;
+  }
+  for (int e = threadIdx.x; e < nent; e += blockDim.x) {
+    const MfEntry E = ent[e];
+    s_sup[e] = (uint32_t)E.sup;
+    s_out[e] = (uint32_t)E.outb;
+    s_flip[e] = (uint32_t)E.flip;
+    s_jw[e] = (uint32_t)E.jw;
+    s_amp[e] = amp_of((AV*)nullptr, E.amp);
+  }
+  __syncthreads();
+  const double sc = scale_dev ? *scale_dev : scale;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < dim; r += stride) {
+    const uint32_t s = (uint32_t)__ldg(basis + r);
+    VV acc = vfma(diag[r], x[r], vzero(VV{}));
+    for (int e0 = 0; e0 < nent; e0 += 32) {
+      const int ne = min(32, nent - e0);
+      unsigned mask = 0;
+      for (int q = 0; q < ne; ++q) mask |= (unsigned)((s & s_sup[e0 + q]) == s_out[e0 + q]) << q;
+      while (mask) {
+        const int e = e0 + __ffs(mask) - 1;
+        mask &= mask - 1;
+        const uint32_t c = s ^ s_flip[e];
+        uint32_t col = 0;
+        bool in = true;
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          const uint32_t v = (c >> R.lo[f]) & R.wmask[f];
+          in &= (__popc(v) == R.k[f]);
+          const uint32_t* T = R.tab + R.off[f];
+          const int kk = R.k[f] + 1;
+          uint32_t a = __ldg(T + (v & 255u) * kk);
+          int cb = __popc(v & 255u);
+          if (R.nb[f] > 1) {
+            a += __ldg(T + (256u + ((v >> 8) & 255u)) * kk + cb);
+            cb += __popc((v >> 8) & 255u);
+          }
+          if (R.nb[f] > 2) {
+            a += __ldg(T + (512u + ((v >> 16) & 255u)) * kk + cb);
+            cb += __popc((v >> 16) & 255u);
+          }
+          if (R.nb[f] > 3) a += __ldg(T + (768u + (v >> 24)) * kk + cb);
+          col += a * R.stride[f];
+        }
+        if (!in) continue;
+        AV a = s_amp[e];
+        if (__popc(c & s_jw[e]) & 1) a = vneg(a);
+        acc = vfma(a, ld_ro(x + col), acc);
+      }
+    }
+    y[r] = vscale(sc, acc);
+  }
+}
+
+// Builds the 32-bit form when the register has at most 32 bits, the sector is
+// a product of at most two fields and the dimension fits in 32 bits.
+static bool mf32_prepare(qd_ham* H, Mf32& R) {
+  const SectorView& V = H->sec->view;
+  if (!H->mf_tables || V.nbits > 32 || H->dim >= (1ll << 31)) return false;
+  int nf = 0;
+  for (int f = 0; f < V.nfields; ++f)
+    if (!V.fields[f].is_free) ++nf;
+  if (nf != V.nfields || nf < 1 || nf > 2) return false;
+  if (!H->mf_tab32.p) return false;  // built with the tables (ham_build_matrix_free)
+  std::memset(&R, 0, sizeof(R));
+  R.nf = nf;
+  for (int f = 0; f < nf; ++f) {
+    const Field& F = V.fields[f];
+    R.lo[f] = F.lo;
+    R.k[f] = F.k;
+    R.nb[f] = H->mf_rank.nb[f];
+    R.wmask[f] = (F.width >= 32) ? 0xffffffffu : ((1u << F.width) - 1u);
+    R.stride[f] = (uint32_t)F.stride;
+    R.off[f] = (int)H->mf_rank.off[f];
+  }
+  R.tab = H->mf_tab32.p;
+  return true;
 }
 
 template <typename AV, typename VV>
@@ -385,6 +499,20 @@ static void launch_mf_typed(Ctx* ctx, qd_ham* H, const AV* diag, const VV* x, VV
   A.scale_dev = scale_dev;
   A.stop = stop;
   A.step = step;
+  Mf32 R;
+  if (mf32_prepare(H, R)) {
+    const int ne = std::max(H->mf_nent, 1);
+    const size_t smem32 = (((size_t)4 * ne * sizeof(uint32_t) + 15) & ~(size_t)15) + (size_t)ne * sizeof(AV);
+    if (R.nf == 1)
+      mf_spmv32_kernel<AV, VV, 1><<<mf_grid(ctx, H->dim), 256, smem32, ctx->stream>>>(
+          H->dim, H->sec->basis.p, diag, H->mf_ent.p, H->mf_nent, R, x, y, scale, scale_dev, stop, step);
+    else
+      mf_spmv32_kernel<AV, VV, 2><<<mf_grid(ctx, H->dim), 256, smem32, ctx->stream>>>(
+          H->dim, H->sec->basis.p, diag, H->mf_ent.p, H->mf_nent, R, x, y, scale, scale_dev, stop, step);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+    return;
+  }
   const size_t smem = (size_t)std::max(H->mf_nent, 1) * (4 * sizeof(uint64_t) + sizeof(AV));
   mf_spmv_kernel<AV, VV><<<mf_grid(ctx, H->dim), 256, smem, ctx->stream>>>(A);
   QD_CHECK_LAUNCH();
