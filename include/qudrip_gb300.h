@@ -208,6 +208,11 @@ qd_status qd_ham_apply(qd_ham *ham, qd_state *x, int t_in, qd_state *y,
 /* psi(:,t)^dagger * H * psi(:,t), unnormalised, as State::eval
  * (state.hpp:33-45). */
 qd_status qd_state_eval(qd_state *psi, int t, qd_ham *ham, double *re_im);
+/* <psi(:,t)|O_i|psi(:,t)> for nobs operators of psi's sector and context
+ * (replaces the loop of McManager::incrAllObs, mc_manager.hpp:88-106):
+ * re_im receives 2*nobs doubles; the fused products run back to back with
+ * one copy of the results. */
+qd_status qd_obs_eval(qd_state *psi, int t, int nobs, qd_ham *const *obs, double *re_im);
 
 /* ------------------------------------------------------------------ */
 /* Lanczos ground state                                               */

@@ -27,6 +27,7 @@
 #include <complex>
 #include <cstdint>
 #include <fstream>
+#include <map>
 #include <memory>
 #include <random>
 #include <stdexcept>
@@ -455,6 +456,60 @@ inline void shuffle_state(State& psi, uint64_t seed = 12345) {
   for (auto& x : v) x /= std::sqrt(n2);
   psi.set(v);
 }
+
+// ------------------------------------------------------------------ observables
+// McManager (mc_manager.hpp:14-214) without MPI: named groups of `dim`
+// operators with an (nt x dim) table each; incrAllObs evaluates every
+// operator on psi(psi_tstp) in one qd_obs_eval pass and adds into row tstp.
+class McManager {
+ public:
+  McManager(int nt, State* p_psi) : nt_(nt), p_psi_(p_psi), Nmc_((size_t)nt, 0) {}
+  explicit McManager(State* p_psi) : McManager(p_psi->nt(), p_psi) {}
+
+  void addObs(const std::string& name, int dim) {
+    data_[name] = std::vector<value_type>((size_t)nt_ * dim, value_type(0.0, 0.0));
+    dims_[name] = dim;
+    obs_[name] = std::vector<SpMatrix>((size_t)dim);
+  }
+  void updateMatrix(const std::string& name, int idx, const SpMatrix& mat) { obs_.at(name).at((size_t)idx) = mat; }
+  SpMatrix& matrix(const std::string& name, int idx) { return obs_.at(name).at((size_t)idx); }
+
+  void incrAllObs(int tstp, int psi_tstp = -1) {
+    if (psi_tstp == -1) psi_tstp = tstp;
+    std::vector<qd_ham*> hs;
+    std::vector<value_type*> dst;
+    for (auto& o : obs_)
+      for (size_t d = 0; d < o.second.size(); ++d) {
+        hs.push_back(o.second[d].handle());
+        dst.push_back(&data_[o.first][(size_t)tstp * dims_[o.first] + d]);
+      }
+    if (!hs.empty()) {
+      std::vector<double> v(2 * hs.size());
+      check(qd_obs_eval(p_psi_->handle(), psi_tstp, (int)hs.size(), hs.data(), v.data()), "incrAllObs");
+      for (size_t i = 0; i < hs.size(); ++i) *dst[i] += value_type(v[2 * i], v[2 * i + 1]);
+    }
+    ++Nmc_[(size_t)tstp];
+  }
+  void normAll() {
+    for (auto& d : data_)
+      for (int t = 0; t < nt_; ++t)
+        for (int k = 0; k < dims_[d.first]; ++k) d.second[(size_t)t * dims_[d.first] + k] *= 1.0 / Nmc_[(size_t)t];
+  }
+  void clearAll() {
+    for (auto& d : data_) std::fill(d.second.begin(), d.second.end(), value_type(0.0, 0.0));
+  }
+  value_type value(const std::string& name, int t, int d) const {
+    return data_.at(name).at((size_t)t * dims_.at(name) + d);
+  }
+
+ private:
+  int nt_;
+  State* p_psi_;
+  std::vector<int> Nmc_;
+  std::map<std::string, std::vector<value_type>> data_;
+  std::map<std::string, int> dims_;
+  std::map<std::string, std::vector<SpMatrix>> obs_;
+};
 
 // ------------------------------------------------------------------ solvers
 namespace Arnoldi {

@@ -11,5 +11,5 @@ from .operators import (II, id, pauli_x, pauli_y, pauli_z, getQbits, getNset, ge
 from .engine import (Context, default_context, Sector, Constrain, LooseConstrain, Hamiltonian,  # noqa: F401
                      State, getState, apply, start_vector, shuffle_state, LanczosSolver, ArnoldiSolver, Arnoldi,
                      batch_lanczos, traj_run, lanczos_evolve, seeded_start, Server, Hermitian,
-                     HermitianLanczosSolver)
+                     HermitianLanczosSolver, obs_eval, McManager)
 from . import _capi  # noqa: F401

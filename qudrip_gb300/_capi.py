@@ -183,6 +183,7 @@ _SIGNATURES = {
     "qd_state_copy": [_P, C.c_int, _P, C.c_int],
     "qd_ham_apply": [_P, _P, C.c_int, _P, C.c_int],
     "qd_state_eval": [_P, C.c_int, _P, _DP],
+    "qd_obs_eval": [_P, C.c_int, C.c_int, C.POINTER(C.c_void_p), _DP],
     "qd_lanczos_ground": [_P, _P, C.c_int, C.POINTER(qd_lanczos_opts), _DP,
                           C.POINTER(qd_lanczos_result)],
     "qd_hermitian_lanczos_ground": [_P, _P, C.c_int, C.c_int, _DP, C.POINTER(qd_lanczos_result)],

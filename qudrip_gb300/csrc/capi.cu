@@ -424,6 +424,17 @@ qd_status qd_state_eval(qd_state* psi, int t, qd_ham* ham, double* re_im) {
   });
 }
 
+qd_status qd_obs_eval(qd_state* psi, int t, int nobs, qd_ham* const* obs, double* re_im) {
+  return guard([&] {
+    QD_REQUIRE(psi && obs && re_im && nobs >= 1 && t >= 0 && t < psi->nt, QD_ERR_INVALID, "bad argument");
+    for (int i = 0; i < nobs; ++i)
+      QD_REQUIRE(obs[i] && obs[i]->dim == psi->dim && obs[i]->ctx == psi->ctx, QD_ERR_INVALID,
+                 "observable %d: null, other dimension or other context", i);
+    DeviceGuard dg(psi->ctx->device);
+    obs_eval_many(obs, nobs, psi->col(t), reinterpret_cast<cplx*>(re_im));
+  });
+}
+
 // ------------------------------------------------------------------ Lanczos
 qd_status qd_lanczos_ground(qd_ham* ham, qd_state* psi, int t, const qd_lanczos_opts* opts, double* evals_out,
                             qd_lanczos_result* res) {

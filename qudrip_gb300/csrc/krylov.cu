@@ -310,6 +310,11 @@ Workspace::Workspace(Ctx* c) : ctx(c) {
 GridRed<double> Workspace::red_d(int slot) {
   return GridRed<double>{partials_d.p, tickets.p + (size_t)slot * (1 + kRedMaxGroups), gpart_d.p};
 }
+// One-level form (the last block adds every block partial): for grids of a
+// few hundred blocks it saves a fence-and-ticket round on the critical tail.
+GridRed<double> Workspace::red_d_flat(int slot) {
+  return GridRed<double>{partials_d.p, tickets.p + (size_t)slot * (1 + kRedMaxGroups), nullptr};
+}
 GridRed<cplx> Workspace::red_c(int slot) {
   return GridRed<cplx>{partials_c.p, tickets.p + (size_t)slot * (1 + kRedMaxGroups), gpart_c.p};
 }
@@ -342,6 +347,27 @@ cplx state_eval(qd_ham* H, const cplx* psi) {
   QD_CUDA(cudaMemcpyAsync(&h, out.p, sizeof(cplx), cudaMemcpyDeviceToHost, ctx->stream));
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
   return h;
+}
+
+// <psi|O_i|psi> for a list of operators (McManager::incrAllObs,
+// mc_manager.hpp:88-106): every product is fused with its inner product and
+// the launches go back to back on one stream, with one copy of all results.
+void obs_eval_many(qd_ham* const* obs, int nobs, const cplx* psi, cplx* out_host) {
+  Ctx* ctx = obs[0]->ctx;
+  const int64_t n = obs[0]->dim;
+  DBuf<cplx> tmp(n + 1);
+  DBuf<cplx> out(nobs);
+  for (int i = 0; i < nobs; ++i) {
+    qd_ham* H = obs[i];
+    QD_REQUIRE(H->ctx == ctx && H->dim == n, QD_ERR_INVALID, "observable %d: other context or dimension", i);
+    Workspace& W = ham_workspace(H);
+    if (H->flags & QD_HAM_REAL)
+      launch_spmv<double, cplx>(ctx, H, H->vals_r.p, psi, tmp.p, 1.0, psi, W.red_c(0), out.p + i, nullptr, 0, -1);
+    else
+      launch_spmv<cplx, cplx>(ctx, H, H->vals_c.p, psi, tmp.p, 1.0, psi, W.red_c(0), out.p + i, nullptr, 0, -1);
+  }
+  QD_CUDA(cudaMemcpyAsync(out_host, out.p, nobs * sizeof(cplx), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
 // ||psi||^2 on the Hamiltonian's stream.
@@ -479,7 +505,7 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int kd
     }
     // K2, K3 (K3 also writes the fixed-point copy of v_k for the next product)
     lz_vector_passes<VV>(ctx, n, B.stop.p, k, B.w.p, V1, V2, s1, s2, B.beta.p + k, B.alpha.p + k, B.dots.p + k, Vk,
-                         B.nrm2.p + k, B.nrm.p + k, B.scl.p + k, W.red_tri<VV>(2), W.red_d(3), Xnext,
+                         B.nrm2.p + k, B.nrm.p + k, B.scl.p + k, W.red_tri<VV>(2), W.red_d_flat(3), Xnext,
                          fxk == 1 ? H->fx->F : 0, fxk == 1 ? B.ovf.p : nullptr, fxk != 0);
   }
 }

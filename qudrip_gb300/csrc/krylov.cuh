@@ -105,6 +105,7 @@ struct Workspace {
 
   explicit Workspace(Ctx* c);
   GridRed<double> red_d(int slot);
+  GridRed<double> red_d_flat(int slot);
   GridRed<cplx> red_c(int slot);
   template <typename VV>
   GridRed<Tri<VV>> red_tri(int slot) {
@@ -123,6 +124,7 @@ Workspace& ham_workspace(qd_ham* H);
 void ham_apply_c(qd_ham* H, const cplx* x, cplx* y);
 cplx state_eval(qd_ham* H, const cplx* psi);
 double state_norm2(qd_ham* H, const cplx* psi);
+void obs_eval_many(qd_ham* const* obs, int nobs, const cplx* psi, cplx* out_host);
 void lanczos_ground(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, double* evals_out, qd_lanczos_result* res);
 void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per_launch);
 void lanczos_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int m, int nsteps, int* act_out,

@@ -430,6 +430,77 @@ def lanczos_evolve(H: Hamiltonian, psi: State, t_in: int, t_out: int, h: float, 
     return act.value
 
 
+def obs_eval(psi: State, t: int, observables) -> np.ndarray:
+    """<psi(t)|O_i|psi(t)> for a list of lowered operators, one device pass each, one copy back."""
+    n = len(observables)
+    hp = (C.c_void_p * n)(*[o.handle.value for o in observables])
+    out = np.zeros(2 * n)
+    A.call("qd_obs_eval", psi.handle, t, n, hp, out.ctypes.data_as(A._DP))
+    return out[0::2] + 1j * out[1::2]
+
+
+class McManager:
+    """McManager (mc_manager.hpp:14-214) without MPI: observables are named groups
+    of `dim` operators, data[name] is an (nt, dim) complex table.
+
+    addObs(name, dim), updateMatrix(name, idx, H) / incrMatrix / matrix(name, idx);
+    addAux(name, name2, func, dim) derives a table from name2's values;
+    incrAllObs(tstp, psi_tstp=-1) adds psi.eval(psi_tstp, O) of every operator into
+    row tstp (all evaluations in one device pass list, qd_obs_eval) and counts the
+    sample; normAll() divides row t by its sample count; clearAll([tstp]).  Ranks
+    combine tables with a host sum instead of MPI_Reduce (collectAll)."""
+
+    def __init__(self, nt: int, psi: State):
+        self.nt = nt
+        self.psi = psi
+        self.data = {}
+        self.obs = {}
+        self.aux = {}
+        self.func = {}
+        self.Nmc = np.zeros(nt, dtype=np.int64)
+
+    def addObs(self, name: str, dim: int) -> None:
+        self.data[name] = np.zeros((self.nt, dim), dtype=np.complex128)
+        self.obs[name] = [None] * dim
+        self.aux[name] = []
+
+    def addAux(self, name: str, name2: str, func, dim: int) -> None:
+        if name2 not in self.obs:
+            raise KeyError("addAux: wrong dependent variable!")
+        self.data[name] = np.zeros((self.nt, dim), dtype=np.complex128)
+        self.func[name] = func
+        self.aux[name2].append(name)
+
+    def updateMatrix(self, name: str, idx: int, mat: Hamiltonian) -> None:
+        self.obs[name][idx] = mat
+
+    def matrix(self, name: str, idx: int) -> Hamiltonian:
+        return self.obs[name][idx]
+
+    def incrAllObs(self, tstp: int, psi_tstp: int = -1) -> None:
+        if psi_tstp == -1:
+            psi_tstp = tstp
+        keys = [(n, d) for n, mats in self.obs.items() for d in range(len(mats))]
+        if keys:
+            vals = obs_eval(self.psi, psi_tstp, [self.obs[n][d] for n, d in keys])
+            for (n, d), v in zip(keys, vals):
+                self.data[n][tstp, d] += v
+                for a in self.aux[n]:
+                    self.data[a][tstp, d] += self.func[a](v)
+        self.Nmc[tstp] += 1
+
+    def clearAll(self, tstp: Optional[int] = None) -> None:
+        for t in self.data.values():
+            if tstp is None:
+                t[:] = 0
+            else:
+                t[tstp] = 0
+
+    def normAll(self) -> None:
+        for t in self.data.values():
+            t /= self.Nmc[:, None]
+
+
 def seeded_start(seed: int, dim: int) -> np.ndarray:
     """The start vector the request loop draws for `seed` (Philox4x32-10, host copy)."""
     out = np.empty(dim)
