@@ -251,11 +251,10 @@ def gpu_arm(args, rank, world, local):
     v0 = q.start_vector(dim, SEED).astype(np.complex128)
     psi = q.getState(sec, 2)
     psi.set(1, v0)  # resident start vector
-    solver = q.Arnoldi.getLanczosSolver(sec, KRY)
 
-    def solve_resident():
+    def solve_resident():  # a fresh solver per solve (a solver keeps its Krylov space between calls)
         A.call("qd_state_copy", psi.handle, 1, psi.handle, 0)
-        return solver.getGroundState(H, psi(0), 0)
+        return q.Arnoldi.getLanczosSolver(sec, KRY).getGroundState(H, psi(0), 0)
 
     for _ in range(args.warmup):
         solve_resident()
@@ -316,7 +315,7 @@ def gpu_arm(args, rank, world, local):
 
     def e2e_step():
         A.call("qd_state_upload", psi.handle, 0, dptr)
-        r = solver.getGroundState(H, psi(0), 0)
+        r = q.Arnoldi.getLanczosSolver(sec, KRY).getGroundState(H, psi(0), 0)
         E = psi.eval(0, H)
         A.call("qd_state_download", psi.handle, 0, optr)
         return r, E
@@ -384,11 +383,9 @@ def matrix_free_leg(ctx, H, sec, psi, ritz_csr):
     reference energy (scipy eigsh, tests/golden) and the CSR-path Ritz value."""
     import qudrip_gb300 as q
     from qudrip_gb300 import _capi as A
-    solver = q.LanczosSolver(sec, KRY, spmv=A.QD_SPMV_MATRIX_FREE)
-
     def solve():
         A.call("qd_state_copy", psi.handle, 1, psi.handle, 0)
-        return solver.getGroundState(H, psi(0), 0)
+        return q.LanczosSolver(sec, KRY, spmv=A.QD_SPMV_MATRIX_FREE).getGroundState(H, psi(0), 0)
 
     solve()
     ctx.sync()

@@ -226,7 +226,9 @@ typedef struct {
   int32_t krylov_dim; /* kry_dim of getLanczosSolver(index, kry_dim) */
   int32_t spmv;       /* QD_SPMV_CSR or QD_SPMV_MATRIX_FREE */
   int32_t ritz;       /* QD_RITZ_STORED_BASIS (default) or QD_RITZ_SECOND_PASS */
-  int32_t reserved;
+  int32_t add_dim;    /* getGroundState's add_dim: 0 or -1 runs krylov_dim steps; k in
+                         1..krylov_dim-1 runs k steps now and keeps the solve open for
+                         qd_lanczos_extend (updateKrylovRepr, sparse_algorithm.hpp:521-546) */
 } qd_lanczos_opts;
 
 typedef struct {
@@ -244,6 +246,15 @@ typedef struct {
 qd_status qd_lanczos_ground(qd_ham *ham, qd_state *psi, int t,
                             const qd_lanczos_opts *opts, double *evals_out,
                             qd_lanczos_result *res);
+
+/* A later getGroundState(H, psi, tstp, add_dim) on the same solver:
+ * continues the last qd_lanczos_ground on this operator (same krylov_dim and
+ * product kind) for opts->add_dim more steps (0 or -1: up to krylov_dim) from
+ * its stored basis, then writes the Ritz vector of the grown space to
+ * psi(:, t) and the eigenvalues to evals_out.  A solve that broke down, or
+ * whose buffers a Krylov evolution on the operator reused, does not grow. */
+qd_status qd_lanczos_extend(qd_ham *ham, qd_state *psi, int t, const qd_lanczos_opts *opts,
+                            double *evals_out, qd_lanczos_result *res);
 
 /* ------------------------------------------------------------------ */
 /* Krylov real-time step                                              */

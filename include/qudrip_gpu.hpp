@@ -24,6 +24,8 @@
 // instead of aborting.
 #pragma once
 
+#include <algorithm>
+#include <cmath>
 #include <complex>
 #include <cstdint>
 #include <fstream>
@@ -516,20 +518,39 @@ namespace Arnoldi {
 
 class LanczosSolver {
  public:
-  LanczosSolver(const SubIndex&, int kry_dim) : kry_dim_(kry_dim) {}
+  LanczosSolver(const SubIndex&, int kry_dim) : kry_dim_(kry_dim), evs_(1, 0.0) {}
   // products through the matrix-free form (qd_ham_build_matrix_free) instead of the CSR matrix
   void setMatrixFree(bool on) { spmv_ = on ? QD_SPMV_MATRIX_FREE : QD_SPMV_CSR; }
-  void getGroundState(const SpMatrix& H, State& psi, int tstp) {
+  // number of tracked eigenvalues and their initial values (sparse_algorithm.hpp:494-500)
+  void convergeEV(int N, double iv = 0.0) {
+    if (!(N < kry_dim_)) throw Error(QD_ERR_INVALID, "convergeEV: N must be below kry_dim");
+    evs_.assign((size_t)N, iv);
+  }
+  // The first call starts from psi(tstp) and runs add_dim steps (all kry_dim
+  // for -1); later calls grow the same Krylov space by add_dim more steps
+  // (sparse_algorithm.hpp:564-585); a full space returns at once.
+  void getGroundState(const SpMatrix& H, State& psi, int tstp, int add_dim = -1) {
+    if (act_ >= kry_dim_) return;
     qd_lanczos_opts o{};
     o.krylov_dim = kry_dim_;
     o.spmv = spmv_;
     o.ritz = QD_RITZ_STORED_BASIS;
+    o.add_dim = add_dim > 0 ? add_dim : 0;
     evals_.assign((size_t)kry_dim_, 0.0);
-    check(qd_lanczos_ground(H.handle(), psi.handle(), tstp, &o, evals_.data(), &res_), "getGroundState");
-    evals_.resize((size_t)res_.act_dim);
+    if (act_ == 0)
+      check(qd_lanczos_ground(H.handle(), psi.handle(), tstp, &o, evals_.data(), &res_), "getGroundState");
+    else
+      check(qd_lanczos_extend(H.handle(), psi.handle(), tstp, &o, evals_.data(), &res_), "getGroundState");
+    act_ = res_.act_dim;
+    evals_.resize((size_t)act_);
+    const size_t m = std::min(evs_.size(), (size_t)act_);
+    double e2 = 0.0;
+    for (size_t i = 0; i < m; ++i) e2 += (evals_[i] - evs_[i]) * (evals_[i] - evs_[i]);
+    err_ = std::sqrt(e2);
+    for (size_t i = 0; i < m; ++i) evs_[i] = evals_[i];
   }
-  double error() const { return res_.err; }
-  int act_dim() const { return res_.act_dim; }
+  double error() const { return err_; }
+  int act_dim() const { return act_; }
   const std::vector<double>& eigenvalues() const { return evals_; }
   void storeE(const std::string& fname) const {
     std::ofstream f(fname);
@@ -539,6 +560,9 @@ class LanczosSolver {
  private:
   int kry_dim_;
   int spmv_ = QD_SPMV_CSR;
+  int act_ = 0;
+  double err_ = 0.0;
+  std::vector<double> evs_;
   qd_lanczos_result res_{};
   std::vector<double> evals_;
 };

@@ -70,7 +70,7 @@ class qd_ham_info(C.Structure):
 
 class qd_lanczos_opts(C.Structure):
     _fields_ = [("krylov_dim", C.c_int32), ("spmv", C.c_int32), ("ritz", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("add_dim", C.c_int32)]
 
 
 class qd_lanczos_result(C.Structure):
@@ -186,6 +186,7 @@ _SIGNATURES = {
     "qd_obs_eval": [_P, C.c_int, C.c_int, C.POINTER(C.c_void_p), _DP],
     "qd_lanczos_ground": [_P, _P, C.c_int, C.POINTER(qd_lanczos_opts), _DP,
                           C.POINTER(qd_lanczos_result)],
+    "qd_lanczos_extend": [_P, _P, C.c_int, C.POINTER(qd_lanczos_opts), _DP, C.POINTER(qd_lanczos_result)],
     "qd_hermitian_lanczos_ground": [_P, _P, C.c_int, C.c_int, _DP, C.POINTER(qd_lanczos_result)],
     "qd_lanczos_evolve": [_P, _P, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_int)],
     "qd_seeded_start": [C.c_uint64, C.c_int64, _DP],

@@ -475,6 +475,18 @@ qd_status qd_arnoldi_evolve(qd_ham* ham, qd_state* psi, int t_in, int t_out, dou
   });
 }
 
+qd_status qd_lanczos_extend(qd_ham* ham, qd_state* psi, int t, const qd_lanczos_opts* opts, double* evals_out,
+                            qd_lanczos_result* res) {
+  return guard([&] {
+    QD_REQUIRE(ham && psi && opts && res, QD_ERR_INVALID, "null argument");
+    QD_REQUIRE(t >= 0 && t < psi->nt, QD_ERR_INVALID, "bad column");
+    QD_REQUIRE(psi->dim == ham->dim, QD_ERR_INVALID, "dimension mismatch");
+    DeviceGuard dg(ham->ctx->device);
+    std::memset(res, 0, sizeof(*res));
+    lanczos_extend(ham, psi->col(t), *opts, evals_out, res);
+  });
+}
+
 qd_status qd_hermitian_lanczos_ground(qd_ham* ham, qd_state* psi, int t, int kry_dim, double* evals_out,
                                       qd_lanczos_result* res) {
   return guard([&] {

@@ -478,11 +478,11 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
 template <typename MV, typename VV>
 // fxk: 0 the product alone (CSR or matrix-free), then K2; 1 the uniform-
 // coupling form with fixed-point sums fused with the step's inner products.
-static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int kdim, Workspace& W, bool mf,
-                        int fxk = 0) {
+static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int k_first, int k_last, Workspace& W,
+                        bool mf, int fxk = 0) {
   Ctx* ctx = H->ctx;
   const int64_t n = H->dim;
-  for (int k = 1; k <= kdim; ++k) {
+  for (int k = k_first; k <= k_last; ++k) {
     const VV* V1 = B.V.p + (int64_t)(k - 1) * B.ld;
     const VV* V2 = (k >= 2) ? B.V.p + (int64_t)(k - 2) * B.ld : nullptr;
     VV* Vk = B.V.p + (int64_t)k * B.ld;
@@ -525,6 +525,11 @@ LanczosBuffers<cplx>& buffers_for<cplx>(Workspace& W, int64_t n, int kdim) {
 }
 
 template <typename MV, typename VV>
+static void lanczos_finish(qd_ham* H, cplx* psi, const double* psi_nrm2, const qd_lanczos_opts& o,
+                           LanczosBuffers<VV>& B, Workspace& W, const MV* vals, bool mf, int fxk, int fxF,
+                           double* evals_out, qd_lanczos_result* res);
+
+template <typename MV, typename VV>
 static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, const qd_lanczos_opts& o,
                                 double* evals_out, qd_lanczos_result* res) {
   Ctx* ctx = H->ctx;
@@ -563,7 +568,16 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
     QD_CUDA(cudaMemsetAsync(B.ovf.p, 0, sizeof(int), ctx->stream));
     if constexpr (std::is_same<VV, double>::value) launch_fx_shadow(ctx, n, B.V.p, B.X.p, fxF, B.ovf.p);
   }
-  B.run_graph(ctx, [&]() { lanczos_run<MV, VV>(H, vals, B, kdim, W, mf, fxk); });
+  const int steps = (o.add_dim > 0 && o.add_dim < kdim) ? o.add_dim : kdim;  // add_dim of an incremental start
+  if (steps == kdim)
+    B.run_graph(ctx, [&]() { lanczos_run<MV, VV>(H, vals, B, 1, kdim, W, mf, fxk); });
+  else
+    lanczos_run<MV, VV>(H, vals, B, 1, steps, W, mf, fxk);
+  B.done = steps;
+  W.lz_vv = std::is_same<VV, double>::value ? 1 : 2;
+  W.lz_mv = std::is_same<MV, double>::value ? 1 : 2;
+  W.lz_mf = mf;
+  W.lz_fxk = fxk;
   if (fx) {
     int ov = 0;
     QD_CUDA(cudaMemcpyAsync(&ov, B.ovf.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -576,6 +590,28 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
     }
   }
   if (timing) QD_CUDA(cudaEventRecord(ctx->events[13], ctx->stream));
+  lanczos_finish<MV, VV>(H, psi, psi_nrm2, o, B, W, vals, mf, fxk, fxF, evals_out, res);
+  if (timing) {
+    float g = 0.f;
+    QD_CUDA(cudaEventElapsedTime(&g, ctx->events[12], ctx->events[13]));
+    const double host_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_t0).count();
+    std::fprintf(stderr, "[qd timing] lanczos n=%lld k=%d: recurrence %.3f ms (%.1f us/step), whole solve %.3f ms\n",
+                 (long long)n, kdim, g, 1e3 * g / kdim, host_ms);
+  }
+}
+
+// Eigen-decomposition of the tridiagonal matrix of the B.done steps run so
+// far and the Ritz vector of its lowest level, written to psi.
+template <typename MV, typename VV>
+static void lanczos_finish(qd_ham* H, cplx* psi, const double* psi_nrm2, const qd_lanczos_opts& o,
+                           LanczosBuffers<VV>& B, Workspace& W, const MV* vals, bool mf, int fxk, int fxF,
+                           double* evals_out, qd_lanczos_result* res) {
+  Ctx* ctx = H->ctx;
+  const int64_t n = H->dim;
+  const int kdim = B.done;
+  const bool fx = fxk == 1;
+  const int vg = vec_grid(ctx, n);
   int matvecs = kdim;
 
   std::vector<VV> alpha(kdim + 1);
@@ -608,7 +644,7 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
       QD_CUDA(cudaMemsetAsync(B.ovf.p, 0, sizeof(int), ctx->stream));
       if constexpr (std::is_same<VV, double>::value) launch_fx_shadow(ctx, n, B.V.p, B.X.p, fxF, B.ovf.p);
     }
-    lanczos_run<MV, VV>(H, vals, B, act, W, mf, fxk);
+    lanczos_run<MV, VV>(H, vals, B, 1, act, W, mf, fxk);
     matvecs += act;
   }
   // psi = sum_k y_k v_k = sum_k (y_k s_k) V[k]
@@ -621,20 +657,64 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
-  if (timing) {
-    float g = 0.f;
-    QD_CUDA(cudaEventElapsedTime(&g, ctx->events[12], ctx->events[13]));
-    const double host_ms =
-        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - host_t0).count();
-    std::fprintf(stderr, "[qd timing] lanczos n=%lld k=%d: recurrence %.3f ms (%.1f us/step), whole solve %.3f ms\n",
-                 (long long)n, kdim, g, 1e3 * g / kdim, host_ms);
-  }
   if (evals_out) std::memcpy(evals_out, d.data(), act * sizeof(double));
   res->act_dim = act;
   res->breakdown = stop ? 1 : 0;
   res->matvecs = matvecs;
   res->ritz_value = d[0];
   res->err = std::fabs(d[0]);
+}
+
+// updateKrylovRepr with add_dim (sparse_algorithm.hpp:521-546): the recurrence
+// of the last solve on this operator continues for add_dim more steps (up to
+// its krylov_dim) from the stored basis, and the Ritz vector of the grown
+// space is written to psi.
+template <typename MV, typename VV>
+static void lanczos_extend_impl(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, double* evals_out,
+                                qd_lanczos_result* res) {
+  Ctx* ctx = H->ctx;
+  Workspace& W = ham_workspace(H);
+  LanczosBuffers<VV>& B = buffers_for<VV>(W, H->dim, o.krylov_dim);
+  const MV* vals = nullptr;
+  if constexpr (std::is_same<MV, double>::value) vals = H->vals_r.p;
+  else vals = H->vals_c.p;
+  int stop = 0;
+  QD_CUDA(cudaMemcpyAsync(&stop, B.stop.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  const int add = (o.add_dim > 0) ? std::min(o.add_dim, B.kdim - B.done) : B.kdim - B.done;
+  if (!stop && add > 0) {
+    lanczos_run<MV, VV>(H, vals, B, B.done + 1, B.done + add, W, W.lz_mf, W.lz_fxk);
+    B.done += add;
+  }
+  if (W.lz_fxk == 1) {
+    int ov = 0;
+    QD_CUDA(cudaMemcpyAsync(&ov, B.ovf.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    QD_CUDA(cudaStreamSynchronize(ctx->stream));
+    QD_REQUIRE(!ov, QD_ERR_OVERFLOW, "a Lanczos vector left the fixed-point range; restart the solve");
+  }
+  qd_lanczos_opts o2 = o;
+  o2.ritz = QD_RITZ_STORED_BASIS;
+  lanczos_finish<MV, VV>(H, psi, nullptr, o2, B, W, vals, W.lz_mf, W.lz_fxk, W.lz_fxk == 1 ? H->fx->F : 0,
+                         evals_out, res);
+}
+
+void lanczos_extend(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, double* evals_out, qd_lanczos_result* res) {
+  Workspace& W = ham_workspace(H);
+  QD_REQUIRE(W.lz_vv != 0, QD_ERR_INVALID, "no Lanczos solve on this operator to continue");
+  const bool dbl = (W.lz_vv == 1);
+  LanczosBuffers<double>& Bd = W.lz_d;
+  LanczosBuffers<cplx>& Bc = W.lz_c;
+  const int kd = dbl ? Bd.kdim : Bc.kdim;
+  QD_REQUIRE(o.krylov_dim == kd, QD_ERR_INVALID, "krylov_dim %d differs from the running solve's %d", o.krylov_dim,
+             kd);
+  QD_REQUIRE((o.spmv == QD_SPMV_MATRIX_FREE) == (W.lz_mf != 0), QD_ERR_INVALID,
+             "the product kind differs from the running solve's");
+  if (dbl)
+    lanczos_extend_impl<double, double>(H, psi, o, evals_out, res);
+  else if (W.lz_mv == 1)
+    lanczos_extend_impl<double, cplx>(H, psi, o, evals_out, res);
+  else
+    lanczos_extend_impl<cplx, cplx>(H, psi, o, evals_out, res);
 }
 
 void lanczos_ground(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, double* evals_out, qd_lanczos_result* res) {
@@ -924,6 +1004,7 @@ static void lanczos_evolve_steps(qd_ham* H, cplx* psi, double h, int m, int nste
   if constexpr (std::is_same<MV, double>::value) vals = H->vals_r.p;
   else vals = H->vals_c.p;
   const int mv_kind = std::is_same<MV, double>::value ? 1 : 2;
+  W.lz_vv = 0;  // the Lanczos buffers are reused here: no ground-state run left to continue
   if (!W.evolve) W.evolve.reset(new EvolveGraph());
   EvolveGraph& G = *W.evolve;
   if (!G.nrm2.p) {
@@ -955,7 +1036,7 @@ static void lanczos_evolve_steps(qd_ham* H, cplx* psi, double h, int m, int nste
       init_v0_kernel<cplx><<<vg, kVecThreads, 0, ctx->stream>>>(n, psi, G.nrm2.p, B.V.p);
       QD_CHECK_LAUNCH();
       QD_LAUNCHED(ctx);
-      lanczos_run<MV, cplx>(H, vals, B, kdim, W, false);
+      lanczos_run<MV, cplx>(H, vals, B, 1, kdim, W, false);
       texp_kernel<<<1, 32, 0, ctx->stream>>>(kdim, h, B.alpha.p, B.nrm.p, B.scl.p, B.stop.p, G.y.p, G.act.p,
                                              G.matvecs.p);
       QD_CHECK_LAUNCH();

@@ -30,6 +30,7 @@ struct LanczosBuffers {
   DBuf<int> ovf;
   cudaGraphExec_t exec = nullptr;
   int kind = 0;  // product the captured graph launches (0 CSR, 1 matrix-free, 2 fixed-point)
+  int done = 0;  // Lanczos steps run on the stored basis (incremental solves continue from here)
   void ensure_fx() {
     if (!X.p) {
       X.alloc((size_t)2 * ld);
@@ -95,6 +96,9 @@ struct EvolveGraphDeleter {
 struct Workspace {
   Ctx* ctx;
   std::unique_ptr<EvolveGraph, EvolveGraphDeleter> evolve;  // cached Krylov-step graph
+  // the last Lanczos ground-state run: vector type (1 real, 2 complex), value
+  // type (1 real, 2 complex), product kind -- what a continuation must reuse
+  int lz_vv = 0, lz_mv = 0, lz_mf = 0, lz_fxk = 0;
   DBuf<double> partials_d, gpart_d;
   DBuf<cplx> partials_c, gpart_c;
   DBuf<Tri<double>> partials_td, gpart_td;
@@ -126,6 +130,7 @@ cplx state_eval(qd_ham* H, const cplx* psi);
 double state_norm2(qd_ham* H, const cplx* psi);
 void obs_eval_many(qd_ham* const* obs, int nobs, const cplx* psi, cplx* out_host);
 void lanczos_ground(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, double* evals_out, qd_lanczos_result* res);
+void lanczos_extend(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, double* evals_out, qd_lanczos_result* res);
 void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per_launch);
 void lanczos_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int m, int nsteps, int* act_out,
                     int64_t* matvecs_out);

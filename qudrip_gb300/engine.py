@@ -271,7 +271,15 @@ def shuffle_state(psi: State, seed: int = 12345) -> None:
 
 
 class LanczosSolver:
-    """Arnoldi::getLanczosSolver(index, kry_dim) -- ArnoldiSolver<T, herm=1>."""
+    """Arnoldi::getLanczosSolver(index, kry_dim) -- ArnoldiSolver<T, herm=1>.
+
+    As the reference solver, it keeps its Krylov space between calls: the
+    first getGroundState(H, psi, tstp, add_dim) starts from psi(tstp) and runs
+    add_dim steps (all kry_dim steps for add_dim = -1); later calls continue
+    the same space by add_dim more steps (qd_lanczos_extend) until kry_dim, and
+    once it is full they return at once.  error() is the change of the lowest
+    N eigenvalues since the previous call, N and the initial values set by
+    convergeEV(N, iv) (sparse_algorithm.hpp:494-500, 564-585)."""
 
     def __init__(self, index: Sector, kry_dim: int, spmv: int = A.QD_SPMV_CSR,
                  ritz: int = A.QD_RITZ_STORED_BASIS):
@@ -282,19 +290,28 @@ class LanczosSolver:
         self._evals = np.empty(0)
         self._act = 0
         self._err = 0.0
+        self._evs = np.zeros(1)
         self.result = None
 
+    def convergeEV(self, N: int, iv: float = 0.0) -> None:
+        if not N < self.kry_dim:
+            raise ValueError("convergeEV: N must be below kry_dim")
+        self._evs = np.full(N, float(iv))
+
     def getGroundState(self, H: Hamiltonian, psi: State, tstp: int, add_dim: int = -1):
-        if add_dim != -1:
-            raise NotImplementedError("incremental add_dim restarts are not supported")
-        opts = A.qd_lanczos_opts(self.kry_dim, self.spmv, self.ritz, 0)
+        if self._act >= self.kry_dim:
+            return self.result
+        opts = A.qd_lanczos_opts(self.kry_dim, self.spmv, self.ritz, add_dim if add_dim > 0 else 0)
         evals = np.empty(self.kry_dim, dtype=np.float64)
         res = A.qd_lanczos_result()
-        A.call("qd_lanczos_ground", H.handle, psi.handle, tstp, C.byref(opts),
-               evals.ctypes.data_as(C.POINTER(C.c_double)), C.byref(res))
+        name = "qd_lanczos_ground" if self._act == 0 else "qd_lanczos_extend"
+        A.call(name, H.handle, psi.handle, tstp, C.byref(opts), evals.ctypes.data_as(C.POINTER(C.c_double)),
+               C.byref(res))
         self._act = res.act_dim
         self._evals = evals[:res.act_dim].copy()
-        self._err = res.err
+        m = min(len(self._evs), res.act_dim)
+        self._err = float(np.sqrt(np.sum((self._evals[:m] - self._evs[:m]) ** 2)))
+        self._evs[:m] = self._evals[:m]
         self.result = res
         return res
 

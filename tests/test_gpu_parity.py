@@ -279,3 +279,34 @@ def test_every_product_kernel(ctx, name):
     A.call("qd_ham_autotune", gh.handle, 3, C.byref(chosen), C.byref(ms))
     # 120 (the uniform-coupling fixed-point form) competes where it applies
     assert (chosen.value in A.SPMV_KERNELS or chosen.value == A.QD_SPMV_FX) and ms.value > 0
+
+
+def test_incremental_add_dim_grows_the_same_krylov_space(ctx):
+    """getGroundState(..., add_dim) three times = one solve of the full dimension
+    (updateKrylovRepr, sparse_algorithm.hpp:521-546), with error() the change of
+    the tracked eigenvalues between calls."""
+    spec, ham = chains.xxz_chain(14, 1.0, 0.8, True, list(np.linspace(-0.5, 0.7, 14)))
+    gsec, gh = gpu_objects(spec, ham)
+    v0 = q.start_vector(gsec.dim, 21)
+    one = q.Arnoldi.getLanczosSolver(gsec, 60)
+    p1 = q.getState(gsec, 1)
+    p1.set(0, v0)
+    one.getGroundState(gh, p1(0), 0)
+    inc = q.Arnoldi.getLanczosSolver(gsec, 60)
+    inc.convergeEV(2)
+    p2 = q.getState(gsec, 1)
+    p2.set(0, v0)
+    oh = O.Ham(O.Sector(spec), ham)
+    prev = np.zeros(2)
+    for step, k in enumerate((20, 40, 60)):
+        inc.getGroundState(gh, p2(0), 0, add_dim=20)
+        assert inc.act_dim() == k
+        ev = inc.eigenvalues()
+        assert abs(inc.error() - np.sqrt(np.sum((ev[:2] - prev) ** 2))) <= 1e-12 * (1 + abs(ev[0]))
+        prev = ev[:2].copy()
+        o = oh.lanczos_ground(v0, k)
+        assert abs(ev[0] - o["ritz"]) <= 1e-10 * abs(o["ritz"])
+    assert np.array_equal(inc.eigenvalues(), one.eigenvalues())
+    assert np.array_equal(p2.get(0), p1.get(0))
+    inc.getGroundState(gh, p2(0), 0, add_dim=20)  # the space is full: nothing changes
+    assert inc.act_dim() == 60
