@@ -105,10 +105,15 @@ class ClockSampler:
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
+            return
+        # wait (at most 3 s) for the first sample so the timed region is covered
+        t_end = time.monotonic() + 3.0
+        while time.monotonic() < t_end and os.path.getsize(self.path) == 0 and self.proc.poll() is None:
+            time.sleep(0.01)
 
     def stop(self):
         if not self.proc:
@@ -620,7 +625,7 @@ def serving_mix(n_req=400, rate=200.0, seed=77, **opts):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=30)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")

@@ -5,7 +5,9 @@ package, and only as the checker: the qudrip_gb300 product never imports it.
 
 `qd_oracle.cpp` restates the reference algorithms (see its header for the
 file:line map and for the parity status: the reference needs Eigen3, which is
-absent, so the oracle is pinned by independent known answers in tests/golden/).
+absent, and has no tests or golden vectors, so parity is unpinned against the
+reference itself; the oracle is checked against independent known answers in
+tests/golden/).
 `build()` compiles it with g++ (-ffp-contract=off, so x86-64 and aarch64 hosts
 produce the same bits) into oracle/_build/libqdoracle.so.
 """

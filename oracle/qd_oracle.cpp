@@ -4,13 +4,15 @@
 // GB300 engine: tests/, __graft_entry__.smoke() and bench.py's CPU baseline
 // are its only users.  Nothing in the qudrip_gb300 product links or calls it.
 //
-// Parity status: QuDrip itself cannot be compiled in this environment (it is
-// header-only C++20 on Eigen3 >= 3.3, CMakeLists.txt:18, and Eigen is not
-// installed), and QuDrip ships no tests or golden vectors.  The restatement
-// below follows the reference line by line (each function cites the file:line
-// it restates) and is pinned by independent known answers committed under
-// tests/golden/: free-fermion closed forms, dense exact diagonalisation and
-// scipy eigsh energies, and structural counts (dim, nnz).
+// Parity status: parity unpinned against the reference itself.  QuDrip cannot
+// be compiled in this environment (it is header-only C++20 on Eigen3 >= 3.3,
+// CMakeLists.txt:18, and Eigen is not installed), and QuDrip ships no tests or
+// golden vectors, so no output of the reference is available to compare
+// with.  The restatement below follows the reference line by line (each
+// function cites the file:line it restates) and is checked against
+// independent known answers committed under tests/golden/: free-fermion
+// closed forms, dense exact diagonalisation with explicit Jordan-Wigner
+// strings, scipy eigsh energies, and structural counts (dim, nnz).
 //
 // Arithmetic: complex products are written out as (ac - bd, ad + bc) with
 // separate roundings, which is what GCC emits for std::complex<double> on
