@@ -252,6 +252,8 @@ def gpu_arm(args, rank, world, local):
     spec, ham = chains.xxz_chain(L)
     sec = q.Sector(spec.index, spec.constraints, ctx=ctx)
     H = sec.lower(ham)
+    if args.product is not None:
+        A.call("qd_ham_set_spmv_kernel", H.handle, args.product)
     dim = sec.dim
     v0 = q.start_vector(dim, SEED).astype(np.complex128)
     psi = q.getState(sec, 2)
@@ -518,6 +520,8 @@ def spmv_only(args, local):
     spec, ham = chains.xxz_chain(L)
     sec = q.Sector(spec.index, spec.constraints, ctx=ctx)
     H = sec.lower(ham)
+    if args.product is not None:
+        A.call("qd_ham_set_spmv_kernel", H.handle, args.product)
     kernels = sorted(A.SPMV_KERNELS) + [A.QD_SPMV_MATRIX_FREE] if args.spmv_only == 9999 else [args.spmv_only]
     hbm_peak, _ = peaks()
     for k in kernels:
@@ -634,6 +638,8 @@ def main():
                     help="only time product KERNEL on the L=24 matrix (100..111 CSR kernels, 1 matrix-free, "
                          "9999 all)")
     ap.add_argument("--iters", type=int, default=50)
+    ap.add_argument("--product", type=int, default=None, metavar="KERNEL",
+                    help="product kernel of the Lanczos solves (qd_ham_set_spmv_kernel code; default: the engine's)")
     ap.add_argument("--serve-only", action="store_true", help="only run the serving mix")
     ap.add_argument("--serve-requests", type=int, default=400)
     args = ap.parse_args()

@@ -338,9 +338,11 @@ qd_status qd_traj_run(qd_ham *heff, const qd_traj_desc *desc, const double *psi0
  * Hamiltonian (iters back-to-back launches on the context stream, timed with
  * CUDA events), and the kernel's algorithmic HBM bytes per launch:
  * CSR: nnz*(value + 4) + (dim+1)*8 + dim*(x + y) bytes; 120: nnz_offdiag*4 +
- * (dim+1)*4 + dim*(8 diagonal + 8 x + 16 fixed-point x + 8 y); 1 (matrix-free):
+ * (dim+1)*4 + dim*(8 diagonal + 8 x + 16 fixed-point x + 8 y); 121: dim*(4
+ * state + 8 diagonal + 8 x + 16 fixed-point x + 8 y); 1 (matrix-free):
  * dim*(8 basis + diagonal + x + y).  Code 0 times what the Lanczos path
- * launches.  Diagnostic codes:
+ * launches (for 120 and 121 with the fused inner products: + 8 v2 per row).
+ * Diagnostic codes:
  * 2000 + kernel times the product with the fused Lanczos dot epilogue; 3001
  * and 3002 time the two Lanczos vector kernels alone (real Hamiltonians). */
 qd_status qd_ham_time_spmv(qd_ham *ham, int spmv, int iters, double *avg_ms,
@@ -356,11 +358,16 @@ qd_status qd_ham_time_spmv(qd_ham *ham, int spmv, int iters, double *avg_ms,
  * values and each row's off-diagonal sum is accumulated exactly in 128-bit
  * fixed point from a fixed-point copy of the vector, rounded once to FP64.
  * It is the default wherever it applies (real start vector); choosing any
- * other code turns it off.  All give the same products up to rounding. */
+ * other code turns it off.  121: the same form with the columns computed on
+ * the fly from the operator's terms instead of read (product sectors of at
+ * most 32 bits; kept only after a build-time check that every row's columns
+ * equal its stored ones, so 121 and 120 give bit-identical solves).  All
+ * give the same products up to rounding. */
 qd_status qd_ham_set_spmv_kernel(qd_ham *ham, int kernel);
-/* Time every product kernel on this Hamiltonian (120 included where it
- * applies) and keep the fastest for the solvers (the autotuner); returns the
- * choice and its average ms. */
+/* Time every product kernel on this Hamiltonian (120 and 121 included where
+ * they apply, timed as the recurrence launches them, with its inner products)
+ * and keep the fastest for the solvers (the autotuner); returns the choice
+ * and its average ms. */
 qd_status qd_ham_autotune(qd_ham *ham, int iters, int *chosen, double *best_ms);
 
 /* <psi|H|psi> for a CSR Hamiltonian, with no device allocation at all.

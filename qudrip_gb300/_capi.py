@@ -37,6 +37,7 @@ QD_SPMV_MATRIX_FREE = 1
 QD_RITZ_STORED_BASIS = 0
 QD_RITZ_SECOND_PASS = 1
 QD_SPMV_FX = 120  # uniform-coupling form with exact fixed-point row sums
+QD_SPMV_FX_SLOTS = 121  # the same with the columns computed on the fly from the terms
 SPMV_KERNELS = {100: "tile", 101: "balanced", 102: "vector2", 103: "vector4", 104: "vector8",
                 105: "scalar", 106: "row4", 107: "row8", 108: "row4_stream", 109: "row8_stream",
                 110: "row_exact", 111: "row_sorted"}

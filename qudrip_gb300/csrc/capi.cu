@@ -270,8 +270,9 @@ qd_status qd_ham_get_info(qd_ham* ham, qd_ham_info* info) {
     info->flags = ham->flags;
     info->max_row_nnz = ham->max_row_nnz;
     info->has_matrix_free = ham->has_mf ? 1 : 0;
-    info->product_kernel = ((ham->flags & QD_HAM_REAL) && ham->fx_allowed && ham_build_fx(ham)) ? kSpmvFx
-                                                                                                 : ham->spmv_variant;
+    info->product_kernel = ham->spmv_variant;
+    if ((ham->flags & QD_HAM_REAL) && ham->fx_allowed && ham_build_fx(ham))
+      info->product_kernel = (ham->fx->use_slots && ham->fx->slots_state > 0) ? kSpmvFxSlots : kSpmvFx;
   });
 }
 
@@ -454,7 +455,7 @@ qd_status qd_lanczos_ground(qd_ham* ham, qd_state* psi, int t, const qd_lanczos_
 qd_status qd_ham_time_spmv(qd_ham* ham, int spmv, int iters, double* avg_ms, double* bytes_per_launch) {
   return guard([&] {
     QD_REQUIRE(ham && avg_ms && bytes_per_launch && iters >= 1, QD_ERR_INVALID, "bad argument");
-    const bool plain = spmv == QD_SPMV_CSR || spmv == QD_SPMV_MATRIX_FREE || spmv == kSpmvFx ||
+    const bool plain = spmv == QD_SPMV_CSR || spmv == QD_SPMV_MATRIX_FREE || spmv == kSpmvFx || spmv == kSpmvFxSlots ||
                        (spmv >= kSpmvTile && spmv <= kSpmvLast);
     const bool fused = spmv >= 2000 + kSpmvTile && spmv <= 2000 + kSpmvLast;
     const bool vec = spmv == 3001 || spmv == 3002;
@@ -554,11 +555,14 @@ qd_status qd_traj_run(qd_ham* heff, const qd_traj_desc* desc, const double* psi0
 
 qd_status qd_ham_set_spmv_kernel(qd_ham* ham, int kernel) {
   return guard([&] {
-    QD_REQUIRE(ham && ((kernel >= kSpmvTile && kernel <= kSpmvLast) || kernel == kSpmvFx), QD_ERR_INVALID,
-               "unknown product kernel");
+    QD_REQUIRE(ham && ((kernel >= kSpmvTile && kernel <= kSpmvLast) || kernel == kSpmvFx || kernel == kSpmvFxSlots),
+               QD_ERR_INVALID, "unknown product kernel");
     DeviceGuard dg(ham->ctx->device);
-    if (kernel == kSpmvFx) {
+    if (kernel == kSpmvFx || kernel == kSpmvFxSlots) {
       QD_REQUIRE(ham_build_fx(ham), QD_ERR_UNSUPPORTED, "the fixed-point form does not apply to this operator");
+      QD_REQUIRE(kernel == kSpmvFx || ham->fx->slots_state > 0, QD_ERR_UNSUPPORTED,
+                 "the columns of this operator cannot be computed on the fly (code 121)");
+      ham->fx->use_slots = (kernel == kSpmvFxSlots);
       ham->fx_allowed = true;
       return;
     }
@@ -586,13 +590,24 @@ qd_status qd_ham_autotune(qd_ham* ham, int iters, int* chosen, double* best_ms) 
     ham->spmv_variant = pick;
     ham->fx_allowed = false;
     if ((ham->flags & QD_HAM_REAL) && ham_build_fx(ham)) {
-      double ms = 0;
-      time_spmv(ham, kSpmvFx, iters, &ms, &bytes);
-      if (ms < best) {
-        best = ms;
-        pick = kSpmvFx;
+      // the fixed-point forms as the recurrence launches them (fused with the step's inner products,
+      // which a CSR kernel leaves to a separate pass): a conservative comparison for them
+      const bool slots0 = ham->fx->use_slots;
+      int fx_pick = 0;
+      for (int v = kSpmvFx; v <= kSpmvFxSlots; ++v) {
+        if (v == kSpmvFxSlots && ham->fx->slots_state <= 0) continue;
+        double ms = 0;
         ham->fx_allowed = true;
+        ham->fx->use_slots = (v == kSpmvFxSlots);
+        time_spmv(ham, QD_SPMV_CSR, iters, &ms, &bytes);
+        if (ms < best) {
+          best = ms;
+          pick = v;
+          fx_pick = v;
+        }
       }
+      ham->fx_allowed = fx_pick != 0;
+      ham->fx->use_slots = fx_pick ? (fx_pick == kSpmvFxSlots) : slots0;
     }
     if (chosen) *chosen = pick;
     if (best_ms) *best_ms = best;

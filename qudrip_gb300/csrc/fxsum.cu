@@ -5,6 +5,7 @@
 
 #include "fxsum.cuh"
 #include "ham.cuh"
+#include "krylov.cuh"
 #include "scan.cuh"
 #include "spmv.cuh"
 #include "vec.cuh"
@@ -51,14 +52,40 @@ __global__ void fx_count_kernel(int64_t n, const int64_t* rowptr, const int32_t*
   }
 }
 
+// Columns of row r in gather order: by the highest bit in which the column's
+// state differs from the row's state, highest first (ties by column).  Rows
+// next to each other share their high bits, so the entries of a warp's 32
+// rows that flip high bits line up lane by lane and land on consecutive X
+// values: the first gathers of a warp coalesce, and the ones that flip low
+// bits fall near the warp's own rows.  The row sum is an exact integer sum,
+// so the order does not change any result.
+__device__ __forceinline__ int fx_order_key(uint64_t s, const uint64_t* basis, int32_t c) {
+  return 63 - __clzll((long long)(s ^ basis[c]));
+}
+
 __global__ void fx_fill_kernel(int64_t n, const int64_t* rowptr, const int32_t* colidx, const double* vals,
-                               const int64_t* off, int32_t* rowptr32, int32_t* colidx_fx) {
+                               const int64_t* off, const uint64_t* basis, int32_t* rowptr32, int32_t* colidx_fx) {
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r <= n; r += (int64_t)gridDim.x * blockDim.x) {
     rowptr32[r] = (int32_t)off[r];
     if (r == n) break;
-    int64_t o = off[r];
+    const int64_t o0 = off[r];
+    int64_t o = o0;
     for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k)
       if (colidx[k] != (int32_t)r && vals[k] != 0.0) colidx_fx[o++] = colidx[k];
+    const uint64_t s = basis[r];
+    for (int64_t i = o0 + 1; i < o; ++i) {  // insertion sort: rows hold at most 128 columns
+      const int32_t c = colidx_fx[i];
+      const int kc = fx_order_key(s, basis, c);
+      int64_t j = i - 1;
+      while (j >= o0) {
+        const int32_t p = colidx_fx[j];
+        const int kp = fx_order_key(s, basis, p);
+        if (kp > kc || (kp == kc && p < c)) break;
+        colidx_fx[j + 1] = p;
+        --j;
+      }
+      colidx_fx[j + 1] = c;
+    }
   }
 }
 
@@ -114,12 +141,14 @@ bool ham_build_fx(qd_ham* H) {
   fx->colidx.alloc(std::max<int64_t>(total, 1) + 16);
   QD_CUDA(cudaMemsetAsync(fx->colidx.p, 0, fx->colidx.bytes(), ctx->stream));
   fx_fill_kernel<<<fx_grid(ctx, n + 1), 256, 0, ctx->stream>>>(n, H->rowptr.p, H->colidx.p, H->vals_r.p, off.p,
+                                                               H->sec->basis.p,
                                                                fx->rowptr.p, fx->colidx.p);
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
   H->fx = std::move(fx);
   H->fx_state = 1;
+  ham_build_fx_slots(H);  // columns on the fly where the operator's terms allow it
   return true;
 }
 
@@ -224,6 +253,10 @@ void launch_fx_dots(Ctx* ctx, const qd_ham* H, const double* x, const __int128* 
   const double cF = std::ldexp(f.c, -f.F);
   const int g = fx_dots_grid(ctx, H->dim);
   QD_REQUIRE(g <= kMaxGrid, QD_ERR_UNSUPPORTED, "reduction grid exceeds its partials buffer");
+  if (f.slots_state > 0 && f.use_slots) {  // same grid: the same reduction tree as below
+    launch_fx_slots_dots(ctx, H, x, X, V2, y, s1, s2, stop, step, beta, alpha, dots, red, g);
+    return;
+  }
   if (V2)
     spmv_fx_dots_kernel<true><<<g, 256, 0, ctx->stream>>>(H->dim, f.rowptr.p, f.colidx.p, f.diag.p, x, X, V2, y, cF,
                                                            s1, s2, stop, step, beta, alpha, dots, red);
@@ -243,6 +276,10 @@ __global__ void fx_shadow_kernel(int64_t n, const double* x, __int128* X, int F,
 void launch_fx(Ctx* ctx, const qd_ham* H, const double* x, const __int128* X, double* y, const double* scale_dev,
                const int* stop, int step) {
   const FxForm& f = *H->fx;
+  if (f.slots_state > 0 && f.use_slots) {
+    launch_fx_slots(ctx, H, x, X, y, scale_dev, stop, step);
+    return;
+  }
   const double cF = std::ldexp(f.c, -f.F);
   spmv_fx_kernel<<<(unsigned)std::max<int64_t>(1, ceil_div(H->dim, 256)), 256, 0, ctx->stream>>>(
       H->dim, f.rowptr.p, f.colidx.p, f.diag.p, x, X, y, cF, scale_dev, stop, step);

@@ -15,20 +15,76 @@
 // bits of headroom for up to 128 summands: F = 119 - ceil(log2(bound)), so
 // elements down to 2^-66 of the bound convert exactly and the result is at
 // least as accurate as a sequential FP64 sum.  A value above the bound sets
-// an overflow flag and the solver reruns on the FP64 CSR product.
+// an overflow flag and the solver reruns on the FP64 CSR product.  (Turning
+// each gathered FP64 value into fixed point inside the product instead costs
+// about 20 integer instructions per gather, more than the copy saves.)
 #pragma once
+
+#include <cstdint>
 
 #include "common.cuh"
 
 namespace qd {
 
+// Columns on the fly (kernel code 121).  When the operator came from terms on
+// a product sector of at most 32 bits, the off-diagonal columns of row r
+// (state s) are not read from memory but computed from the compiled
+// transitions (ham.cuh, MfEntry).  A transition whose support is a contiguous
+// run of bits of one field changes the colex rank only inside the run, by an
+// amount fixed by the run's input pattern p and the number m of set bits of
+// the field below the run: its column is r + delta[p][m].  Such transitions
+// are grouped into run slots (one support, at most one transition per input
+// pattern), each a shift, a mask, a popcount and one table load per row; the
+// table holds the offset and a 0/1 weight, so a slot with no transition for
+// the row adds X[r] * 0.
+// Other transitions go into rank slots (one support and flip, up to four
+// input patterns) and rank s ^ flip by byte tables.  All lanes of a warp take
+// the same slot at the same time, so for slots on high bits 32 consecutive
+// rows gather 32 consecutive X values.  The slot form is kept only after a
+// check over every row that its columns are exactly the stored columns of the
+// row, so its integer sums, and its products, are bit-identical to code 120's.
+constexpr int kFxSlotWidth = 4;
+struct FxSlot {    // rank slot
+  uint32_t sup;    // support bits
+  uint32_t flip;   // input ^ output on the support
+  uint32_t pad[2];
+  uint32_t outb[kFxSlotWidth];  // input patterns on the support; unused ones hold ~sup (never match)
+};
+// run slot (uint4): x = lowest bit of the run, y = run mask (after the shift),
+// z = bits of the run's field below the run, w = offset of delta[0][0]; the
+// table row of pattern p starts at w + p * kk; entries are {offset, weight}.
+
+// Ranking of a product sector of at most two constrained fields in 32 bits by
+// byte tables (mfree.cu builds the same tables for its 32-bit product).
+struct Rank32 {
+  int nf;
+  int lo[2], k[2], nb[2];
+  uint32_t wmask[2];
+  uint32_t stride[2];
+  int off[2];
+  const uint32_t* tab;
+};
+
 struct FxForm {
   DBuf<int32_t> rowptr;  // dim + 1 (off-diagonal entries only)
-  DBuf<int32_t> colidx;  // off-diagonal columns, ascending within each row
+  DBuf<int32_t> colidx;  // off-diagonal columns of each row in gather order (fx_fill_kernel)
   DBuf<double> diag;     // d_r (0 where the CSR has no diagonal entry)
   double c = 0.0;        // the common off-diagonal value
   int F = 0;             // fixed-point scale 2^F
   int64_t nnz = 0;
+  // columns on the fly (code 121)
+  int slots_state = 0;     // 0 not tried, 1 built and checked, -1 not applicable
+  bool use_slots = false;  // the products take the slot form (code 121) instead of the stored columns
+  int nrun = 0;            // run slots, a multiple of 4 (padding slots never match)
+  int nslot = 0;           // rank slots, a multiple of 4
+  int kk = 0;              // run-table row length: max over fields of k + 1
+  int ndtab = 0;
+  DBuf<uint4> runs;
+  DBuf<FxSlot> slots;
+  DBuf<int2> dtab;
+  DBuf<uint32_t> basis32;  // the sector's basis in 32 bits
+  DBuf<uint32_t> rtab;     // byte tables of Rank32
+  Rank32 rank{};
 };
 
 #ifdef __CUDACC__

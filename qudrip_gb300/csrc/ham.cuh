@@ -111,6 +111,9 @@ void ham_lower(qd_ham* H, const qd_term* terms, int nterms, const qd_gate* gates
 void ham_transpose(Ctx* ctx, int64_t n, const int64_t* ptr, const int32_t* idx, const cplx* vals,
                    int64_t nnz, int64_t* out_ptr, int32_t* out_idx, cplx* out_vals);
 void ham_build_matrix_free(qd_ham* H);
+void compile_terms(const qd_ham* H, std::vector<MfEntry>& off, std::vector<MfEntry>& dia);
+void build_tables(const qd_sector* S, MfRank& rk, std::vector<int64_t>& tab);
+bool ham_build_fx_slots(qd_ham* H);
 bool ham_lower_pull(qd_ham* H);
 void mf_apply_c(qd_ham* H, const cplx* x, cplx* y);
 bool ham_build_fx(qd_ham* H);

@@ -409,8 +409,20 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   const bool mf = (spmv == QD_SPMV_MATRIX_FREE);
   if (mf) ham_build_matrix_free(H);
   // code 0: the product the real Lanczos path launches (the fixed-point form when it applies)
-  const bool fx = real && (spmv == kSpmvFx || (spmv == QD_SPMV_CSR && H->fx_allowed)) && ham_build_fx(H);
-  QD_REQUIRE(spmv != kSpmvFx || fx, QD_ERR_UNSUPPORTED, "the fixed-point form does not apply to this operator");
+  const bool fxcode = spmv == kSpmvFx || spmv == kSpmvFxSlots;
+  const bool fx = real && (fxcode || (spmv == QD_SPMV_CSR && H->fx_allowed)) && ham_build_fx(H);
+  QD_REQUIRE(!fxcode || fx, QD_ERR_UNSUPPORTED, "the fixed-point form does not apply to this operator");
+  QD_REQUIRE(spmv != kSpmvFxSlots || H->fx->slots_state > 0, QD_ERR_UNSUPPORTED,
+             "the columns of this operator cannot be computed on the fly (code 121)");
+  struct SlotChoice {  // 120 / 121 pick the column source for this timing only
+    FxForm* f;
+    bool saved;
+    ~SlotChoice() {
+      if (f) f->use_slots = saved;
+    }
+  } choice{fx ? H->fx.get() : nullptr, fx ? H->fx->use_slots : true};
+  if (fx && fxcode) H->fx->use_slots = (spmv == kSpmvFxSlots);
+  const bool slots = fx && H->fx->use_slots && H->fx->slots_state > 0;
   DBuf<__int128> X(fx ? n + 32 : 1);
   if (fx) QD_CUDA(cudaMemsetAsync(X.p, 0, X.bytes(), ctx->stream));
   auto launch = [&]() {
@@ -472,6 +484,8 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   if (fx)  // columns, row pointers (int32), diagonal, x, its fixed-point copy, y (+ v2 for the fused dots)
     *bytes_per_launch = (double)H->fx->nnz * 4.0 + (double)(n + 1) * 4.0 +
                         (double)n * (8.0 + 8.0 + 16.0 + 8.0 + (spmv == QD_SPMV_CSR ? 8.0 : 0.0));
+  if (slots)  // 32-bit state, diagonal, x, its fixed-point copy once, y (+ v2)
+    *bytes_per_launch = (double)n * (4.0 + 8.0 + 8.0 + 16.0 + 8.0 + (spmv == QD_SPMV_CSR ? 8.0 : 0.0));
 }
 
 // ---------------------------------------------------------------- Lanczos

@@ -138,6 +138,11 @@ void hermitian_lanczos_ground(qd_ham* H, cplx* psi, int kdim, double* evals_out,
 void launch_fx_dots(Ctx* ctx, const qd_ham* H, const double* x, const __int128* X, const double* V2, double* y,
                     const double* s1, const double* s2, const int* stop, int step, double* beta, double* alpha,
                     Tri<double>* dots, GridRed<Tri<double>> red);
+void launch_fx_slots(Ctx* ctx, const qd_ham* H, const double* x, const __int128* X, double* y,
+                     const double* scale_dev, const int* stop, int step);
+void launch_fx_slots_dots(Ctx* ctx, const qd_ham* H, const double* x, const __int128* X, const double* V2,
+                          double* y, const double* s1, const double* s2, const int* stop, int step, double* beta,
+                          double* alpha, Tri<double>* dots, GridRed<Tri<double>> red, int grid);
 template <typename VV>
 void launch_mf(Ctx* ctx, qd_ham* H, const VV* x, VV* y, double scale, const double* scale_dev, const int* stop,
                int step);

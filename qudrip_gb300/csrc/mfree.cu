@@ -101,7 +101,7 @@ static bool host_leaf(const std::vector<qd_gate>& G, const qd_term& T, int nbit,
   return true;
 }
 
-static void compile_terms(const qd_ham* H, std::vector<MfEntry>& off, std::vector<MfEntry>& dia) {
+void compile_terms(const qd_ham* H, std::vector<MfEntry>& off, std::vector<MfEntry>& dia) {
   const std::vector<qd_term>& terms = H->host_terms;
   const std::vector<qd_gate>& gates = H->host_gates;
   for (size_t t = 0; t < terms.size(); ++t) {
@@ -159,7 +159,7 @@ static void compile_terms(const qd_ham* H, std::vector<MfEntry>& off, std::vecto
   }
 }
 
-static void build_tables(const qd_sector* S, MfRank& rk, std::vector<int64_t>& tab) {
+void build_tables(const qd_sector* S, MfRank& rk, std::vector<int64_t>& tab) {
   int64_t C[64][64];
   for (int n = 0; n < 64; ++n)
     for (int k = 0; k < 64; ++k) C[n][k] = (k == 0) ? 1 : (n == 0 ? 0 : C[n - 1][k - 1] + C[n - 1][k]);

@@ -32,6 +32,7 @@ enum SpmvVariant {
   kSpmvRowSorted = 111, // as 110, rows taken in length order within 256-row windows
   kSpmvLast = 111,
   kSpmvFx = 120,        // uniform-coupling form, exact fixed-point sums (fxsum.cuh)
+  kSpmvFxSlots = 121,   // as 120 with the columns computed on the fly (fxslots.cu)
 };
 
 constexpr int kSpmvWarps = 4;  // warps per block

@@ -62,3 +62,86 @@ def test_fixed_point_product_timing_and_applicability(ctx):
     r, _ = solve(sec2, H2, v0, 60)
     o = O.Ham(O.Sector(spec2), ham2).lanczos_ground(v0, 60)
     assert abs(r.ritz_value - o["ritz"]) <= 1e-10 * abs(o["ritz"])
+
+
+def product_kernel(H):
+    info = A.qd_ham_info()
+    A.call("qd_ham_get_info", H.handle, info)
+    return info.product_kernel
+
+
+def two_species_xy(L, periodic):
+    """Hard-core bosons of two species on bits 0..L-1 and L..2L-1 (two popcount fields), uniform hopping."""
+    from qudrip_gb300.operators import (II, SectorSpec, getBoseGate, getEmptyOperator, getNdo, getNup, getQbits,
+                                        pauli_x, pauli_y, pauli_z)
+    pre = getQbits(2 * L)
+    spec = SectorSpec(pre, [getNup(pre, L) == L // 2, getNdo(pre, L) == L // 2 - 1])
+    gc, ga, gz = getBoseGate(pre), getBoseGate(pre), getBoseGate(pre)
+    gc << 0.5 * (pauli_x + II * pauli_y)
+    ga << 0.5 * (pauli_x - II * pauli_y)
+    gz << 0.5 * pauli_z
+    ham = getEmptyOperator()
+    for sp in (0, L):
+        for i in range(L if periodic else L - 1):
+            a, b = sp + i, sp + (i + 1) % L
+            ham = ham + 0.75 * (gc(a) * ga(b)) + 0.75 * (gc(b) * ga(a))
+    for i in range(L):
+        ham = ham + 1.3 * (gz(i) * gz(i + L))
+    return spec, ham
+
+
+CASES = {
+    "xxz16_periodic": lambda: chains.xxz_chain(16, 1.0, 0.7, periodic=True),
+    "xxz14_open_fields": lambda: chains.xxz_chain(14, 1.0, 1.0, periodic=False,
+                                                  fields=np.random.default_rng(3).uniform(-1, 1, 14)),
+    "xy12_open": lambda: chains.xy_chain(12),
+    "two_species_periodic": lambda: two_species_xy(6, True),
+    "two_species_open": lambda: two_species_xy(7, False),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_columns_on_the_fly_bit_identical_to_stored_columns(ctx, name):
+    """Code 121 computes each row's columns from the compiled terms (a table over the set bits below a
+    contiguous support, byte-table ranks for the periodic bond); the build checks them against the stored
+    columns, and the recurrence launches the same grid and reduction, so the solve is bit-identical."""
+    spec, ham = CASES[name]()
+    sec, H = gpu_objects(spec, ham)
+    assert product_kernel(H) == A.QD_SPMV_FX  # stored columns by default; 121 where it is chosen
+    v0 = q.start_vector(sec.dim, 17)
+    r121, psi121 = solve(sec, H, v0, 60, kernel=A.QD_SPMV_FX_SLOTS)
+    r120, psi120 = solve(sec, H, v0, 60, kernel=A.QD_SPMV_FX)
+    assert product_kernel(H) == A.QD_SPMV_FX
+    assert r121.ritz_value == r120.ritz_value and r121.act_dim == r120.act_dim
+    assert np.array_equal(psi121, psi120)
+    o = O.Ham(O.Sector(spec), ham).lanczos_ground(v0, 60)
+    assert abs(r121.ritz_value - o["ritz"]) <= 1e-10 * abs(o["ritz"])
+
+
+def test_columns_on_the_fly_timing_and_fallback(ctx):
+    spec, ham = chains.xxz_chain(16, 1.0, 1.0, periodic=True)
+    sec, H = gpu_objects(spec, ham)
+    ms, nb = C.c_double(), C.c_double()
+    A.call("qd_ham_time_spmv", H.handle, A.QD_SPMV_FX_SLOTS, 5, C.byref(ms), C.byref(nb))
+    assert ms.value > 0 and nb.value == sec.dim * (4 + 8 + 8 + 16 + 8)
+    A.call("qd_ham_set_spmv_kernel", H.handle, A.QD_SPMV_FX_SLOTS)
+    A.call("qd_ham_time_spmv", H.handle, A.QD_SPMV_CSR, 5, C.byref(ms), C.byref(nb))  # what Lanczos launches
+    assert nb.value == sec.dim * (4 + 8 + 8 + 16 + 8 + 8)
+    # a term on 7 sites is beyond the compiled form: the stored columns stay, 121 is refused, 120 runs
+    from qudrip_gb300.operators import II, SectorSpec, getBoseGate, getEmptyOperator, getNset, getQbits
+    pre = getQbits(12)
+    gc, ga, gn = getBoseGate(pre), getBoseGate(pre), getBoseGate(pre)
+    gc << 0.5 * (q.pauli_x + II * q.pauli_y)
+    ga << 0.5 * (q.pauli_x - II * q.pauli_y)
+    gn << np.array([[0, 0], [0, 1]], dtype=complex)
+    ham2 = getEmptyOperator()
+    for i in range(11):
+        ham2 = ham2 + gc(i) * ga(i + 1) + gc(i + 1) * ga(i)
+    ham2 = ham2 + gc(0) * ga(2) * gn(3) * gn(4) * gn(5) * gn(6) * gn(7)
+    ham2 = ham2 + gc(2) * ga(0) * gn(3) * gn(4) * gn(5) * gn(6) * gn(7)
+    sec2, H2 = gpu_objects(SectorSpec(pre, [getNset(pre) == 6]), ham2)
+    assert product_kernel(H2) == A.QD_SPMV_FX
+    if True:
+        with pytest.raises(A.QDError) as e:
+            A.call("qd_ham_set_spmv_kernel", H2.handle, A.QD_SPMV_FX_SLOTS)
+        assert e.value.code == A.QD_ERR_UNSUPPORTED
