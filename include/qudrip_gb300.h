@@ -172,6 +172,20 @@ qd_status qd_ham_lower(qd_sector *sec, const qd_term *terms, int nterms,
 qd_status qd_ham_destroy(qd_ham *ham);
 qd_status qd_ham_get_info(qd_ham *ham, qd_ham_info *info);
 
+/* *out = a + b for two matrices on the same sector: the union of their
+ * patterns, each value a + b (a + 0 where only one has the entry), explicit
+ * zeros kept -- Eigen's sparse sum of two lowered SpMatrix values, as
+ * Model::getHamiltonianMatrix (lattice.hpp:339-354) and McManager::incrMatrix
+ * (mc_manager.hpp:72-79) use it.  The result has no operator terms, so it has
+ * no matrix-free form (qd_ham_build_matrix_free answers QD_ERR_UNSUPPORTED). */
+qd_status qd_ham_add(const qd_ham *a, const qd_ham *b, qd_ham **out);
+/* *out = an independent copy of a (the value semantics of SpMatrix). */
+qd_status qd_ham_copy(const qd_ham *a, qd_ham **out);
+/* ham *= (re + i im), value by value with the rounding of a std::complex
+ * product (McManager::normMatrix, mc_manager.hpp:81-83); the derived forms
+ * (fixed-point, matrix-free, cached solver graphs) are dropped. */
+qd_status qd_ham_scale(qd_ham *ham, double re, double im);
+
 /* Matrix-free form: replaces Operator::map_acc / OperatorSum::map_acc
  * (operator.hpp:215-232, operator_abel.hpp:36-49).  Compiles the operator
  * tree into per-support transitions (terms of at most 6 sites, at most 512

@@ -16,6 +16,11 @@
 //   getState, psi(t), psi.eval(t, H)                     state.hpp:9-104
 //   Arnoldi::getLanczosSolver(index, k).getGroundState   sparse_algorithm.hpp:475-604
 //   Arnoldi::getSolver(index, k).evolve                  sparse_algorithm.hpp:548-562
+//   SpMatrix + SpMatrix, SpMatrix *= s (device-side)     Eigen sparse sum / scale
+//   McManager (addObs, addAux, updateMatrix, incrMatrix, normMatrix, incrAllObs,
+//   clearAll, normAll, collectAll, outFile, obsValue)    mc_manager.hpp:14-214
+//   Lattice / LatticeFunction / Model / params_type      qudrip_gpu_lattice.hpp
+//   param_finder                                         qudrip_gpu_params.hpp
 //
 // Differences a caller sees: matrices are the small `Matrix` type below
 // (2x2 gate matrices) instead of Eigen; the lowered operator is a device
@@ -29,6 +34,8 @@
 #include <complex>
 #include <cstdint>
 #include <fstream>
+#include <functional>
+#include <iostream>
 #include <map>
 #include <memory>
 #include <random>
@@ -370,6 +377,30 @@ class SpMatrix {
   int64_t cols() const { return info_.dim; }
   int64_t nonZeros() const { return info_.nnz; }
   qd_ham* handle() const { return ham_.get(); }
+  bool empty() const { return !ham_; }
+  // Eigen's sparse sum: union pattern, a + b per value, explicit zeros kept.
+  SpMatrix operator+(const SpMatrix& o) const {
+    qd_ham* h = nullptr;
+    check(qd_ham_add(ham_.get(), o.ham_.get(), &h), "SpMatrix +");
+    return SpMatrix(h);
+  }
+  SpMatrix& operator+=(const SpMatrix& o) { return *this = *this + o; }
+  // Value semantics: a copy shares the device matrix until one of them is scaled.
+  SpMatrix& operator*=(value_type s) {
+    if (ham_.use_count() > 1) {
+      qd_ham* h = nullptr;
+      check(qd_ham_copy(ham_.get(), &h), "SpMatrix copy");
+      *this = SpMatrix(h);
+    }
+    check(qd_ham_scale(ham_.get(), s.real(), s.imag()), "SpMatrix *=");
+    check(qd_ham_get_info(ham_.get(), &info_), "qd_ham_get_info");
+    return *this;
+  }
+  SpMatrix operator*(value_type s) const {
+    SpMatrix r = *this;
+    r *= s;
+    return r;
+  }
   // Reference layout: column pointers, row indices, complex values.
   void csc(std::vector<int64_t>& colptr, std::vector<int32_t>& rowidx, std::vector<value_type>& vals) const {
     colptr.resize((size_t)info_.dim + 1);
@@ -460,48 +491,121 @@ inline void shuffle_state(State& psi, uint64_t seed = 12345) {
 }
 
 // ------------------------------------------------------------------ observables
-// McManager (mc_manager.hpp:14-214) without MPI: named groups of `dim`
+#define MC_REAL 0
+#define MC_COMPLEX 1
+using functor_type = std::function<value_type(const value_type&)>;
+
+// McManager (mc_manager.hpp:14-214) in one process: named groups of `dim`
 // operators with an (nt x dim) table each; incrAllObs evaluates every
 // operator on psi(psi_tstp) in one qd_obs_eval pass and adds into row tstp.
+// collectAll is the one-process case of the reference's MPI_Reduce (nothing
+// to combine; replicas combine their tables on the host).  obsValue(name, t,
+// idx) reads row t, column idx.
 class McManager {
  public:
   McManager(int nt, State* p_psi) : nt_(nt), p_psi_(p_psi), Nmc_((size_t)nt, 0) {}
   explicit McManager(State* p_psi) : McManager(p_psi->nt(), p_psi) {}
 
-  void addObs(const std::string& name, int dim) {
+  void addObs(const std::string& name, int dim, int type = MC_COMPLEX) {
     data_[name] = std::vector<value_type>((size_t)nt_ * dim, value_type(0.0, 0.0));
     dims_[name] = dim;
+    type_[name] = type;
     obs_[name] = std::vector<SpMatrix>((size_t)dim);
+    aux_[name] = {};
+  }
+  void addAux(const std::string& name, const std::string& name2, const functor_type& func, int dim,
+              int aux_type = MC_COMPLEX) {
+    if (obs_.find(name2) == obs_.end()) throw std::string{"addAux: wrong dependent variable!"};
+    data_[name] = std::vector<value_type>((size_t)nt_ * dim, value_type(0.0, 0.0));
+    dims_[name] = dim;
+    type_[name] = aux_type;
+    func_[name] = func;
+    aux_[name2].push_back(name);
   }
   void updateMatrix(const std::string& name, int idx, const SpMatrix& mat) { obs_.at(name).at((size_t)idx) = mat; }
+  void incrMatrix(const std::string& name, int idx, const SpMatrix& mat) {
+    SpMatrix& m = obs_.at(name).at((size_t)idx);
+    if (m.empty()) m = mat;
+    else m += mat;
+  }
+  void normMatrix(const std::string& name, int idx, value_type s) { obs_.at(name).at((size_t)idx) *= s; }
   SpMatrix& matrix(const std::string& name, int idx) { return obs_.at(name).at((size_t)idx); }
 
   void incrAllObs(int tstp, int psi_tstp = -1) {
     if (psi_tstp == -1) psi_tstp = tstp;
     std::vector<qd_ham*> hs;
-    std::vector<value_type*> dst;
+    std::vector<std::pair<std::string, size_t>> dst;
     for (auto& o : obs_)
       for (size_t d = 0; d < o.second.size(); ++d) {
         hs.push_back(o.second[d].handle());
-        dst.push_back(&data_[o.first][(size_t)tstp * dims_[o.first] + d]);
+        dst.emplace_back(o.first, d);
       }
     if (!hs.empty()) {
       std::vector<double> v(2 * hs.size());
       check(qd_obs_eval(p_psi_->handle(), psi_tstp, (int)hs.size(), hs.data(), v.data()), "incrAllObs");
-      for (size_t i = 0; i < hs.size(); ++i) *dst[i] += value_type(v[2 * i], v[2 * i + 1]);
+      for (size_t i = 0; i < hs.size(); ++i) {
+        const value_type term(v[2 * i], v[2 * i + 1]);
+        const std::string& n = dst[i].first;
+        const size_t d = dst[i].second;
+        data_[n][(size_t)tstp * dims_[n] + d] += term;
+        for (const auto& a : aux_[n]) data_[a][(size_t)tstp * dims_[a] + d] += func_[a](term);
+      }
     }
     ++Nmc_[(size_t)tstp];
+  }
+  void clearAll(int tstp) {
+    for (auto& d : data_)
+      for (int k = 0; k < dims_[d.first]; ++k) d.second[(size_t)tstp * dims_[d.first] + k] = 0.0;
+  }
+  void clearAll() {
+    for (auto& d : data_) std::fill(d.second.begin(), d.second.end(), value_type(0.0, 0.0));
   }
   void normAll() {
     for (auto& d : data_)
       for (int t = 0; t < nt_; ++t)
         for (int k = 0; k < dims_[d.first]; ++k) d.second[(size_t)t * dims_[d.first] + k] *= 1.0 / Nmc_[(size_t)t];
   }
-  void clearAll() {
-    for (auto& d : data_) std::fill(d.second.begin(), d.second.end(), value_type(0.0, 0.0));
+  void collectAll() {}
+  int report() const { return 0; }
+  value_type obsValue(const std::string& name, int tstp, int idx) const {
+    return data_.at(name).at((size_t)tstp * dims_.at(name) + idx);
   }
-  value_type value(const std::string& name, int t, int d) const {
-    return data_.at(name).at((size_t)t * dims_.at(name) + d);
+  value_type value(const std::string& name, int t, int d) const { return obsValue(name, t, d); }
+
+  // The TSV table of mc_manager.hpp:147-196: "#time[\tindex]", one column per
+  // real observable and two (real, imag) per complex one, std::to_string
+  // values; with dim > 1 a row per index and a blank line after each time.
+  void outFile(double h, const std::string& fname, const std::vector<std::string>& obs_names,
+               int precision = 6) const {
+    (void)precision;  // the reference takes it and does not use it
+    std::ofstream f(fname);
+    auto it0 = data_.find(obs_names.at(0));
+    if (it0 == data_.end()) throw std::string{"outFile: wrong name!!"};
+    const int dim = dims_.at(obs_names[0]);
+    std::string label = dim > 1 ? "#time\tindex" : "#time";
+    for (const auto& n : obs_names) {
+      auto it = type_.find(n);
+      if (it == type_.end()) throw std::string{"outFile: wrong name!!"};
+      if (it->second == MC_REAL) label += "\t" + n;
+      else label += "\t" + n + "(real)" + "\t" + n + "(imag)";
+      if (dims_.at(n) != dim) {
+        std::cout << "mismatched dimensions" << std::endl;
+        return;
+      }
+    }
+    f << label << std::endl;
+    for (int t = 0; t < nt_; ++t) {
+      for (int idx = 0; idx < dim; ++idx) {
+        label = dim > 1 ? std::to_string(t * h) + "\t" + std::to_string(idx) : std::to_string(t * h);
+        for (const auto& n : obs_names) {
+          const value_type v = data_.at(n)[(size_t)t * dims_.at(n) + idx];
+          label += "\t" + std::to_string(v.real());
+          if (type_.at(n) == MC_COMPLEX) label += "\t" + std::to_string(v.imag());
+        }
+        f << label << std::endl;
+      }
+      if (dim > 1) f << std::endl;
+    }
   }
 
  private:
@@ -510,7 +614,10 @@ class McManager {
   std::vector<int> Nmc_;
   std::map<std::string, std::vector<value_type>> data_;
   std::map<std::string, int> dims_;
+  std::map<std::string, int> type_;
   std::map<std::string, std::vector<SpMatrix>> obs_;
+  std::map<std::string, std::vector<std::string>> aux_;
+  std::map<std::string, functor_type> func_;
 };
 
 // ------------------------------------------------------------------ solvers

@@ -11,5 +11,7 @@ from .operators import (II, id, pauli_x, pauli_y, pauli_z, getQbits, getNset, ge
 from .engine import (Context, default_context, Sector, Constrain, LooseConstrain, Hamiltonian,  # noqa: F401
                      State, getState, apply, start_vector, shuffle_state, LanczosSolver, ArnoldiSolver, Arnoldi,
                      batch_lanczos, traj_run, lanczos_evolve, seeded_start, Server, Hermitian,
-                     HermitianLanczosSolver, obs_eval, McManager)
+                     HermitianLanczosSolver, obs_eval, McManager, MC_REAL, MC_COMPLEX)
+from .lattice import params_type, Lattice, LatticeFunction, Model, get_reci  # noqa: F401
+from .params import param_finder  # noqa: F401
 from . import _capi  # noqa: F401

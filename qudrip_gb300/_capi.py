@@ -172,6 +172,9 @@ _SIGNATURES = {
     "qd_ham_lower": [_P, C.POINTER(qd_term), C.c_int, C.POINTER(qd_gate), C.c_int, _PP],
     "qd_ham_destroy": [_P],
     "qd_ham_get_info": [_P, C.POINTER(qd_ham_info)],
+    "qd_ham_add": [_P, _P, _PP],
+    "qd_ham_copy": [_P, _PP],
+    "qd_ham_scale": [_P, C.c_double, C.c_double],
     "qd_ham_build_matrix_free": [_P],
     "qd_ham_apply_matrix_free": [_P, _P, C.c_int, _P, C.c_int],
     "qd_ham_download_csc": [_P, _I64P, C.POINTER(C.c_int32), _DP],

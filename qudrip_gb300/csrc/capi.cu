@@ -252,6 +252,49 @@ qd_status qd_ham_lower(qd_sector* sec, const qd_term* terms, int nterms, const q
   });
 }
 
+qd_status qd_ham_add(const qd_ham* a, const qd_ham* b, qd_ham** out) {
+  return guard([&] {
+    QD_REQUIRE(a && b && out, QD_ERR_INVALID, "qd_ham_add: null argument");
+    QD_REQUIRE(a->sec == b->sec, QD_ERR_INVALID, "qd_ham_add: the operands live on different sectors");
+    DeviceGuard dg(a->ctx->device);
+    auto* H = new qd_ham();
+    H->ctx = a->ctx;
+    H->sec = a->sec;
+    try {
+      ham_add(a, b, H);
+    } catch (...) {
+      delete H;
+      throw;
+    }
+    *out = H;
+  });
+}
+
+qd_status qd_ham_copy(const qd_ham* a, qd_ham** out) {
+  return guard([&] {
+    QD_REQUIRE(a && out, QD_ERR_INVALID, "qd_ham_copy: null argument");
+    DeviceGuard dg(a->ctx->device);
+    auto* H = new qd_ham();
+    H->ctx = a->ctx;
+    H->sec = a->sec;
+    try {
+      ham_copy(a, H);
+    } catch (...) {
+      delete H;
+      throw;
+    }
+    *out = H;
+  });
+}
+
+qd_status qd_ham_scale(qd_ham* ham, double re, double im) {
+  return guard([&] {
+    QD_REQUIRE(ham, QD_ERR_INVALID, "qd_ham_scale: null argument");
+    DeviceGuard dg(ham->ctx->device);
+    ham_scale(ham, mkc(re, im));
+  });
+}
+
 qd_status qd_ham_destroy(qd_ham* ham) {
   return guard([&] {
     if (!ham) return;

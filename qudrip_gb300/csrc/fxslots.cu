@@ -264,7 +264,7 @@ bool ham_build_fx_slots(qd_ham* H) {
   if (f.slots_state != 0) return f.slots_state > 0;
   f.slots_state = -1;
   const SectorView& V = H->sec->view;
-  if (H->host_terms.empty() || V.rank_kind != 1 || V.nbits > 32 || H->dim >= (1ll << 31)) return false;
+  if (!H->from_terms || V.rank_kind != 1 || V.nbits > 32 || H->dim >= (1ll << 31)) return false;
   if (V.nfields < 1 || V.nfields > 2) return false;
   uint32_t fmask[2] = {0u, 0u};
   int kk = 1;

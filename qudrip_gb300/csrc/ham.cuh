@@ -102,12 +102,17 @@ struct qd_ham {
   qd::MfRank mf_rank{};
   std::vector<qd_term> host_terms;
   std::vector<qd_gate> host_gates;
+  bool from_terms = false;  // the values are the lowering of host_terms (not a sum or a multiple of matrices)
   std::unique_ptr<qd::Workspace, qd::WorkspaceDeleter> ws;  // solver buffers, reused across calls
   std::unique_ptr<qd::ArnoldiBuffers, qd::ArnoldiDeleter> arnoldi;
 };
 
 namespace qd {
 void ham_lower(qd_ham* H, const qd_term* terms, int nterms, const qd_gate* gates, int ngates);
+void ham_finish(qd_ham* H);
+void ham_add(const qd_ham* A, const qd_ham* B, qd_ham* out);
+void ham_copy(const qd_ham* A, qd_ham* out);
+void ham_scale(qd_ham* H, cplx s);
 void ham_transpose(Ctx* ctx, int64_t n, const int64_t* ptr, const int32_t* idx, const cplx* vals,
                    int64_t nnz, int64_t* out_ptr, int32_t* out_idx, cplx* out_vals);
 void ham_build_matrix_free(qd_ham* H);

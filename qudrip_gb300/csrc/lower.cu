@@ -316,6 +316,7 @@ void ham_lower(qd_ham* H, const qd_term* terms, int nterms, const qd_gate* gates
   }
   H->host_terms.assign(terms, terms + nterms);
   H->host_gates.assign(gates, gates + ngates);
+  H->from_terms = true;
   const int64_t dim = S->view.dim;
   H->dim = dim;
   DBuf<TermDev> dterms(ht.size());
@@ -373,6 +374,14 @@ void ham_lower(qd_ham* H, const qd_term* terms, int nterms, const qd_gate* gates
     ham_transpose(ctx, dim, colptr.p, rowidx.p, cvals.p, nnz, H->rowptr.p, H->colidx.p, H->vals_c.p);
   }
 
+  ham_finish(H);
+}
+
+// Flags (real, Hermitian), the longest row and the real copies of the values
+// of a CSR matrix held by H.
+void ham_finish(qd_ham* H) {
+  Ctx* ctx = H->ctx;
+  const int64_t dim = H->dim;
   DBuf<int> flags(3);
   QD_CUDA(cudaMemsetAsync(flags.p, 0, 3 * sizeof(int), ctx->stream));
   if (dim > 0) {
@@ -387,6 +396,8 @@ void ham_lower(qd_ham* H, const qd_term* terms, int nterms, const qd_gate* gates
   H->flags = (hf[0] ? 0 : QD_HAM_REAL) | (hf[1] ? 0 : QD_HAM_HERMITIAN);
   H->max_row_nnz = hf[2];
   const int64_t nnz = H->nnz;
+  H->vals_r = DBuf<double>();
+  H->vals_f = DBuf<float>();
   if (H->flags & QD_HAM_REAL) {
     H->vals_r.alloc(nnz + 16);
     H->vals_f.alloc(nnz + 16);

@@ -319,6 +319,8 @@ static int mf_grid(Ctx* ctx, int64_t n) {
 
 void ham_build_matrix_free(qd_ham* H) {
   if (H->has_mf) return;
+  QD_REQUIRE(H->from_terms, QD_ERR_UNSUPPORTED,
+             "the matrix-free form compiles operator terms; this matrix is a sum or a multiple of lowered ones");
   Ctx* ctx = H->ctx;
   const qd_sector* S = H->sec;
   std::vector<MfEntry> off, dia;

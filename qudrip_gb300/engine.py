@@ -128,20 +128,59 @@ def LooseConstrain(index: QbitsIndex, tight: int, *constraints: Constraint,
 
 
 class Hamiltonian:
-    """A lowered OperatorSum (qd_ham): CSR on the device, reference CSC on demand."""
+    """A lowered OperatorSum (qd_ham): CSR on the device, reference CSC on demand.
 
-    def __init__(self, sector: Sector, opsum: OperatorSum):
+    `a + b` is the reference's SpMatrix sum (union pattern, values added, explicit
+    zeros kept: qd_ham_add), `s * a` a scaled copy and `a.scale(s)` scales in place
+    (qd_ham_scale); Hamiltonian.zero(sector) is the empty matrix SpMatrix(n, n)."""
+
+    def __init__(self, sector: Sector, opsum: Optional[OperatorSum] = None, handle=None):
         self.sector = sector
         self.ctx = sector.ctx
-        terms, nt, gates, ng = opsum.pack()
         self.handle = C.c_void_p()
-        A.call("qd_ham_lower", sector.handle, terms, nt, gates, ng, C.byref(self.handle))
+        if handle is not None:
+            self.handle = handle
+        else:
+            terms, nt, gates, ng = (opsum or OperatorSum([])).pack()
+            A.call("qd_ham_lower", sector.handle, terms, nt, gates, ng, C.byref(self.handle))
+        self._refresh()
+
+    def _refresh(self):
         info = A.qd_ham_info()
         A.call("qd_ham_get_info", self.handle, C.byref(info))
         self.dim = info.dim
         self.nnz = info.nnz
         self.flags = info.flags
         self.max_row_nnz = info.max_row_nnz
+
+    @staticmethod
+    def zero(sector: Sector) -> "Hamiltonian":
+        return Hamiltonian(sector, OperatorSum([]))
+
+    def __add__(self, other: "Hamiltonian") -> "Hamiltonian":
+        if not isinstance(other, Hamiltonian):
+            return NotImplemented
+        h = C.c_void_p()
+        A.call("qd_ham_add", self.handle, other.handle, C.byref(h))
+        return Hamiltonian(self.sector, handle=h)
+
+    def copy(self) -> "Hamiltonian":
+        h = C.c_void_p()
+        A.call("qd_ham_copy", self.handle, C.byref(h))
+        return Hamiltonian(self.sector, handle=h)
+
+    def scale(self, s) -> "Hamiltonian":
+        s = complex(s)
+        A.call("qd_ham_scale", self.handle, s.real, s.imag)
+        self._refresh()
+        return self
+
+    def __mul__(self, s) -> "Hamiltonian":
+        if isinstance(s, Hamiltonian):
+            return NotImplemented
+        return self.copy().scale(s)
+
+    __rmul__ = __mul__
 
     @property
     def is_real(self) -> bool:
@@ -456,16 +495,28 @@ def obs_eval(psi: State, t: int, observables) -> np.ndarray:
     return out[0::2] + 1j * out[1::2]
 
 
-class McManager:
-    """McManager (mc_manager.hpp:14-214) without MPI: observables are named groups
-    of `dim` operators, data[name] is an (nt, dim) complex table.
+MC_REAL = 0
+MC_COMPLEX = 1
 
-    addObs(name, dim), updateMatrix(name, idx, H) / incrMatrix / matrix(name, idx);
-    addAux(name, name2, func, dim) derives a table from name2's values;
+
+def _to_string(v) -> str:
+    """std::to_string: %d for integers, %f for floating point."""
+    return "%d" % v if isinstance(v, (int, np.integer)) else "%f" % v
+
+
+class McManager:
+    """McManager (mc_manager.hpp:14-214): observables are named groups of `dim`
+    operators, data[name] is an (nt, dim) complex table.
+
+    addObs(name, dim, type=MC_COMPLEX), updateMatrix(name, idx, H) / incrMatrix
+    (matrix sum) / normMatrix (in-place multiple) / matrix(name, idx);
+    addAux(name, name2, func, dim, aux_type) derives a table from name2's values;
     incrAllObs(tstp, psi_tstp=-1) adds psi.eval(psi_tstp, O) of every operator into
     row tstp (all evaluations in one device pass list, qd_obs_eval) and counts the
-    sample; normAll() divides row t by its sample count; clearAll([tstp]).  Ranks
-    combine tables with a host sum instead of MPI_Reduce (collectAll)."""
+    sample; normAll() divides row t by its sample count; clearAll([tstp]);
+    collectAll() averages the tables over the ranks of torch.distributed (the
+    reference's MPI_Reduce, then / Nproc), a no-op in one process; outFile(h,
+    fname, names) writes the reference's TSV table (rank 0 only)."""
 
     def __init__(self, nt: int, psi: State):
         self.nt = nt
@@ -474,22 +525,36 @@ class McManager:
         self.obs = {}
         self.aux = {}
         self.func = {}
+        self.type = {}
         self.Nmc = np.zeros(nt, dtype=np.int64)
 
-    def addObs(self, name: str, dim: int) -> None:
+    def report(self) -> int:
+        import torch.distributed as dist
+        return dist.get_rank() if dist.is_available() and dist.is_initialized() else 0
+
+    def addObs(self, name: str, dim: int, type: int = MC_COMPLEX) -> None:
         self.data[name] = np.zeros((self.nt, dim), dtype=np.complex128)
         self.obs[name] = [None] * dim
         self.aux[name] = []
+        self.type[name] = type
 
-    def addAux(self, name: str, name2: str, func, dim: int) -> None:
+    def addAux(self, name: str, name2: str, func, dim: int, aux_type: int = MC_COMPLEX) -> None:
         if name2 not in self.obs:
             raise KeyError("addAux: wrong dependent variable!")
         self.data[name] = np.zeros((self.nt, dim), dtype=np.complex128)
         self.func[name] = func
+        self.type[name] = aux_type
         self.aux[name2].append(name)
 
     def updateMatrix(self, name: str, idx: int, mat: Hamiltonian) -> None:
         self.obs[name][idx] = mat
+
+    def incrMatrix(self, name: str, idx: int, mat: Hamiltonian) -> None:
+        cur = self.obs[name][idx]
+        self.obs[name][idx] = mat.copy() if cur is None else cur + mat
+
+    def normMatrix(self, name: str, idx: int, s) -> None:
+        self.obs[name][idx].scale(s)
 
     def matrix(self, name: str, idx: int) -> Hamiltonian:
         return self.obs[name][idx]
@@ -516,6 +581,51 @@ class McManager:
     def normAll(self) -> None:
         for t in self.data.values():
             t /= self.Nmc[:, None]
+
+    def collectAll(self) -> None:
+        import torch
+        import torch.distributed as dist
+        if not (dist.is_available() and dist.is_initialized()):
+            return
+        n = dist.get_world_size()
+        for name in sorted(self.data):
+            t = torch.from_numpy(self.data[name].view(np.float64).copy())
+            dist.all_reduce(t)
+            self.data[name] = (t.numpy() / n).view(np.complex128)
+
+    def obsValue(self, name: str, tstp: int, idx: int) -> complex:
+        return complex(self.data[name][tstp, idx])
+
+    def outFile(self, h: float, fname: str, obs_names, precision: int = 6) -> None:
+        """The TSV table of mc_manager.hpp:147-196: "#time[\tindex]" and one column per
+        real observable or two (real, imag) per complex one, values as std::to_string
+        writes them; with dim > 1 a row per index and a blank line after each time."""
+        if self.report() != 0:
+            return
+        with open(fname, "w") as f:
+            if obs_names[0] not in self.data:
+                raise KeyError("outFile: wrong name!!")
+            dim = self.data[obs_names[0]].shape[1]
+            label = "#time\tindex" if dim > 1 else "#time"
+            for n in obs_names:
+                if n not in self.type:
+                    raise KeyError("outFile: wrong name!!")
+                label += ("\t" + n) if self.type[n] == MC_REAL else ("\t" + n + "(real)" + "\t" + n + "(imag)")
+                if self.data[n].shape[1] != dim:
+                    print("mismatched dimensions")
+                    return
+            f.write(label + "\n")
+            for t in range(self.nt):
+                for idx in range(dim):
+                    row = _to_string(t * h) + ("\t" + _to_string(idx) if dim > 1 else "")
+                    for n in obs_names:
+                        v = self.data[n][t, idx]
+                        row += "\t" + _to_string(float(v.real))
+                        if self.type[n] == MC_COMPLEX:
+                            row += "\t" + _to_string(float(v.imag))
+                    f.write(row + "\n")
+                if dim > 1:
+                    f.write("\n")
 
 
 def seeded_start(seed: int, dim: int) -> np.ndarray:
