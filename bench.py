@@ -413,7 +413,9 @@ def matrix_free_leg(ctx, H, sec, psi, ritz_csr):
             "bytes_per_product": pb.value, "ritz_value": r.ritz_value,
             "rel_dE_vs_reference_E0": abs(r.ritz_value - e0) / abs(e0),
             "rel_dE_vs_csr_path": abs(r.ritz_value - ritz_csr) / abs(ritz_csr),
-            "device_bytes_of_the_operator": "basis 8 B/row + diagonal 8 B/row (no CSR)"}
+            "device_bytes_of_the_operator": ("uniform couplings: 32-bit states 4 B/row + diagonal 8 B/row + slot "
+                                             "tables of a few KB (no CSR is read); otherwise basis 8 B/row + "
+                                             "diagonal 8 B/row")}
 
 
 def batched_sweep(ctx, n_inst=512, steps=80, seed=2024):

@@ -191,7 +191,11 @@ qd_status qd_ham_scale(qd_ham *ham, double re, double im);
  * tree into per-support transitions (terms of at most 6 sites, at most 512
  * state-changing transitions in all) and a stored diagonal; products then read
  * only the basis, the diagonal and the vectors.  Solvers take it with
- * qd_lanczos_opts.spmv = QD_SPMV_MATRIX_FREE (built on demand). */
+ * qd_lanczos_opts.spmv = QD_SPMV_MATRIX_FREE (built on demand).  For real
+ * operators with one value on every off-diagonal entry, the matrix-free
+ * Lanczos recurrence runs the exact fixed-point slot form (kernel code 121)
+ * built from the transitions alone (no stored matrix is read), bit-identical
+ * to the stored-matrix recurrence; other operators take the FP64 product. */
 qd_status qd_ham_build_matrix_free(qd_ham *ham);
 /* y(:, t_out) = H x(:, t_in) through the matrix-free form (x != y). */
 qd_status qd_ham_apply_matrix_free(qd_ham *ham, qd_state *x, int t_in,
@@ -354,8 +358,11 @@ qd_status qd_traj_run(qd_ham *heff, const qd_traj_desc *desc, const double *psi0
  * CSR: nnz*(value + 4) + (dim+1)*8 + dim*(x + y) bytes; 120: nnz_offdiag*4 +
  * (dim+1)*4 + dim*(8 diagonal + 8 x + 16 fixed-point x + 8 y); 121: dim*(4
  * state + 8 diagonal + 8 x + 16 fixed-point x + 8 y); 1 (matrix-free):
- * dim*(8 basis + diagonal + x + y).  Code 0 times what the Lanczos path
- * launches (for 120 and 121 with the fused inner products: + 8 v2 per row).
+ * dim*(8 basis + diagonal + x + y), or, where one value c is on every
+ * off-diagonal entry, the 121 slot form built from the terms alone with its
+ * fused inner products, dim*(4 + 8 + 8 + 16 + 8 + 8).  Code 0 times what the
+ * Lanczos path launches (for 120 and 121 with the fused inner products: + 8 v2
+ * per row).
  * Diagnostic codes:
  * 2000 + kernel times the product with the fused Lanczos dot epilogue; 3001
  * and 3002 time the two Lanczos vector kernels alone (real Hamiltonians). */

@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <vector>
 
 #include "ham.cuh"
@@ -218,8 +219,7 @@ __global__ void __launch_bounds__(256, 6) spmv_fx_slots_dots_kernel(
 }
 
 // ---------------------------------------------------------------- host
-static FxSlotArgs slot_args(const qd_ham* H) {
-  const FxForm& f = *H->fx;
+static FxSlotArgs slot_args(const qd_ham* H, const FxForm& f) {
   FxSlotArgs A;
   std::memset(&A, 0, sizeof(A));
   A.n = H->dim;
@@ -259,10 +259,10 @@ static int64_t window_rank(uint32_t w, int a, int m, const int64_t (*C)[65]) {
   return r;
 }
 
-bool ham_build_fx_slots(qd_ham* H) {
-  FxForm& f = *H->fx;
-  if (f.slots_state != 0) return f.slots_state > 0;
-  f.slots_state = -1;
+// Slots, tables, the 32-bit basis and (when rank slots exist, or `tables`)
+// the byte tables of the form f for the transitions of value c; false when
+// the operator's terms do not give this form.
+static bool make_slots(qd_ham* H, FxForm& f, double c, bool tables) {
   const SectorView& V = H->sec->view;
   if (!H->from_terms || V.rank_kind != 1 || V.nbits > 32 || H->dim >= (1ll << 31)) return false;
   if (V.nfields < 1 || V.nfields > 2) return false;
@@ -298,7 +298,7 @@ bool ham_build_fx_slots(qd_ham* H) {
   for (const MfEntry& e : off) {
     if (e.amp.im != 0.0 || e.jw != 0) return false;
     if (e.amp.re == 0.0) continue;  // an explicit zero is no column of the uniform form
-    if (e.amp.re != f.c) return false;
+    if (e.amp.re != c) return false;
     const uint32_t sup = (uint32_t)e.sup, outb = (uint32_t)e.outb, flip = (uint32_t)e.flip;
     bool in = true;
     for (int i = 0; i < V.nfields; ++i)
@@ -408,7 +408,7 @@ bool ham_build_fx_slots(qd_ham* H) {
     QD_CUDA(cudaMemcpyAsync(f.dtab.p, dtab.data(), dtab.size() * sizeof(int2), cudaMemcpyHostToDevice,
                             ctx->stream));
   std::memset(&f.rank, 0, sizeof(f.rank));
-  if (!groups.empty()) {
+  if (!groups.empty() || tables) {
     MfRank rk;
     std::memset(&rk, 0, sizeof(rk));
     std::vector<int64_t> tab;
@@ -434,9 +434,32 @@ bool ham_build_fx_slots(qd_ham* H) {
   basis32_kernel<<<slot_grid(ctx, n), 256, 0, ctx->stream>>>(n, H->sec->basis.p, f.basis32.p);
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  return true;
+}
+
+static void drop_slots(FxForm& f) {
+  f.runs.release();
+  f.slots.release();
+  f.dtab.release();
+  f.basis32.release();
+  f.rtab.release();
+  f.nrun = f.nslot = f.ndtab = 0;
+}
+
+bool ham_build_fx_slots(qd_ham* H) {
+  FxForm& f = *H->fx;
+  if (f.slots_state != 0) return f.slots_state > 0;
+  f.slots_state = -1;
+  if (!make_slots(H, f, f.c, false)) {
+    drop_slots(f);
+    return false;
+  }
+  Ctx* ctx = H->ctx;
+  const int64_t n = H->dim;
   DBuf<int> bad(1);
   QD_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), ctx->stream));
-  const FxSlotArgs A = slot_args(H);
+  const FxSlotArgs A = slot_args(H, f);
   fx_slots_check_kernel<<<slot_grid(ctx, n), 256, slot_smem(f), ctx->stream>>>(A, f.rowptr.p, f.colidx.p, bad.p);
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
@@ -444,40 +467,195 @@ bool ham_build_fx_slots(qd_ham* H) {
   QD_CUDA(cudaMemcpyAsync(&hb, bad.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
   if (hb) {
-    f.runs.release();
-    f.slots.release();
-    f.dtab.release();
-    f.basis32.release();
-    f.rtab.release();
-    f.nrun = f.nslot = f.ndtab = 0;
+    drop_slots(f);
     return false;
   }
   f.slots_state = 1;
   return true;
 }
 
-void launch_fx_slots(Ctx* ctx, const qd_ham* H, const double* x, const __int128* X, double* y,
+// ---------------------------------------------------------------- the form without a stored matrix
+// Per row: every column in range, none twice, at most 128; the row bound
+// |c| + ... + |c| (one per column, added in turn) + |d_r|, as the stored-matrix
+// form sums its values, so both give the same scale F.
+__global__ void __launch_bounds__(256) fx_slots_rows_kernel(FxSlotArgs A, double absc, int* bad,
+                                                            unsigned long long* rowmax) {
+  const SlotSmem S = stage_slots(A);
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < A.n; r += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t s = A.basis[r];
+    int cols[128];
+    int cnt = 0;
+    bool ok = true;
+    auto take = [&](int c) {
+      if (c < 0 || (int64_t)c >= A.n || cnt >= 128) {
+        ok = false;
+        return;
+      }
+      for (int i = 0; i < cnt; ++i) ok &= (cols[i] != c);
+      cols[cnt++] = c;
+    };
+    for (int g = 0; g < A.nrun && ok; ++g) {
+      const int2 h = run_hit(S.runs[g], S.dt, A.kk, s);
+      if (h.y) take((int)r + h.x);
+    }
+    for (int g = 0; g < A.nslot && ok; ++g)
+      if (slot_hit(S.slots[g], s)) take((int)rank32(A.R, s ^ S.slots[g].flip));
+    if (!ok) atomicOr(bad, 1);
+    double sum = 0.0;
+    for (int i = 0; i < cnt; ++i) sum += absc;
+    sum += fabs(A.diag[r]);
+    atomicMax(rowmax, (unsigned long long)__double_as_longlong(sum));
+  }
+}
+
+// Colex rank of a field value (the sector's rank of one field), for the host check.
+static int64_t host_colex(uint32_t v, const int64_t (*C)[65]) {
+  int64_t r = 0;
+  int j = 0;
+  for (int p = 0; p < 32; ++p)
+    if ((v >> p) & 1u) {
+      ++j;
+      if (j <= p) r += C[p][j];
+    }
+  return r;
+}
+
+// The run tables against whole-field ranks: for every pattern with a
+// transition and every count m of set bits below the run that a state of the
+// field can have, two states (the remaining set bits just above the run, or
+// at the top of the field) must both move by the tabulated offset.
+static bool check_run_tables(const qd_ham* H, const FxForm& f, const std::vector<uint4>& runs,
+                             const std::vector<int2>& dtab, const std::vector<std::vector<int64_t>>& flips) {
+  const SectorView& V = H->sec->view;
+  int64_t C[65][65];
+  for (int n = 0; n < 65; ++n)
+    for (int k = 0; k < 65; ++k) C[n][k] = (k == 0) ? 1 : (n == 0 ? 0 : C[n - 1][k - 1] + C[n - 1][k]);
+  for (size_t q = 0; q < runs.size() && q < flips.size(); ++q) {
+    const uint4 R = runs[q];
+    int fi = -1;
+    for (int i = 0; i < V.nfields; ++i)
+      if ((int)R.x >= V.fields[i].lo && (int)R.x < V.fields[i].lo + V.fields[i].width) fi = i;
+    if (fi < 0) return false;
+    const Field& F = V.fields[fi];
+    const int a = (int)R.x - F.lo, w = __builtin_popcount(R.y), above = F.width - a - w;
+    for (uint32_t p = 0; p <= R.y; ++p) {
+      if (flips[q][p] < 0) continue;
+      for (int m = 0; m <= a; ++m) {
+        const int rest = F.k - m - __builtin_popcount(p);
+        if (rest < 0 || rest > above) continue;
+        const int2 d = dtab[R.w + p * f.kk + m];
+        if (!d.y) return false;
+        for (int place = 0; place < 2; ++place) {
+          uint32_t v = (m ? ((1u << m) - 1u) : 0u) | (p << a);
+          for (int i = 0; i < rest; ++i) v |= 1u << (place ? (F.width - 1 - i) : (a + w + i));
+          const uint32_t vc = v ^ ((uint32_t)flips[q][p] << a);
+          const int64_t dl = (host_colex(vc, C) - host_colex(v, C)) * F.stride;
+          if (dl != (int64_t)d.x) return false;
+        }
+      }
+    }
+  }
+  return true;
+}
+
+bool ham_build_mf_fx(qd_ham* H) {
+  if (H->mfx_state != 0) return H->mfx_state > 0;
+  H->mfx_state = -1;
+  if (!H->from_terms || !(H->flags & QD_HAM_REAL) || H->dim < 1) return false;
+  ham_build_matrix_free(H);
+  if (!H->mf_real) return false;
+  std::vector<MfEntry> off, dia;
+  compile_terms(H, off, dia);
+  double c = 0.0;
+  for (const MfEntry& e : off)
+    if (e.amp.re != 0.0 || e.amp.im != 0.0) {
+      c = e.amp.re;
+      break;
+    }
+  if (c == 0.0) return false;
+  std::unique_ptr<FxForm> f(new FxForm());
+  f->c = c;
+  if (!make_slots(H, *f, c, true)) return false;
+  // the run tables, checked on the host against whole-field ranks
+  {
+    std::vector<uint4> runs((size_t)f->nrun);
+    std::vector<int2> dtab((size_t)f->ndtab);
+    QD_CUDA(cudaMemcpy(runs.data(), f->runs.p, runs.size() * sizeof(uint4), cudaMemcpyDeviceToHost));
+    QD_CUDA(cudaMemcpy(dtab.data(), f->dtab.p, dtab.size() * sizeof(int2), cudaMemcpyDeviceToHost));
+    std::vector<std::vector<int64_t>> flips(runs.size());
+    for (size_t q = 0; q < runs.size(); ++q) flips[q].assign((size_t)runs[q].y + 1, -1);
+    // recover each run slot's flips from its entries: a pattern with weight 1 took one transition
+    std::vector<int> seen(runs.size(), 0);
+    const SectorView& V = H->sec->view;
+    for (const MfEntry& e : off) {
+      if (e.amp.re != c || e.amp.im != 0.0) continue;
+      bool in = true;  // make_slots keeps only transitions that stay in the sector
+      for (int i = 0; i < V.nfields; ++i) {
+        const uint32_t fm = (uint32_t)((((uint64_t)1 << V.fields[i].width) - 1) << V.fields[i].lo);
+        in &= __builtin_popcount((uint32_t)e.outb & fm) == __builtin_popcount((uint32_t)(e.outb ^ e.flip) & fm);
+      }
+      if (!in) continue;
+      const uint32_t sup = (uint32_t)e.sup;
+      const int lo = __builtin_ctz(sup);
+      for (size_t q = 0; q < runs.size(); ++q) {
+        if ((int)runs[q].x != lo || (runs[q].y << lo) != sup) continue;
+        const uint32_t pat = ((uint32_t)e.outb >> lo) & runs[q].y;
+        if (flips[q][pat] >= 0) continue;  // a later slot of the same support holds it
+        flips[q][pat] = ((uint32_t)e.flip >> lo) & runs[q].y;
+        break;
+      }
+    }
+    if (!check_run_tables(H, *f, runs, dtab, flips)) return false;
+  }
+  Ctx* ctx = H->ctx;
+  const int64_t n = H->dim;
+  f->diag.alloc(n);
+  QD_CUDA(cudaMemcpyAsync(f->diag.p, H->diag_r.p, n * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  DBuf<int> bad(1);
+  DBuf<unsigned long long> rowmax(1);
+  QD_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), ctx->stream));
+  QD_CUDA(cudaMemsetAsync(rowmax.p, 0, sizeof(unsigned long long), ctx->stream));
+  fx_slots_rows_kernel<<<slot_grid(ctx, n), 256, slot_smem(*f), ctx->stream>>>(slot_args(H, *f), std::fabs(c),
+                                                                              bad.p, rowmax.p);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  int hb = 1;
+  unsigned long long rb = 0;
+  QD_CUDA(cudaMemcpyAsync(&hb, bad.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(&rb, rowmax.p, sizeof(rb), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  double rm = 0.0;
+  std::memcpy(&rm, &rb, 8);
+  if (hb || !std::isfinite(rm)) return false;
+  const int eb = (int)std::ceil(std::log2(std::max(1.0, rm))) + 1;  // as ham_build_fx
+  f->F = 119 - eb;
+  f->nnz = 0;
+  f->use_slots = true;
+  f->slots_state = 1;
+  H->mfx = std::move(f);
+  H->mfx_state = 1;
+  return true;
+}
+
+void launch_fx_slots(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x, const __int128* X, double* y,
                      const double* scale_dev, const int* stop, int step) {
-  const FxForm& f = *H->fx;
   const double cF = std::ldexp(f.c, -f.F);
-  spmv_fx_slots_kernel<<<slot_grid(ctx, H->dim), 256, slot_smem(f), ctx->stream>>>(slot_args(H), x, X, y, cF,
+  spmv_fx_slots_kernel<<<slot_grid(ctx, H->dim), 256, slot_smem(f), ctx->stream>>>(slot_args(H, f), x, X, y, cF,
                                                                                     scale_dev, stop, step);
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
 }
 
-void launch_fx_slots_dots(Ctx* ctx, const qd_ham* H, const double* x, const __int128* X, const double* V2,
-                          double* y,
-                          const double* s1, const double* s2, const int* stop, int step, double* beta,
-                          double* alpha, Tri<double>* dots, GridRed<Tri<double>> red, int grid) {
-  const FxForm& f = *H->fx;
+void launch_fx_slots_dots(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x, const __int128* X,
+                          const double* V2, double* y, const double* s1, const double* s2, const int* stop, int step,
+                          double* beta, double* alpha, Tri<double>* dots, GridRed<Tri<double>> red, int grid) {
   const double cF = std::ldexp(f.c, -f.F);
   const size_t sm = slot_smem(f);
   if (V2)
-    spmv_fx_slots_dots_kernel<true><<<grid, 256, sm, ctx->stream>>>(slot_args(H), x, X, V2, y, cF, s1, s2, stop,
+    spmv_fx_slots_dots_kernel<true><<<grid, 256, sm, ctx->stream>>>(slot_args(H, f), x, X, V2, y, cF, s1, s2, stop,
                                                                     step, beta, alpha, dots, red);
   else
-    spmv_fx_slots_dots_kernel<false><<<grid, 256, sm, ctx->stream>>>(slot_args(H), x, X, x, y, cF, s1, s1, stop,
+    spmv_fx_slots_dots_kernel<false><<<grid, 256, sm, ctx->stream>>>(slot_args(H, f), x, X, x, y, cF, s1, s1, stop,
                                                                      step, beta, alpha, dots, red);
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);

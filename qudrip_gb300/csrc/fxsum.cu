@@ -246,15 +246,14 @@ static int fx_dots_grid(Ctx* ctx, int64_t n) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)ctx->num_sms * per_sm));
 }
 
-void launch_fx_dots(Ctx* ctx, const qd_ham* H, const double* x, const __int128* X, const double* V2, double* y,
-                    const double* s1, const double* s2, const int* stop, int step, double* beta, double* alpha,
-                    Tri<double>* dots, GridRed<Tri<double>> red) {
-  const FxForm& f = *H->fx;
+void launch_fx_dots(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x, const __int128* X,
+                    const double* V2, double* y, const double* s1, const double* s2, const int* stop, int step,
+                    double* beta, double* alpha, Tri<double>* dots, GridRed<Tri<double>> red) {
   const double cF = std::ldexp(f.c, -f.F);
   const int g = fx_dots_grid(ctx, H->dim);
   QD_REQUIRE(g <= kMaxGrid, QD_ERR_UNSUPPORTED, "reduction grid exceeds its partials buffer");
   if (f.slots_state > 0 && f.use_slots) {  // same grid: the same reduction tree as below
-    launch_fx_slots_dots(ctx, H, x, X, V2, y, s1, s2, stop, step, beta, alpha, dots, red, g);
+    launch_fx_slots_dots(ctx, H, f, x, X, V2, y, s1, s2, stop, step, beta, alpha, dots, red, g);
     return;
   }
   if (V2)
@@ -273,11 +272,10 @@ __global__ void fx_shadow_kernel(int64_t n, const double* x, __int128* X, int F,
     X[i] = fx_from_double(x[i], F, ovf);
 }
 
-void launch_fx(Ctx* ctx, const qd_ham* H, const double* x, const __int128* X, double* y, const double* scale_dev,
-               const int* stop, int step) {
-  const FxForm& f = *H->fx;
+void launch_fx(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x, const __int128* X, double* y,
+               const double* scale_dev, const int* stop, int step) {
   if (f.slots_state > 0 && f.use_slots) {
-    launch_fx_slots(ctx, H, x, X, y, scale_dev, stop, step);
+    launch_fx_slots(ctx, H, f, x, X, y, scale_dev, stop, step);
     return;
   }
   const double cF = std::ldexp(f.c, -f.F);

@@ -89,6 +89,8 @@ struct qd_ham {
   int fx_state = 0;          // 0 not tried, 1 built, -1 not applicable
   bool fx_allowed = true;    // the Lanczos product uses it when built (kernel code 120)
   std::unique_ptr<qd::FxForm> fx;
+  int mfx_state = 0;                 // the same form built from the terms alone (matrix-free Lanczos)
+  std::unique_ptr<qd::FxForm> mfx;
   // matrix-free form (qd_ham_build_matrix_free)
   bool has_mf = false;
   bool mf_real = false;      // every amplitude and diagonal entry is real
@@ -119,11 +121,12 @@ void ham_build_matrix_free(qd_ham* H);
 void compile_terms(const qd_ham* H, std::vector<MfEntry>& off, std::vector<MfEntry>& dia);
 void build_tables(const qd_sector* S, MfRank& rk, std::vector<int64_t>& tab);
 bool ham_build_fx_slots(qd_ham* H);
+bool ham_build_mf_fx(qd_ham* H);
 bool ham_lower_pull(qd_ham* H);
 void mf_apply_c(qd_ham* H, const cplx* x, cplx* y);
 bool ham_build_fx(qd_ham* H);
-void launch_fx(Ctx* ctx, const qd_ham* H, const double* x, const __int128* X, double* y, const double* scale_dev,
-               const int* stop, int step);
+void launch_fx(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x, const __int128* X, double* y,
+               const double* scale_dev, const int* stop, int step);
 void launch_fx_shadow(Ctx* ctx, int64_t n, const double* x, __int128* X, int F, int* ovf);
 void ham_ensure_row_order(qd_ham* H);
 double ham_norm_inf(qd_ham* H);

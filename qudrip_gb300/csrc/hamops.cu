@@ -129,6 +129,8 @@ void ham_scale(qd_ham* H, cplx s) {
   H->arnoldi.reset();
   H->fx.reset();
   H->fx_state = 0;
+  H->mfx.reset();
+  H->mfx_state = 0;
   H->fx_allowed = true;
   H->has_mf = false;
   H->mf_ent = DBuf<MfEntry>();

@@ -408,6 +408,8 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   const double* s1 = (const double*)scal.p;
   const bool mf = (spmv == QD_SPMV_MATRIX_FREE);
   if (mf) ham_build_matrix_free(H);
+  // code 1: what the matrix-free Lanczos path launches (the slot form with its dots where it applies)
+  const bool mfx = mf && real && H->fx_allowed && ham_build_mf_fx(H);
   // code 0: the product the real Lanczos path launches (the fixed-point form when it applies)
   const bool fxcode = spmv == kSpmvFx || spmv == kSpmvFxSlots;
   const bool fx = real && (fxcode || (spmv == QD_SPMV_CSR && H->fx_allowed)) && ham_build_fx(H);
@@ -423,17 +425,23 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   } choice{fx ? H->fx.get() : nullptr, fx ? H->fx->use_slots : true};
   if (fx && fxcode) H->fx->use_slots = (spmv == kSpmvFxSlots);
   const bool slots = fx && H->fx->use_slots && H->fx->slots_state > 0;
-  DBuf<__int128> X(fx ? n + 32 : 1);
-  if (fx) QD_CUDA(cudaMemsetAsync(X.p, 0, X.bytes(), ctx->stream));
+  DBuf<__int128> X((fx || mfx) ? n + 32 : 1);
+  if (fx || mfx) QD_CUDA(cudaMemsetAsync(X.p, 0, X.bytes(), ctx->stream));
   auto launch = [&]() {
+    if (mfx) {
+      double* d = (double*)scal.p;
+      launch_fx_dots(ctx, H, *H->mfx, (const double*)x.p, X.p, (const double*)z.p, (double*)y.p, s1, s1, nullptr,
+                     0, d + 1, d + 2, reinterpret_cast<Tri<double>*>(d + 6), W.red_tri<double>(2));
+      return;
+    }
     if (fx && spmv == QD_SPMV_CSR) {  // what the recurrence launches: the product fused with its dots
       double* d = (double*)scal.p;
-      launch_fx_dots(ctx, H, (const double*)x.p, X.p, (const double*)z.p, (double*)y.p, s1, s1, nullptr, 0, d + 1,
-                     d + 2, reinterpret_cast<Tri<double>*>(d + 6), W.red_tri<double>(2));
+      launch_fx_dots(ctx, H, *H->fx, (const double*)x.p, X.p, (const double*)z.p, (double*)y.p, s1, s1, nullptr, 0,
+                     d + 1, d + 2, reinterpret_cast<Tri<double>*>(d + 6), W.red_tri<double>(2));
       return;
     }
     if (fx) {
-      launch_fx(ctx, H, (const double*)x.p, X.p, (double*)y.p, nullptr, nullptr, 0);
+      launch_fx(ctx, H, *H->fx, (const double*)x.p, X.p, (double*)y.p, nullptr, nullptr, 0);
       return;
     }
     if (mf) {
@@ -481,6 +489,8 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   *bytes_per_launch = (double)H->nnz * (mvb + 4.0) + (double)(n + 1) * 8.0 + (double)n * 2.0 * (double)vb;
   if (mf)  // basis word, diagonal, x[r], y[r] per row (the gathered x comes from L2)
     *bytes_per_launch = (double)n * (8.0 + (H->mf_real ? 8.0 : 16.0) + 2.0 * (double)vb);
+  if (mfx)  // 32-bit state, diagonal, x, its fixed-point copy once, y, v2
+    *bytes_per_launch = (double)n * (4.0 + 8.0 + 8.0 + 16.0 + 8.0 + 8.0);
   if (fx)  // columns, row pointers (int32), diagonal, x, its fixed-point copy, y (+ v2 for the fused dots)
     *bytes_per_launch = (double)H->fx->nnz * 4.0 + (double)(n + 1) * 4.0 +
                         (double)n * (8.0 + 8.0 + 16.0 + 8.0 + (spmv == QD_SPMV_CSR ? 8.0 : 0.0));
@@ -493,7 +503,7 @@ template <typename MV, typename VV>
 // fxk: 0 the product alone (CSR or matrix-free), then K2; 1 the uniform-
 // coupling form with fixed-point sums fused with the step's inner products.
 static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int k_first, int k_last, Workspace& W,
-                        bool mf, int fxk = 0) {
+                        bool mf, int fxk = 0, const FxForm* form = nullptr) {
   Ctx* ctx = H->ctx;
   const int64_t n = H->dim;
   for (int k = k_first; k <= k_last; ++k) {
@@ -507,7 +517,8 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int k_
     __int128* Xnext = (fxk == 1) ? B.X.p + (int64_t)(k & 1) * B.ld : nullptr;
     if constexpr (std::is_same<VV, double>::value) {  // product fused with the step's inner products
       if (fxk == 1)
-        launch_fx_dots(ctx, H, V1, Xprev, V2, B.w.p, s1, s2, B.stop.p, k, B.beta.p + k, B.alpha.p + k, B.dots.p + k,
+        launch_fx_dots(ctx, H, *form, V1, Xprev, V2, B.w.p, s1, s2, B.stop.p, k, B.beta.p + k, B.alpha.p + k,
+                       B.dots.p + k,
                        W.red_tri<double>(2));
     }
     if (fxk == 0) {
@@ -520,7 +531,7 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int k_
     // K2, K3 (K3 also writes the fixed-point copy of v_k for the next product)
     lz_vector_passes<VV>(ctx, n, B.stop.p, k, B.w.p, V1, V2, s1, s2, B.beta.p + k, B.alpha.p + k, B.dots.p + k, Vk,
                          B.nrm2.p + k, B.nrm.p + k, B.scl.p + k, W.red_tri<VV>(2), W.red_d_flat(3), Xnext,
-                         fxk == 1 ? H->fx->F : 0, fxk == 1 ? B.ovf.p : nullptr, fxk != 0);
+                         fxk == 1 ? form->F : 0, fxk == 1 ? B.ovf.p : nullptr, fxk != 0);
   }
 }
 
@@ -540,8 +551,8 @@ LanczosBuffers<cplx>& buffers_for<cplx>(Workspace& W, int64_t n, int kdim) {
 
 template <typename MV, typename VV>
 static void lanczos_finish(qd_ham* H, cplx* psi, const double* psi_nrm2, const qd_lanczos_opts& o,
-                           LanczosBuffers<VV>& B, Workspace& W, const MV* vals, bool mf, int fxk, int fxF,
-                           double* evals_out, qd_lanczos_result* res);
+                           LanczosBuffers<VV>& B, Workspace& W, const MV* vals, bool mf, int fxk,
+                           const FxForm* form, double* evals_out, qd_lanczos_result* res);
 
 template <typename MV, typename VV>
 static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, const qd_lanczos_opts& o,
@@ -566,12 +577,17 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
   const auto host_t0 = std::chrono::steady_clock::now();
   if (timing) QD_CUDA(cudaEventRecord(ctx->events[12], ctx->stream));
   const bool mf = (o.spmv == QD_SPMV_MATRIX_FREE);
-  int fxk = 0;  // 1: the fixed-point uniform-coupling CSR form fused with the dots (fxsum.cuh)
+  // fxk 1: the fixed-point uniform-coupling form fused with the dots (fxsum.cuh): the stored-matrix
+  // form on the CSR path, the form built from the terms alone on the matrix-free path
+  int fxk = 0;
+  const FxForm* form = nullptr;
   if constexpr (std::is_same<VV, double>::value) {
-    if (!mf && H->fx_allowed && ham_build_fx(H)) fxk = 1;
+    if (!mf && H->fx_allowed && ham_build_fx(H)) form = H->fx.get();
+    if (mf && H->fx_allowed && ham_build_mf_fx(H)) form = H->mfx.get();
   }
+  fxk = form ? 1 : 0;
   const bool fx = fxk == 1;
-  const int fxF = fx ? H->fx->F : 0;
+  const int fxF = fx ? form->F : 0;
   const int kind = (mf ? 1 : 0) + 2 * fxk;
   if (B.kind != kind) {
     B.drop_graph();
@@ -584,9 +600,9 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
   }
   const int steps = (o.add_dim > 0 && o.add_dim < kdim) ? o.add_dim : kdim;  // add_dim of an incremental start
   if (steps == kdim)
-    B.run_graph(ctx, [&]() { lanczos_run<MV, VV>(H, vals, B, 1, kdim, W, mf, fxk); });
+    B.run_graph(ctx, [&]() { lanczos_run<MV, VV>(H, vals, B, 1, kdim, W, mf, fxk, form); });
   else
-    lanczos_run<MV, VV>(H, vals, B, 1, steps, W, mf, fxk);
+    lanczos_run<MV, VV>(H, vals, B, 1, steps, W, mf, fxk, form);
   B.done = steps;
   W.lz_vv = std::is_same<VV, double>::value ? 1 : 2;
   W.lz_mv = std::is_same<MV, double>::value ? 1 : 2;
@@ -604,7 +620,7 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
     }
   }
   if (timing) QD_CUDA(cudaEventRecord(ctx->events[13], ctx->stream));
-  lanczos_finish<MV, VV>(H, psi, psi_nrm2, o, B, W, vals, mf, fxk, fxF, evals_out, res);
+  lanczos_finish<MV, VV>(H, psi, psi_nrm2, o, B, W, vals, mf, fxk, form, evals_out, res);
   if (timing) {
     float g = 0.f;
     QD_CUDA(cudaEventElapsedTime(&g, ctx->events[12], ctx->events[13]));
@@ -619,12 +635,13 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
 // far and the Ritz vector of its lowest level, written to psi.
 template <typename MV, typename VV>
 static void lanczos_finish(qd_ham* H, cplx* psi, const double* psi_nrm2, const qd_lanczos_opts& o,
-                           LanczosBuffers<VV>& B, Workspace& W, const MV* vals, bool mf, int fxk, int fxF,
-                           double* evals_out, qd_lanczos_result* res) {
+                           LanczosBuffers<VV>& B, Workspace& W, const MV* vals, bool mf, int fxk,
+                           const FxForm* form, double* evals_out, qd_lanczos_result* res) {
   Ctx* ctx = H->ctx;
   const int64_t n = H->dim;
   const int kdim = B.done;
   const bool fx = fxk == 1;
+  const int fxF = fx ? form->F : 0;
   const int vg = vec_grid(ctx, n);
   int matvecs = kdim;
 
@@ -658,7 +675,7 @@ static void lanczos_finish(qd_ham* H, cplx* psi, const double* psi_nrm2, const q
       QD_CUDA(cudaMemsetAsync(B.ovf.p, 0, sizeof(int), ctx->stream));
       if constexpr (std::is_same<VV, double>::value) launch_fx_shadow(ctx, n, B.V.p, B.X.p, fxF, B.ovf.p);
     }
-    lanczos_run<MV, VV>(H, vals, B, 1, act, W, mf, fxk);
+    lanczos_run<MV, VV>(H, vals, B, 1, act, W, mf, fxk, form);
     matvecs += act;
   }
   // psi = sum_k y_k v_k = sum_k (y_k s_k) V[k]
@@ -696,8 +713,9 @@ static void lanczos_extend_impl(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, 
   QD_CUDA(cudaMemcpyAsync(&stop, B.stop.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
   const int add = (o.add_dim > 0) ? std::min(o.add_dim, B.kdim - B.done) : B.kdim - B.done;
+  const FxForm* form = W.lz_fxk == 1 ? (W.lz_mf ? H->mfx.get() : H->fx.get()) : nullptr;
   if (!stop && add > 0) {
-    lanczos_run<MV, VV>(H, vals, B, B.done + 1, B.done + add, W, W.lz_mf, W.lz_fxk);
+    lanczos_run<MV, VV>(H, vals, B, B.done + 1, B.done + add, W, W.lz_mf, W.lz_fxk, form);
     B.done += add;
   }
   if (W.lz_fxk == 1) {
@@ -708,8 +726,7 @@ static void lanczos_extend_impl(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, 
   }
   qd_lanczos_opts o2 = o;
   o2.ritz = QD_RITZ_STORED_BASIS;
-  lanczos_finish<MV, VV>(H, psi, nullptr, o2, B, W, vals, W.lz_mf, W.lz_fxk, W.lz_fxk == 1 ? H->fx->F : 0,
-                         evals_out, res);
+  lanczos_finish<MV, VV>(H, psi, nullptr, o2, B, W, vals, W.lz_mf, W.lz_fxk, form, evals_out, res);
 }
 
 void lanczos_extend(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, double* evals_out, qd_lanczos_result* res) {

@@ -135,14 +135,14 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
 void lanczos_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int m, int nsteps, int* act_out,
                     int64_t* matvecs_out);
 void hermitian_lanczos_ground(qd_ham* H, cplx* psi, int kdim, double* evals_out, qd_lanczos_result* res);
-void launch_fx_dots(Ctx* ctx, const qd_ham* H, const double* x, const __int128* X, const double* V2, double* y,
-                    const double* s1, const double* s2, const int* stop, int step, double* beta, double* alpha,
-                    Tri<double>* dots, GridRed<Tri<double>> red);
-void launch_fx_slots(Ctx* ctx, const qd_ham* H, const double* x, const __int128* X, double* y,
+void launch_fx_dots(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x, const __int128* X,
+                    const double* V2, double* y, const double* s1, const double* s2, const int* stop, int step,
+                    double* beta, double* alpha, Tri<double>* dots, GridRed<Tri<double>> red);
+void launch_fx_slots(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x, const __int128* X, double* y,
                      const double* scale_dev, const int* stop, int step);
-void launch_fx_slots_dots(Ctx* ctx, const qd_ham* H, const double* x, const __int128* X, const double* V2,
-                          double* y, const double* s1, const double* s2, const int* stop, int step, double* beta,
-                          double* alpha, Tri<double>* dots, GridRed<Tri<double>> red, int grid);
+void launch_fx_slots_dots(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x, const __int128* X,
+                          const double* V2, double* y, const double* s1, const double* s2, const int* stop, int step,
+                          double* beta, double* alpha, Tri<double>* dots, GridRed<Tri<double>> red, int grid);
 template <typename VV>
 void launch_mf(Ctx* ctx, qd_ham* H, const VV* x, VV* y, double scale, const double* scale_dev, const int* stop,
                int step);

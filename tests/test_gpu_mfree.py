@@ -91,3 +91,63 @@ def test_matrix_free_lanczos_xxz24_energy(ctx, golden):
     p2.set(0, v0)
     rc = q.LanczosSolver(sec, 100).getGroundState(Hc, p2, 0)
     assert abs(r.ritz_value - rc.ritz_value) <= 1e-11 * abs(e0)
+
+
+def _lanczos(sec, H, v0, kry, spmv=A.QD_SPMV_CSR, kernel=None):
+    if kernel is not None:
+        A.call("qd_ham_set_spmv_kernel", H.handle, kernel)
+    psi = q.getState(sec, 1)
+    psi.set(0, v0)
+    r = q.LanczosSolver(sec, kry, spmv=spmv).getGroundState(H, psi, 0)
+    return r, psi.get(0)
+
+
+def _mf_bytes(H):
+    import ctypes as C
+    ms, nb = C.c_double(), C.c_double()
+    A.call("qd_ham_time_spmv", H.handle, A.QD_SPMV_MATRIX_FREE, 2, C.byref(ms), C.byref(nb))
+    return nb.value
+
+
+@pytest.mark.parametrize("case", ["xxz16", "xy14_open", "two_species"])
+def test_matrix_free_uniform_form_bit_identical_to_csr(ctx, case):
+    """Uniform couplings on the matrix-free path take the slot form built from the terms alone (no stored
+    matrix: offsets checked on the host against whole-field ranks, rows checked on the device); its
+    recurrence is bit-identical to the stored-matrix forms (codes 120 and 121)."""
+    from test_gpu_fx import two_species_xy
+    spec, ham = {"xxz16": lambda: chains.xxz_chain(16, 1.0, 0.8, periodic=True,
+                                                   fields=np.linspace(-1, 1, 16)),
+                 "xy14_open": lambda: chains.xy_chain(14),
+                 "two_species": lambda: two_species_xy(6, True)}[case]()
+    sec, H = gpu_objects(spec, ham)
+    v0 = q.start_vector(sec.dim, 31)
+    r_mf, p_mf = _lanczos(sec, H, v0, 80, spmv=A.QD_SPMV_MATRIX_FREE)
+    assert _mf_bytes(H) == sec.dim * (4 + 8 + 8 + 16 + 8 + 8)  # the slot form, not the FP64 matrix-free product
+    r_120, p_120 = _lanczos(sec, H, v0, 80, kernel=A.QD_SPMV_FX)
+    r_121, p_121 = _lanczos(sec, H, v0, 80, kernel=A.QD_SPMV_FX_SLOTS)
+    assert r_mf.ritz_value == r_120.ritz_value == r_121.ritz_value
+    assert np.array_equal(p_mf, p_120) and np.array_equal(p_mf, p_121)
+    o = O.Ham(O.Sector(spec), ham).lanczos_ground(v0, 80)
+    assert abs(r_mf.ritz_value - o["ritz"]) <= 1e-10 * abs(o["ritz"])
+
+
+def test_matrix_free_nonuniform_keeps_fp64_product(ctx):
+    """Bond-dependent couplings: no single off-diagonal value, so the matrix-free path stays on the FP64
+    product of the compiled transitions (8-byte basis words), and agrees with the CSR path."""
+    L = 12
+    pre = q.getQbits(L)
+    gc, ga = q.getBoseGate(pre), q.getBoseGate(pre)
+    gc << 0.5 * (q.pauli_x + q.II * q.pauli_y)
+    ga << 0.5 * (q.pauli_x - q.II * q.pauli_y)
+    J = np.random.default_rng(5).uniform(0.5, 1.5, L)
+    ham = q.getEmptyOperator()
+    for i in range(L):
+        j = (i + 1) % L
+        ham = ham + float(J[i]) * (gc(i) * ga(j)) + float(J[i]) * (gc(j) * ga(i))
+    spec = q.SectorSpec(pre, [q.getNset(pre) == L // 2])
+    sec, H = gpu_objects(spec, ham)
+    v0 = q.start_vector(sec.dim, 8)
+    r_mf, _ = _lanczos(sec, H, v0, 60, spmv=A.QD_SPMV_MATRIX_FREE)
+    assert _mf_bytes(H) == sec.dim * (8 + 8 + 8 + 8)
+    r_csr, _ = _lanczos(sec, H, v0, 60)
+    assert abs(r_mf.ritz_value - r_csr.ritz_value) <= 1e-12 * abs(r_csr.ritz_value)
