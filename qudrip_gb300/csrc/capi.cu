@@ -603,7 +603,7 @@ qd_status qd_ham_set_spmv_kernel(qd_ham* ham, int kernel) {
     DeviceGuard dg(ham->ctx->device);
     if (kernel == kSpmvFx || kernel == kSpmvFxSlots) {
       QD_REQUIRE(ham_build_fx(ham), QD_ERR_UNSUPPORTED, "the fixed-point form does not apply to this operator");
-      QD_REQUIRE(kernel == kSpmvFx || ham->fx->slots_state > 0, QD_ERR_UNSUPPORTED,
+      QD_REQUIRE(kernel == kSpmvFx || ham_build_fx_slots(ham), QD_ERR_UNSUPPORTED,
                  "the columns of this operator cannot be computed on the fly (code 121)");
       ham->fx->use_slots = (kernel == kSpmvFxSlots);
       ham->fx_allowed = true;
@@ -638,7 +638,7 @@ qd_status qd_ham_autotune(qd_ham* ham, int iters, int* chosen, double* best_ms) 
       const bool slots0 = ham->fx->use_slots;
       int fx_pick = 0;
       for (int v = kSpmvFx; v <= kSpmvFxSlots; ++v) {
-        if (v == kSpmvFxSlots && ham->fx->slots_state <= 0) continue;
+        if (v == kSpmvFxSlots && !ham_build_fx_slots(ham)) continue;
         double ms = 0;
         ham->fx_allowed = true;
         ham->fx->use_slots = (v == kSpmvFxSlots);

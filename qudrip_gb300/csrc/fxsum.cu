@@ -148,7 +148,6 @@ bool ham_build_fx(qd_ham* H) {
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
   H->fx = std::move(fx);
   H->fx_state = 1;
-  ham_build_fx_slots(H);  // columns on the fly where the operator's terms allow it
   return true;
 }
 

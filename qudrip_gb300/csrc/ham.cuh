@@ -105,6 +105,7 @@ struct qd_ham {
   std::vector<qd_term> host_terms;
   std::vector<qd_gate> host_gates;
   bool from_terms = false;  // the values are the lowering of host_terms (not a sum or a multiple of matrices)
+  bool one_shot = false;    // solved once (a served request): launch directly instead of capturing a graph
   std::unique_ptr<qd::Workspace, qd::WorkspaceDeleter> ws;  // solver buffers, reused across calls
   std::unique_ptr<qd::ArnoldiBuffers, qd::ArnoldiDeleter> arnoldi;
 };
@@ -130,4 +131,5 @@ void launch_fx(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x, cons
 void launch_fx_shadow(Ctx* ctx, int64_t n, const double* x, __int128* X, int F, int* ovf);
 void ham_ensure_row_order(qd_ham* H);
 double ham_norm_inf(qd_ham* H);
+double ham_gershgorin_halfwidth(qd_ham* H);
 }  // namespace qd

@@ -386,6 +386,30 @@ double state_norm2(qd_ham* H, const cplx* psi) {
   return h;
 }
 
+// psi^dagger psi and psi^dagger H psi with one wait for both (a served result).
+void state_norm2_eval(qd_ham* H, const cplx* psi, double* n2, cplx* e) {
+  Ctx* ctx = H->ctx;
+  Workspace& W = ham_workspace(H);
+  DBuf<char> out(64);
+  DBuf<cplx> tmp(H->dim + 1);
+  double* nrm2 = reinterpret_cast<double*>(out.p);
+  int* has_im = reinterpret_cast<int*>(out.p + 8);
+  cplx* hv = reinterpret_cast<cplx*>(out.p + 16);
+  QD_CUDA(cudaMemsetAsync(has_im, 0, sizeof(int), ctx->stream));
+  colnorm_kernel<<<vec_grid(ctx, H->dim), kVecThreads, 0, ctx->stream>>>(H->dim, psi, nrm2, W.red_d(0), has_im);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  if (H->flags & QD_HAM_REAL)
+    launch_spmv<double, cplx>(ctx, H, H->vals_r.p, psi, tmp.p, 1.0, psi, W.red_c(0), hv, nullptr, 0, -1);
+  else
+    launch_spmv<cplx, cplx>(ctx, H, H->vals_c.p, psi, tmp.p, 1.0, psi, W.red_c(0), hv, nullptr, 0, -1);
+  char host[32];
+  QD_CUDA(cudaMemcpyAsync(host, out.p, sizeof(host), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::memcpy(n2, host, sizeof(double));
+  std::memcpy(e, host + 16, sizeof(cplx));
+}
+
 // The product the real Lanczos path launches, timed back to back.
 void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per_launch) {
   Ctx* ctx = H->ctx;
@@ -414,7 +438,7 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   const bool fxcode = spmv == kSpmvFx || spmv == kSpmvFxSlots;
   const bool fx = real && (fxcode || (spmv == QD_SPMV_CSR && H->fx_allowed)) && ham_build_fx(H);
   QD_REQUIRE(!fxcode || fx, QD_ERR_UNSUPPORTED, "the fixed-point form does not apply to this operator");
-  QD_REQUIRE(spmv != kSpmvFxSlots || H->fx->slots_state > 0, QD_ERR_UNSUPPORTED,
+  QD_REQUIRE(spmv != kSpmvFxSlots || ham_build_fx_slots(H), QD_ERR_UNSUPPORTED,
              "the columns of this operator cannot be computed on the fly (code 121)");
   struct SlotChoice {  // 120 / 121 pick the column source for this timing only
     FxForm* f;
@@ -599,7 +623,7 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
     if constexpr (std::is_same<VV, double>::value) launch_fx_shadow(ctx, n, B.V.p, B.X.p, fxF, B.ovf.p);
   }
   const int steps = (o.add_dim > 0 && o.add_dim < kdim) ? o.add_dim : kdim;  // add_dim of an incremental start
-  if (steps == kdim)
+  if (steps == kdim && !H->one_shot)
     B.run_graph(ctx, [&]() { lanczos_run<MV, VV>(H, vals, B, 1, kdim, W, mf, fxk, form); });
   else
     lanczos_run<MV, VV>(H, vals, B, 1, steps, W, mf, fxk, form);
@@ -1052,29 +1076,35 @@ static void lanczos_evolve_steps(qd_ham* H, cplx* psi, double h, int m, int nste
     B.drop_graph();
     B.kind = 0;
   }
-  if (!G.exec || G.psi != psi || G.h != h || G.m != m || G.mv_kind != mv_kind) {
+  const int vg = vec_grid(ctx, n);
+  // one Krylov step: psi <- exp(-ih H) psi through the short recurrence
+  auto step = [&]() {
+    QD_CUDA(cudaMemsetAsync(B.stop.p, 0, sizeof(int), ctx->stream));
+    colnorm_kernel<<<vg, kVecThreads, 0, ctx->stream>>>(n, psi, G.nrm2.p, W.red_d(0), G.has_im.p);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+    init_v0_kernel<cplx><<<vg, kVecThreads, 0, ctx->stream>>>(n, psi, G.nrm2.p, B.V.p);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+    lanczos_run<MV, cplx>(H, vals, B, 1, kdim, W, false);
+    texp_kernel<<<1, 32, 0, ctx->stream>>>(kdim, h, B.alpha.p, B.nrm.p, B.scl.p, B.stop.p, G.y.p, G.act.p,
+                                           G.matvecs.p);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+    combine_dev_kernel<<<vg, kVecThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, G.y.p, G.act.p, psi);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+  };
+  if (H->one_shot) {  // solved once: capturing a graph would cost more than it saves
+    for (int s = 0; s < nsteps; ++s) step();
+  } else if (!G.exec || G.psi != psi || G.h != h || G.m != m || G.mv_kind != mv_kind) {
     if (G.exec) cudaGraphExecDestroy(G.exec);
     G.exec = nullptr;
-    const int vg = vec_grid(ctx, n);
     cudaGraph_t g = nullptr;
     const int64_t before = ctx->launches;
     QD_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     try {
-      QD_CUDA(cudaMemsetAsync(B.stop.p, 0, sizeof(int), ctx->stream));
-      colnorm_kernel<<<vg, kVecThreads, 0, ctx->stream>>>(n, psi, G.nrm2.p, W.red_d(0), G.has_im.p);
-      QD_CHECK_LAUNCH();
-      QD_LAUNCHED(ctx);
-      init_v0_kernel<cplx><<<vg, kVecThreads, 0, ctx->stream>>>(n, psi, G.nrm2.p, B.V.p);
-      QD_CHECK_LAUNCH();
-      QD_LAUNCHED(ctx);
-      lanczos_run<MV, cplx>(H, vals, B, 1, kdim, W, false);
-      texp_kernel<<<1, 32, 0, ctx->stream>>>(kdim, h, B.alpha.p, B.nrm.p, B.scl.p, B.stop.p, G.y.p, G.act.p,
-                                             G.matvecs.p);
-      QD_CHECK_LAUNCH();
-      QD_LAUNCHED(ctx);
-      combine_dev_kernel<<<vg, kVecThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, G.y.p, G.act.p, psi);
-      QD_CHECK_LAUNCH();
-      QD_LAUNCHED(ctx);
+      step();
     } catch (...) {
       cudaStreamEndCapture(ctx->stream, &g);
       if (g) cudaGraphDestroy(g);
@@ -1092,10 +1122,11 @@ static void lanczos_evolve_steps(qd_ham* H, cplx* psi, double h, int m, int nste
     G.m = m;
     G.mv_kind = mv_kind;
   }
-  for (int s = 0; s < nsteps; ++s) {
-    QD_CUDA(cudaGraphLaunch(G.exec, ctx->stream));
-    ctx->launches += G.kernels;
-  }
+  if (!H->one_shot)
+    for (int s = 0; s < nsteps; ++s) {
+      QD_CUDA(cudaGraphLaunch(G.exec, ctx->stream));
+      ctx->launches += G.kernels;
+    }
   int act = 0;
   long long mv = 0;
   QD_CUDA(cudaMemcpyAsync(&act, G.act.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));

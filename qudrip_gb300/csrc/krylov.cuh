@@ -128,6 +128,7 @@ Workspace& ham_workspace(qd_ham* H);
 void ham_apply_c(qd_ham* H, const cplx* x, cplx* y);
 cplx state_eval(qd_ham* H, const cplx* psi);
 double state_norm2(qd_ham* H, const cplx* psi);
+void state_norm2_eval(qd_ham* H, const cplx* psi, double* n2, cplx* e);
 void obs_eval_many(qd_ham* const* obs, int nobs, const cplx* psi, cplx* out_host);
 void lanczos_ground(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, double* evals_out, qd_lanczos_result* res);
 void lanczos_extend(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, double* evals_out, qd_lanczos_result* res);

@@ -442,6 +442,49 @@ double ham_norm_inf(qd_ham* H) {
   return v;
 }
 
+// Gershgorin interval of the real parts: per row [Re d - R, Re d + R] with R
+// the sum of |off-diagonal| values; keys order doubles as unsigned integers.
+__device__ __forceinline__ unsigned long long ordered_key(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__host__ __device__ inline double from_ordered_key(unsigned long long k) {
+  const unsigned long long b = (k >> 63) ? (k & 0x7fffffffffffffffull) : ~k;
+  double x;
+  memcpy(&x, &b, 8);
+  return x;
+}
+__global__ void gershgorin_kernel(int64_t n, const int64_t* rowptr, const int32_t* colidx, const cplx* vals,
+                                  unsigned long long* lo_neg, unsigned long long* hi) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    double d = 0.0, R = 0.0;
+    for (int64_t k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+      if (colidx[k] == (int32_t)r) d = vals[k].re;
+      else R += hypot(vals[k].re, vals[k].im);
+    }
+    atomicMax(hi, ordered_key(d + R));
+    atomicMax(lo_neg, ordered_key(-(d - R)));
+  }
+}
+
+// Half the width of the Gershgorin interval: for Hermitian H,
+// ||H - c I||_2 <= this, c the interval's centre.
+double ham_gershgorin_halfwidth(qd_ham* H) {
+  Ctx* ctx = H->ctx;
+  if (H->dim <= 0) return 0.0;
+  DBuf<unsigned long long> m(2);
+  QD_CUDA(cudaMemsetAsync(m.p, 0, 2 * sizeof(unsigned long long), ctx->stream));
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(H->dim, 256), (int64_t)ctx->num_sms * 8));
+  gershgorin_kernel<<<g, 256, 0, ctx->stream>>>(H->dim, H->rowptr.p, H->colidx.p, H->vals_c.p, m.p, m.p + 1);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  unsigned long long k[2] = {0, 0};
+  QD_CUDA(cudaMemcpyAsync(k, m.p, sizeof(k), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  const double lo = -from_ordered_key(k[0]), hi = from_ordered_key(k[1]);
+  return 0.5 * (hi - lo);
+}
+
 void ham_ensure_row_order(qd_ham* H) {
   if (H->row_order.p) return;
   const int64_t n = H->dim;

@@ -261,6 +261,7 @@ static void build_request(Ctx* ctx, ServeReq* r, Built& b) {
   b.H = new qd_ham();
   b.H->ctx = ctx;
   b.H->sec = b.sec;
+  b.H->one_shot = true;
   ham_lower(b.H, r->terms.data(), (int)r->terms.size(), r->gates.data(), (int)r->gates.size());
 }
 
@@ -315,12 +316,15 @@ static void run_single(qd_server* S, Lane* L, ServeReq* r, Built* prebuilt) {
       int act = 0;
       if (fast) {
         // Integrate to T = nsteps * dt with the mixed form's own Krylov step:
-        // m = 32 and h = T / n with n = ceil(T ||H||_inf / 8), so that
-        // ||H h|| <= 8 = m / 4 and the Krylov error bound (e ||Hh|| / 2m)^m
-        // stays below 1e-15 per step; the requested (dt, m) is kept when it is
-        // the coarser of the two.
+        // m = 32 and h = T / n with n = ceil(T w / 8), w the half-width of
+        // H's Gershgorin interval.  The Krylov space of H and of H - cI are
+        // the same and exp(-ih(H - cI)) = exp(ihc) exp(-ihH), so the error
+        // bound (e ||h(H - cI)|| / 2m)^m holds for the centre c, with
+        // ||H - cI|| <= w <= ||H||_inf: ||h(H - cI)|| <= 8 = m / 4 keeps it
+        // below 1e-15 per step.  The requested (dt, m) is kept when it is the
+        // coarser of the two.
         const double T = r->d.dt * r->d.nsteps;
-        const double hn = ham_norm_inf(H);
+        const double hn = ham_gershgorin_halfwidth(H);
         int nint = std::max(1, (int)std::ceil(std::fabs(T) * hn / 8.0));
         double h = r->d.dt;
         int m = r->d.krylov_dim, steps = r->d.nsteps;
@@ -345,8 +349,9 @@ static void run_single(qd_server* S, Lane* L, ServeReq* r, Built* prebuilt) {
       t_solved = S->now();
     }
     recharge(S, r, held_bytes(b.sec, H) + (int64_t)psi.bytes());
-    const double n2 = state_norm2(H, psi.p);
-    const cplx e = state_eval(H, psi.p);
+    double n2 = 0.0;
+    cplx e = mkc(0.0, 0.0);
+    state_norm2_eval(H, psi.p, &n2, &e);
     res.norm = std::sqrt(n2);
     res.energy = e.re / n2;
     res.matvecs += 1;
