@@ -385,7 +385,7 @@ def gpu_arm(args, rank, world, local):
 
 
 def matrix_free_leg(ctx, H, sec, psi, ritz_csr):
-    """Config 2's second product: the same L=24 Lanczos solve through the
+    """The L=24 XXZ workload's second product: the same Lanczos solve through the
     matrix-free form (no stored matrix), timed, and checked against the FP64
     reference energy (scipy eigsh, tests/golden) and the CSR-path Ritz value."""
     import qudrip_gb300 as q

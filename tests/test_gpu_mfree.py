@@ -78,7 +78,7 @@ def test_matrix_free_lanczos_xy16_matches_oracle(ctx):
 
 
 def test_matrix_free_lanczos_xxz24_energy(ctx, golden):
-    """Config-2 size: XXZ L=24 periodic, Sz=0 (dim 2,704,156), matrix-free FP64 Lanczos."""
+    """Full size: XXZ L=24 periodic, Sz=0 (dim 2,704,156), matrix-free Lanczos."""
     spec, ham = chains.xxz_chain(24, 1.0, 1.0, periodic=True)
     n = 2704156
     v0 = q.start_vector(n, 7)

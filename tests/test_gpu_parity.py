@@ -169,7 +169,7 @@ def check_energies(oh, ores, solver, res, gpsi, E):
     assert res.act_dim == ores["act_dim"] and res.breakdown == ores["breakdown"]
 
 
-def test_lanczos_xy16_config1(ctx, golden):
+def test_lanczos_xy16_open_chain(ctx, golden):
     spec, ham = chains.xy_chain(16)
     oh, ores, gh, solver, res, gpsi, E = lanczos_pair(spec, ham, 100, 12345)
     check_energies(oh, ores, solver, res, gpsi, E)
@@ -221,7 +221,7 @@ def test_second_pass_equals_stored_basis(ctx):
     assert out[1][1] == out[0][1] + 50
 
 
-def test_xxz_L24_config2_full_size(ctx, golden):
+def test_xxz_L24_periodic_full_size(ctx, golden):
     spec, ham = chains.xxz_chain(24, 1.0, 1.0, True)
     gsec, gh = gpu_objects(spec, ham)
     dim, nnz = golden["xxz_periodic_dim_nnz"]["24"]
