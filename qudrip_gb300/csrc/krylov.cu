@@ -153,7 +153,10 @@ __global__ void __launch_bounds__(kLzThreads, kLzBlocksPerSm)
 
 // K3: V[k] = (w - (beta s2) V2) - (alpha s1) V1   (the reference's two
 // subtractions in its order);  n_k = ||V[k]||, s_k = 1 / n_k, stop if n_k < 1e-10.
-template <typename VV, bool kHas2>
+// kShadow: also write the fixed-point copy X of V[k] that the next product
+// gathers (with evict-first stores of V[k], so that X stays in L2), and raise
+// *ovf once if an element left the fixed-point range.
+template <typename VV, bool kHas2, bool kShadow>
 __global__ void __launch_bounds__(kLzThreads, kLzBlocksPerSm)
     lz_update_kernel(int64_t n, int* stop, int step, const VV* __restrict__ w, const VV* __restrict__ V1,
                      const VV* __restrict__ V2, const double* s1, const double* s2, const VV* alpha,
@@ -166,6 +169,7 @@ __global__ void __launch_bounds__(kLzThreads, kLzBlocksPerSm)
   const int64_t np = n / P::kPer;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   double acc0 = 0.0, acc1 = 0.0;
+  int out = 0;
   int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   for (; p + stride < np; p += 2 * stride) {
     typename P::T o0 = P::load_last(w, p), o1 = P::load_last(w, p + stride);
@@ -177,11 +181,11 @@ __global__ void __launch_bounds__(kLzThreads, kLzBlocksPerSm)
     }
     o0 = P::submul(o0, a, a0);
     o1 = P::submul(o1, a, a1);
-    if (Xk) {  // the next product gathers X, not v_k: keep X in L2
+    if (kShadow) {
       P::store_stream(Vk, p, o0);
       P::store_stream(Vk, p + stride, o1);
-      P::shadow(Xk, p, o0, F, ovf);
-      P::shadow(Xk, p + stride, o1, F, ovf);
+      P::shadow(Xk, p, o0, F, &out);
+      P::shadow(Xk, p + stride, o1, F, &out);
     } else {
       P::store(Vk, p, o0);
       P::store(Vk, p + stride, o1);
@@ -194,7 +198,7 @@ __global__ void __launch_bounds__(kLzThreads, kLzBlocksPerSm)
     if (kHas2) o0 = P::submul(o0, b, P::load_last(V2, p));
     o0 = P::submul(o0, a, P::load(V1, p));
     P::store(Vk, p, o0);
-    if (Xk) P::shadow(Xk, p, o0, F, ovf);
+    if (kShadow) P::shadow(Xk, p, o0, F, &out);
     acc0 = P::nrm(o0, acc0);
   }
   if (P::kPer == 2 && (n & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -202,9 +206,10 @@ __global__ void __launch_bounds__(kLzThreads, kLzBlocksPerSm)
     if (kHas2) o = vsubmul(o, b, V2[n - 1]);
     o = vsubmul(o, a, V1[n - 1]);
     Vk[n - 1] = o;
-    if (Xk) shadow_one(Xk, n - 1, o, F, ovf);
+    if (kShadow) shadow_one(Xk, n - 1, o, F, &out);
     acc0 += vnorm2(o);
   }
+  if (kShadow && out) *ovf = 1;
   if (grid_sum(acc0 + acc1, red, nrm2) && threadIdx.x == 0) {
     const double nr = sqrt(*nrm2);
     *nrm = nr;
@@ -227,8 +232,12 @@ static void lz_vector_passes(Ctx* ctx, int64_t n, int* stop, int step, const VV*
       QD_CHECK_LAUNCH();
       QD_LAUNCHED(ctx);
     }
-    lz_update_kernel<VV, true><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V2, s1, s2, alpha, beta, Vk,
-                                                                  nrm2, nrm, sk, rd, Xk, F, ovf);
+    if (Xk)
+      lz_update_kernel<VV, true, true><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V2, s1, s2, alpha,
+                                                                          beta, Vk, nrm2, nrm, sk, rd, Xk, F, ovf);
+    else
+      lz_update_kernel<VV, true, false><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V2, s1, s2, alpha,
+                                                                           beta, Vk, nrm2, nrm, sk, rd, Xk, F, ovf);
   } else {
     if (!dots_done) {
       lz_dots_kernel<VV, false><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V1, s1, s1, beta, alpha,
@@ -236,8 +245,13 @@ static void lz_vector_passes(Ctx* ctx, int64_t n, int* stop, int step, const VV*
       QD_CHECK_LAUNCH();
       QD_LAUNCHED(ctx);
     }
-    lz_update_kernel<VV, false><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V1, s1, s1, alpha, beta,
-                                                                   Vk, nrm2, nrm, sk, rd, Xk, F, ovf);
+    if (Xk)
+      lz_update_kernel<VV, false, true><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V1, s1, s1, alpha,
+                                                                           beta, Vk, nrm2, nrm, sk, rd, Xk, F, ovf);
+    else
+      lz_update_kernel<VV, false, false><<<g, kLzThreads, 0, ctx->stream>>>(n, stop, step, w, V1, V1, s1, s1,
+                                                                            alpha, beta, Vk, nrm2, nrm, sk, rd, Xk,
+                                                                            F, ovf);
   }
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
@@ -484,7 +498,7 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
             n, nullptr, 0, (const double*)y.p, (const double*)x.p, (const double*)z.p, s1, s1, d + 1, d + 2,
             reinterpret_cast<Tri<double>*>(d + 6), W.red_tri<double>(2));
       else
-        lz_update_kernel<double, true><<<g, kLzThreads, 0, ctx->stream>>>(
+        lz_update_kernel<double, true, false><<<g, kLzThreads, 0, ctx->stream>>>(
             n, nullptr, 0, (const double*)y.p, (const double*)x.p, (const double*)z.p, s1, s1, d + 1, d + 2,
             (double*)t.p, d + 3, d + 4, d + 5, W.red_d(3), nullptr, 0, nullptr);
       QD_CHECK_LAUNCH();
