@@ -1,0 +1,93 @@
+"""Edge cases of the device path: an empty sector, a one-state sector, argument limits, and a
+sector whose Krylov space closes after one step.  The reference has no tests of its own; where its
+behaviour is undefined (a 0 x 0 Lanczos matrix) the engine reports an error code instead."""
+import numpy as np
+import pytest
+
+import oracle as O
+import qudrip_gb300 as q
+from qudrip_gb300 import _capi as A
+from qudrip_gb300 import chains
+
+pytestmark = pytest.mark.gpu
+
+
+def sector(spec):
+    return q.Sector(spec.index, spec.constraints, spec.tight)
+
+
+def test_empty_sector(ctx):
+    spec, ham = chains.xxz_chain(8, 1.0, 1.0, periodic=True)
+    pre = spec.index
+    empty = q.SectorSpec(pre, [q.getNset(pre) == 9])  # more particles than sites: no state
+    sec = sector(empty)
+    assert sec.dim == 0 and len(sec.basis()) == 0
+    H = sec.lower(ham)
+    assert H.dim == 0 and H.nnz == 0
+    with pytest.raises(A.QDError) as e:
+        q.getState(sec, 1)
+    assert e.value.code == A.QD_ERR_INVALID
+    assert (H + H).nnz == 0
+
+
+def test_one_state_sector(ctx):
+    L = 6
+    h = np.linspace(-1.0, 1.0, L)
+    spec, ham = chains.xxz_chain(L, 1.0, 0.5, periodic=True, fields=h)
+    pre = spec.index
+    vac = q.SectorSpec(pre, [q.getNset(pre) == 0])  # the empty chain only
+    sec = sector(vac)
+    assert sec.dim == 1 and list(sec.basis()) == [0]
+    H = sec.lower(ham)
+    E = H.scipy().toarray()[0, 0].real
+    o = O.Ham(O.Sector(vac), ham)
+    assert o.scipy().toarray()[0, 0] == E  # bit for bit
+    psi = q.getState(sec, 1)
+    psi.set(0, np.array([1.0 + 0j]))
+    assert psi.eval(0, H).real == E
+    # the first Lanczos step already closes the space: the reference's act_dim would be 0
+    with pytest.raises(A.QDError) as e:
+        q.LanczosSolver(sec, 10).getGroundState(H, psi, 0)
+    assert e.value.code == A.QD_ERR_BREAKDOWN
+
+
+def test_two_state_sector_closes_after_one_step(ctx):
+    """Two sites, one particle: dim 2.  With the start vector an eigenvector the space closes at the
+    first step (the oracle fails the same way); otherwise it closes at the second, and expandBasis<1>
+    returns step - 1 = 1, so the Ritz value is the start vector's Rayleigh quotient, as in the oracle."""
+    spec, ham = chains.xy_chain(2)
+    sec = sector(spec)
+    assert sec.dim == 2
+    H = sec.lower(ham)
+    psi = q.getState(sec, 1)
+    v0 = np.array([1.0, 1.0]) / np.sqrt(2.0)  # eigenvector of the hop (energy +1)
+    psi.set(0, v0.astype(np.complex128))
+    with pytest.raises(A.QDError) as e:
+        q.LanczosSolver(sec, 5).getGroundState(H, psi, 0)
+    assert e.value.code == A.QD_ERR_BREAKDOWN
+    v1 = np.array([1.0, 0.3])
+    psi.set(0, (v1 / np.linalg.norm(v1)).astype(np.complex128))
+    r = q.LanczosSolver(sec, 5).getGroundState(H, psi, 0)
+    o = O.Ham(O.Sector(spec), ham).lanczos_ground(v1 / np.linalg.norm(v1), 5)
+    assert r.act_dim == o["act_dim"] == 1
+    assert abs(r.ritz_value - 0.6 / 1.09) < 1e-15 and abs(o["ritz"] - r.ritz_value) < 1e-15
+
+
+def test_argument_limits(ctx):
+    spec, ham = chains.xy_chain(8)
+    sec = sector(spec)
+    H = sec.lower(ham)
+    psi = q.getState(sec, 1)
+    psi.set(0, q.start_vector(sec.dim, 1))
+    import ctypes as C
+    for kdim in (0, 4097):
+        opts = A.qd_lanczos_opts(kdim, A.QD_SPMV_CSR, A.QD_RITZ_STORED_BASIS, 0)
+        res = A.qd_lanczos_result()
+        with pytest.raises(A.QDError) as e:
+            A.call("qd_lanczos_ground", H.handle, psi.handle, 0, C.byref(opts), None, C.byref(res))
+        assert e.value.code == A.QD_ERR_INVALID
+    assert q.LanczosSolver(sec, 0).getGroundState(H, psi, 0) is None  # a full (empty) space returns at once
+    with pytest.raises(A.QDError):
+        psi.eval(1, H)  # time slot outside the state
+    with pytest.raises(A.QDError):
+        A.call("qd_ham_set_spmv_kernel", H.handle, 99)
