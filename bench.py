@@ -686,6 +686,8 @@ def main():
     ap.add_argument("--product", type=int, default=None, metavar="KERNEL",
                     help="product kernel of the Lanczos solves (qd_ham_set_spmv_kernel code; default: the engine's)")
     ap.add_argument("--serve-only", action="store_true", help="only run the serving mix")
+    ap.add_argument("--batch-only", type=int, default=None, metavar="N",
+                    help="only run the batched disorder sweep with N instances")
     ap.add_argument("--serve-requests", type=int, default=400)
     args = ap.parse_args()
     rank, world, local = dist_env()
@@ -695,6 +697,10 @@ def main():
         return spmv_only(args, local)
     if args.serve_only:
         print(json.dumps(serving_mix(args.serve_requests)))
+        return 0
+    if args.batch_only is not None:
+        import qudrip_gb300 as q
+        print(json.dumps(batched_sweep(q.Context(local), n_inst=args.batch_only)))
         return 0
     return gpu_arm(args, rank, world, local)
 

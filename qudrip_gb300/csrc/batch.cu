@@ -2,11 +2,19 @@
 //
 // The mixed-precision form of the reference's Lanczos (sparse_algorithm.hpp:
 // 395-425, 564-585) for a packed work list of independent, uneven instances:
-//   * one CTA owns one instance at a time and takes the next one from an
-//     atomic counter; the list is sorted by decreasing nnz (longest first);
+//   * small instances: one CTA owns one instance at a time and takes the next
+//     one from an atomic counter;
+//   * large instances (dim >= kClusterMinDim): a thread-block cluster of
+//     kClusterCtas CTAs owns one instance; each CTA keeps a slice of the rows
+//     of every vector, and the inner products are combined through
+//     distributed shared memory (each CTA adds the CTAs' partials in rank
+//     order, so every CTA holds the same bits) between hardware cluster
+//     barriers -- one SM's memory parallelism is far too little for an
+//     instance of 10^5 rows;
+//   * the lists are sorted by decreasing nnz (longest first);
 //   * matrix values and Krylov vectors are FP32 and so is the product;
 //   * every inner product keeps FP32 partial sums over at most 64 elements per
-//     thread and adds those partials in FP64 (threads, warps, the block);
+//     thread and adds those partials in FP64 (threads, warps, blocks, CTAs);
 //   * after the three-term step (the reference's local orthogonalisation
 //     against the two previous vectors) the new vector is orthogonalised
 //     once more against the whole stored basis (classical Gram-Schmidt);
@@ -14,26 +22,39 @@
 //     implicit QL, the lowest eigenvector by inverse iteration;
 //   * the Ritz vector gets one FP64 refinement: E = psi^T H psi / psi^T psi with
 //     the FP64 matrix values and FP64 accumulation.
-// No block waits on another block, so nothing can hang: the only shared state
-// is the work counter.
+// No CTA spins on another: the only shared state is the work counter, and the
+// CTAs of a cluster meet only at hardware cluster barriers, which the
+// hardware schedules together and every CTA of a cluster reaches the same
+// number of times (the instance index and every stopping decision are the
+// same in all of them).
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <vector>
 
+#include <cooperative_groups.h>
+
 #include "batch.cuh"
 #include "krylov.cuh"
 #include "tridiag.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace qd {
 
 constexpr int kBatchThreads = 512;  // two CTAs per SM
 constexpr int kBatchMaxSteps = 256;
 constexpr int kChunk = 64;  // FP32 partial sums cover at most this many elements
+constexpr int kClusterCtas = 8;          // CTAs of a cluster that shares one large instance
+constexpr int64_t kClusterMinDim = 32768;
 
 struct BlockScratch {
   double red[kBatchThreads / 32];
   double bcast;
+  double xp[2], bc[2];                    // this CTA's partial of a cluster sum, and the sum
+  double hp[2][kBatchMaxSteps + 2];       // this CTA's partials of the Gram-Schmidt coefficients
   double alpha[kBatchMaxSteps + 2];
   double beta[kBatchMaxSteps + 2];
   double y[kBatchMaxSteps + 2];
@@ -58,16 +79,19 @@ __device__ double block_sum_all(double v, BlockScratch& S) {
   return S.bcast;
 }
 
-// <a, b> with FP32 products and partials over <= kChunk elements, FP64 beyond.
-// a and b are 16-byte aligned (every vector starts on a 32-element boundary).
-__device__ double block_dot(const float* __restrict__ a, const float* __restrict__ b, int64_t n, BlockScratch& S) {
+// <a, b> over [lo, hi) with FP32 products and partials over <= kChunk
+// elements, FP64 beyond; the block's total in every thread.  lo is a
+// multiple of 32 and the vectors start on a 32-element boundary.
+__device__ double block_dot(const float* __restrict__ a, const float* __restrict__ b, int64_t lo, int64_t hi,
+                            BlockScratch& S) {
   double dacc = 0.0;
   float acc = 0.f;
   int cnt = 0;
-  const int64_t n4 = n >> 2;
+  const int64_t q0 = lo >> 2, q1 = hi >> 2;
   const float4* a4 = reinterpret_cast<const float4*>(a);
   const float4* b4 = reinterpret_cast<const float4*>(b);
-  for (int64_t i = threadIdx.x; i < n4; i += blockDim.x) {
+#pragma unroll 4
+  for (int64_t i = q0 + threadIdx.x; i < q1; i += blockDim.x) {
     const float4 x = a4[i], y = b4[i];
     acc = fmaf(x.x, y.x, acc);
     acc = fmaf(x.y, y.y, acc);
@@ -79,17 +103,18 @@ __device__ double block_dot(const float* __restrict__ a, const float* __restrict
       cnt = 0;
     }
   }
-  for (int64_t i = (n4 << 2) + threadIdx.x; i < n; i += blockDim.x) acc = fmaf(a[i], b[i], acc);
+  for (int64_t i = (q1 << 2) + threadIdx.x; i < hi; i += blockDim.x) acc = fmaf(a[i], b[i], acc);
   dacc += (double)acc;
   return block_sum_all(dacc, S);
 }
 
-// w -= c * v
-__device__ void block_axpy(float* __restrict__ w, float c, const float* __restrict__ v, int64_t n) {
-  const int64_t n4 = n >> 2;
+// w -= c * v on [lo, hi)
+__device__ void block_axpy(float* __restrict__ w, float c, const float* __restrict__ v, int64_t lo, int64_t hi) {
+  const int64_t q0 = lo >> 2, q1 = hi >> 2;
   float4* w4 = reinterpret_cast<float4*>(w);
   const float4* v4 = reinterpret_cast<const float4*>(v);
-  for (int64_t i = threadIdx.x; i < n4; i += blockDim.x) {
+#pragma unroll 4
+  for (int64_t i = q0 + threadIdx.x; i < q1; i += blockDim.x) {
     float4 x = w4[i];
     const float4 y = v4[i];
     x.x = fmaf(-c, y.x, x.x);
@@ -98,26 +123,60 @@ __device__ void block_axpy(float* __restrict__ w, float c, const float* __restri
     x.w = fmaf(-c, y.w, x.w);
     w4[i] = x;
   }
-  for (int64_t i = (n4 << 2) + threadIdx.x; i < n; i += blockDim.x) w[i] = fmaf(-c, v[i], w[i]);
+  for (int64_t i = (q1 << 2) + threadIdx.x; i < hi; i += blockDim.x) w[i] = fmaf(-c, v[i], w[i]);
 }
 
-// y = H x (FP32 values, FP32 accumulation), one thread per row.
-__device__ void block_spmv_f32(const BatchInst& I, const float* __restrict__ x, float* __restrict__ y) {
-  for (int64_t r = threadIdx.x; r < I.dim; r += blockDim.x) {
+// y = H x on rows [lo, hi) (FP32 values, FP32 accumulation), one thread per
+// row.  x is a basis vector written earlier in the same launch (by this CTA
+// or, for a cluster, by all of its CTAs), so it is read with ordinary loads,
+// not the read-only path.
+__device__ void block_spmv_f32(const BatchInst& I, const float* x, float* __restrict__ y, int64_t lo, int64_t hi) {
+  for (int64_t r = lo + threadIdx.x; r < hi; r += blockDim.x) {
     const int64_t b = I.rowptr[r], e = I.rowptr[r + 1];
     float acc = 0.f;
     int64_t k = b;
     for (; k + 4 <= e; k += 4) {
       const int32_t c0 = I.colidx[k], c1 = I.colidx[k + 1], c2 = I.colidx[k + 2], c3 = I.colidx[k + 3];
       const float v0 = I.vals_f[k], v1 = I.vals_f[k + 1], v2 = I.vals_f[k + 2], v3 = I.vals_f[k + 3];
-      const float x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
+      const float x0 = x[c0], x1 = x[c1], x2 = x[c2], x3 = x[c3];
       acc = fmaf(v0, x0, acc);
       acc = fmaf(v1, x1, acc);
       acc = fmaf(v2, x2, acc);
       acc = fmaf(v3, x3, acc);
     }
-    for (; k < e; ++k) acc = fmaf(I.vals_f[k], __ldg(x + I.colidx[k]), acc);
+    for (; k < e; ++k) acc = fmaf(I.vals_f[k], x[I.colidx[k]], acc);
     y[r] = acc;
+  }
+}
+
+// ---------------------------------------------------------------- cluster sums
+// A barrier over the instance's CTAs (the block for C == 1).
+template <int C>
+__device__ __forceinline__ void inst_sync() {
+  if constexpr (C > 1) cg::this_cluster().sync();
+  else __syncthreads();
+}
+
+// The instance total of a block total: every CTA adds the C partials in rank
+// order from distributed shared memory.  Double-buffered: a buffer is written
+// again only two sums later, after every CTA has passed the barrier between.
+template <int C>
+__device__ double inst_sum(double block_total, BlockScratch& S, int& buf) {
+  if constexpr (C == 1) {
+    return block_total;
+  } else {
+    cg::cluster_group cl = cg::this_cluster();
+    if (threadIdx.x == 0) S.xp[buf] = block_total;
+    cl.sync();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int r = 0; r < C; ++r) t += *cl.map_shared_rank(&S.xp[buf], r);
+      S.bc[buf] = t;
+    }
+    __syncthreads();
+    const double t = S.bc[buf];
+    buf ^= 1;
+    return t;
   }
 }
 
@@ -196,52 +255,63 @@ __device__ double device_tridiag_lowest(int n, const double* d_in, const double*
   return lam;
 }
 
+template <int C>
 __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const BatchInst* __restrict__ list, int ninst,
                                                                      unsigned* counter, double* tri_work) {
   __shared__ BlockScratch S;
+  int rank = 0;
+  if constexpr (C > 1) rank = (int)cg::this_cluster().block_rank();
+  int buf = 0, hbuf = 0;
   for (;;) {
-    if (threadIdx.x == 0) S.idx = (int)atomicAdd(counter, 1u);
-    __syncthreads();
-    const int idx = S.idx;
-    __syncthreads();
-    if (idx >= ninst) return;
+    if (rank == 0 && threadIdx.x == 0) S.idx = (int)atomicAdd(counter, 1u);
+    inst_sync<C>();
+    int idx;
+    if constexpr (C > 1) idx = *cg::this_cluster().map_shared_rank(&S.idx, 0);
+    else idx = S.idx;
+    inst_sync<C>();
+    if (idx >= ninst) return;  // the same index in every CTA of the cluster
     const BatchInst I = list[idx];
     const int64_t n = I.dim;
+    // this CTA's rows: a slice of 32-element multiples (the whole vector for C == 1)
+    const int64_t per = ((n + C - 1) / C + 31) / 32 * 32;
+    const int64_t lo = std::min<int64_t>(n, (int64_t)rank * per), hi = std::min<int64_t>(n, lo + per);
     float* V = I.V;
     float* w = I.w;
     // v_0 = v0 / ||v0||
-    const double nrm0 = sqrt(block_dot(I.v0, I.v0, n, S));
+    const double nrm0 = sqrt(inst_sum<C>(block_dot(I.v0, I.v0, lo, hi, S), S, buf));
     const float inv0 = (float)(1.0 / nrm0);
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) V[i] = I.v0[i] * inv0;
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) V[i] = I.v0[i] * inv0;
     if (threadIdx.x == 0) S.stop = 0;
-    __syncthreads();
+    inst_sync<C>();
     int act = I.steps;
     for (int k = 1; k <= I.steps; ++k) {
       const float* v1 = V + (int64_t)(k - 1) * I.ld;
       const float* v2 = (k >= 2) ? V + (int64_t)(k - 2) * I.ld : nullptr;
-      block_spmv_f32(I, v1, w);
+      block_spmv_f32(I, v1, w, lo, hi);
       __syncthreads();
       double bp = 0.0;
       if (v2) {
-        bp = block_dot(v2, w, n, S);
-        block_axpy(w, (float)bp, v2, n);
+        bp = inst_sum<C>(block_dot(v2, w, lo, hi, S), S, buf);
+        block_axpy(w, (float)bp, v2, lo, hi);
         __syncthreads();
       }
-      const double al = block_dot(v1, w, n, S);
-      block_axpy(w, (float)al, v1, n);
+      const double al = inst_sum<C>(block_dot(v1, w, lo, hi, S), S, buf);
+      block_axpy(w, (float)al, v1, lo, hi);
       __syncthreads();
       // one full Gram-Schmidt pass against v_0 .. v_{k-1}: a warp per basis vector
       {
         const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-        const int64_t n4 = n >> 2;
+        const int64_t q0 = lo >> 2, q1 = hi >> 2;
         const float4* w4 = reinterpret_cast<const float4*>(w);
+        double* part = (C > 1) ? S.hp[hbuf] : S.h;
         for (int j = warp; j < k; j += nw) {
           const float* vj = V + (int64_t)j * I.ld;
           const float4* vj4 = reinterpret_cast<const float4*>(vj);
           double dacc = 0.0;
           float acc = 0.f;
           int cnt = 0;
-          for (int64_t i = lane; i < n4; i += 32) {
+#pragma unroll 4
+          for (int64_t i = q0 + lane; i < q1; i += 32) {
             const float4 x = vj4[i], y = w4[i];
             acc = fmaf(x.x, y.x, acc);
             acc = fmaf(x.y, y.y, acc);
@@ -253,15 +323,26 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const B
               cnt = 0;
             }
           }
-          for (int64_t i = (n4 << 2) + lane; i < n; i += 32) acc = fmaf(vj[i], w[i], acc);
+          for (int64_t i = (q1 << 2) + lane; i < hi; i += 32) acc = fmaf(vj[i], w[i], acc);
           dacc += (double)acc;
           dacc = warp_sum(dacc);
-          if (lane == 0) S.h[j] = dacc;
+          if (lane == 0) part[j] = dacc;
+        }
+        if constexpr (C > 1) {  // the coefficients of the whole vector, the same bits in every CTA
+          cg::cluster_group cl = cg::this_cluster();
+          cl.sync();
+          for (int j = threadIdx.x; j < k; j += blockDim.x) {
+            double t = 0.0;
+            for (int r = 0; r < C; ++r) t += *cl.map_shared_rank(&S.hp[hbuf][j], r);
+            S.h[j] = t;
+          }
+          hbuf ^= 1;
         }
         __syncthreads();
         float4* wm4 = reinterpret_cast<float4*>(w);
-        for (int64_t i = threadIdx.x; i < n4; i += blockDim.x) {
+        for (int64_t i = q0 + threadIdx.x; i < q1; i += blockDim.x) {
           float4 x = wm4[i];
+#pragma unroll 4
           for (int j = 0; j < k; ++j) {
             const float c = -(float)S.h[j];
             const float4 y = reinterpret_cast<const float4*>(V + (int64_t)j * I.ld)[i];
@@ -272,14 +353,14 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const B
           }
           wm4[i] = x;
         }
-        for (int64_t i = (n4 << 2) + threadIdx.x; i < n; i += blockDim.x) {
+        for (int64_t i = (q1 << 2) + threadIdx.x; i < hi; i += blockDim.x) {
           float wi = w[i];
           for (int j = 0; j < k; ++j) wi = fmaf(-(float)S.h[j], V[(int64_t)j * I.ld + i], wi);
           w[i] = wi;
         }
         __syncthreads();
       }
-      const double nr = sqrt(block_dot(w, w, n, S));
+      const double nr = sqrt(inst_sum<C>(block_dot(w, w, lo, hi, S), S, buf));
       if (threadIdx.x == 0) {
         S.alpha[k] = al + S.h[k - 1];
         S.beta[k] = nr;
@@ -289,49 +370,101 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const B
         if (nr < 1e-10 || nr < 1e-5 * scale || k >= n) S.stop = k;
       }
       __syncthreads();
-      if (S.stop) {
-        act = k;  // v_0 .. v_{k-1} span an invariant subspace: T_k is exact
+      if (S.stop) {  // the same decision in every CTA of the cluster
+        act = k;     // v_0 .. v_{k-1} span an invariant subspace: T_k is exact
         break;
       }
       const float inv = (float)(1.0 / nr);
       float* vk = V + (int64_t)k * I.ld;
-      for (int64_t i = threadIdx.x; i < n; i += blockDim.x) vk[i] = w[i] * inv;
-      __syncthreads();
+      for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) vk[i] = w[i] * inv;
+      inst_sync<C>();  // the next product reads all of v_k
     }
     if (act < 1) act = 1;
-    // lowest Ritz pair of tridiag(alpha_1..act, beta_1..act-1)
+    // lowest Ritz pair of tridiag(alpha_1..act, beta_1..act-1), the same in every CTA
     if (threadIdx.x == 0) {
       double* work = tri_work + (size_t)blockIdx.x * 8 * (kBatchMaxSteps + 2);
       const double lam = device_tridiag_lowest(act, S.alpha + 1, S.beta + 1, S.y, work);
-      I.out[0] = lam;
-      I.out[3] = act;
-      I.out[4] = S.stop ? 1 : 0;
+      if (rank == 0) {
+        I.out[0] = lam;
+        I.out[3] = act;
+        I.out[4] = S.stop ? 1 : 0;
+      }
     }
     __syncthreads();
     // Ritz vector psi = sum_k y_k v_k (FP32 storage)
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
       float acc = 0.f;
       for (int k = 0; k < act; ++k) acc = fmaf((float)S.y[k], V[(int64_t)k * I.ld + i], acc);
       I.psi[i] = acc;
     }
-    __syncthreads();
+    inst_sync<C>();  // the refinement reads all of psi
     // FP64 refinement: Rayleigh quotient with the FP64 values
     double num = 0.0, den = 0.0;
-    for (int64_t r = threadIdx.x; r < n; r += blockDim.x) {
+    for (int64_t r = lo + threadIdx.x; r < hi; r += blockDim.x) {
       double hr = 0.0;
       for (int64_t e = I.rowptr[r]; e < I.rowptr[r + 1]; ++e) hr = fma(I.vals_d[e], (double)I.psi[I.colidx[e]], hr);
       const double pr = (double)I.psi[r];
       num = fma(pr, hr, num);
       den = fma(pr, pr, den);
     }
-    num = block_sum_all(num, S);
-    den = block_sum_all(den, S);
-    if (threadIdx.x == 0) {
+    num = inst_sum<C>(block_sum_all(num, S), S, buf);
+    den = inst_sum<C>(block_sum_all(den, S), S, buf);
+    if (rank == 0 && threadIdx.x == 0) {
       I.out[1] = num / den;
       I.out[2] = den;
     }
-    __syncthreads();
+    inst_sync<C>();
   }
+}
+
+// Launches kernel C over `count` instances of `list` with `grid` CTAs
+// (clusters of C CTAs for C > 1).
+template <int C>
+static void launch_batch(Ctx* ctx, const BatchInst* list, int count, unsigned* counter, double* tri_work, int grid) {
+  if (count <= 0) return;
+  if constexpr (C == 1) {
+    batch_lanczos_kernel<1><<<grid, kBatchThreads, 0, ctx->stream>>>(list, count, counter, tri_work);
+  } else {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kBatchThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = ctx->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    QD_CUDA(cudaLaunchKernelEx(&cfg, batch_lanczos_kernel<C>, list, count, counter, tri_work));
+  }
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+}
+
+// Clusters of C CTAs the device keeps resident at once (0 if none).
+template <int C>
+static int resident_clusters(Ctx* ctx) {
+  static thread_local int cached = -1;
+  if (cached >= 0) return cached;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(C * 2 * ctx->num_sms));
+  cfg.blockDim = dim3(kBatchThreads);
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, batch_lanczos_kernel<C>, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    n = 0;
+  }
+  cached = n;
+  return n;
 }
 
 void batch_lanczos(Ctx* ctx, qd_ham* const* hams, const double* const* v0s, int ninst, int steps, double* out) {
@@ -346,13 +479,13 @@ void batch_lanczos(Ctx* ctx, qd_ham* const* hams, const double* const* v0s, int 
     QD_REQUIRE(hams[i]->ctx == ctx, QD_ERR_INVALID, "instance %d: Hamiltonian of another context", i);
   }
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hams[a]->nnz > hams[b]->nnz; });
-  // one arena for every instance's start vector, basis, work vector, Ritz vector
-  std::vector<int64_t> off_v0(ninst), off_V(ninst), off_w(ninst), off_psi(ninst);
+  // large instances (a cluster each) first, each class longest first
+  std::stable_partition(order.begin(), order.end(), [&](int a) { return hams[a]->dim >= kClusterMinDim; });
+  // one arena for every instance's basis, work vector and Ritz vector
+  std::vector<int64_t> off_V(ninst), off_w(ninst), off_psi(ninst);
   int64_t total = 0;
   for (int i = 0; i < ninst; ++i) {
     const int64_t ld = (hams[i]->dim + 31) / 32 * 32;
-    off_v0[i] = total;
-    total += ld;
     off_V[i] = total;
     total += (int64_t)(steps + 1) * ld;
     off_w[i] = total;
@@ -362,15 +495,24 @@ void batch_lanczos(Ctx* ctx, qd_ham* const* hams, const double* const* v0s, int 
   }
   DBuf<float> arena(total);
   DBuf<double> dout((size_t)ninst * 8);
-  std::vector<float> h32;
+  QD_CUDA(cudaMemsetAsync(dout.p, 0, dout.bytes(), ctx->stream));
+  // the start vectors, in FP32, in one copy
+  int64_t v0_total = 0;
+  for (int i = 0; i < ninst; ++i) v0_total += (hams[i]->dim + 31) / 32 * 32;
+  std::vector<float> h32((size_t)v0_total, 0.f);
+  DBuf<float> v0buf(v0_total);
+  std::vector<int64_t> off_h(ninst);
   for (int i = 0; i < ninst; ++i) {
-    h32.assign(v0s[i], v0s[i] + hams[i]->dim);
-    for (int64_t q = 0; q < hams[i]->dim; ++q) h32[q] = (float)v0s[i][q];
-    QD_CUDA(cudaMemcpyAsync(arena.p + off_v0[i], h32.data(), hams[i]->dim * sizeof(float), cudaMemcpyHostToDevice,
-                            ctx->stream));
-    QD_CUDA(cudaStreamSynchronize(ctx->stream));
+    off_h[i] = (i == 0) ? 0 : off_h[i - 1] + (hams[i - 1]->dim + 31) / 32 * 32;
+    for (int64_t q = 0; q < hams[i]->dim; ++q) h32[(size_t)(off_h[i] + q)] = (float)v0s[i][q];
   }
+  QD_CUDA(cudaMemcpyAsync(v0buf.p, h32.data(), h32.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  // the work list: large instances, then small ones
   std::vector<BatchInst> list(ninst);
+  int nlarge = 0;
+  for (int q = 0; q < ninst; ++q) nlarge += (hams[order[q]]->dim >= kClusterMinDim) ? 1 : 0;
+  const int nclusters = resident_clusters<kClusterCtas>(ctx);
+  if (nclusters < 1) nlarge = 0;  // no cluster fits: every instance on one CTA
   for (int q = 0; q < ninst; ++q) {
     const int i = order[q];
     const qd_ham* H = hams[i];
@@ -383,7 +525,7 @@ void batch_lanczos(Ctx* ctx, qd_ham* const* hams, const double* const* v0s, int 
     I.colidx = H->colidx.p;
     I.vals_f = H->vals_f.p;
     I.vals_d = H->vals_r.p;
-    I.v0 = arena.p + off_v0[i];
+    I.v0 = v0buf.p + off_h[i];
     I.V = arena.p + off_V[i];
     I.w = arena.p + off_w[i];
     I.psi = arena.p + off_psi[i];
@@ -391,15 +533,27 @@ void batch_lanczos(Ctx* ctx, qd_ham* const* hams, const double* const* v0s, int 
   }
   DBuf<BatchInst> dlist(ninst);
   QD_CUDA(cudaMemcpyAsync(dlist.p, list.data(), ninst * sizeof(BatchInst), cudaMemcpyHostToDevice, ctx->stream));
-  DBuf<unsigned> counter(1);
-  QD_CUDA(cudaMemsetAsync(counter.p, 0, sizeof(unsigned), ctx->stream));
-  const int grid = std::min(ninst, 2 * ctx->num_sms);
-  DBuf<double> tri_work((size_t)grid * 8 * (kBatchMaxSteps + 2));
-  batch_lanczos_kernel<<<grid, kBatchThreads, 0, ctx->stream>>>(dlist.p, ninst, counter.p, tri_work.p);
-  QD_CHECK_LAUNCH();
-  QD_LAUNCHED(ctx);
+  DBuf<unsigned> counter(2);
+  QD_CUDA(cudaMemsetAsync(counter.p, 0, 2 * sizeof(unsigned), ctx->stream));
+  const int nsmall = ninst - nlarge;
+  const int grid_large = nlarge ? kClusterCtas * std::min(nlarge, nclusters) : 0;
+  const int grid_small = nsmall ? std::min(nsmall, 2 * ctx->num_sms) : 0;
+  DBuf<double> tri_work((size_t)std::max(std::max(grid_large, grid_small), 1) * 8 * (kBatchMaxSteps + 2));
+  const bool timing = std::getenv("QD_TIMING") != nullptr;
+  if (timing) QD_CUDA(cudaEventRecord(ctx->events[12], ctx->stream));
+  launch_batch<kClusterCtas>(ctx, dlist.p, nlarge, counter.p, tri_work.p, grid_large);
+  if (timing) QD_CUDA(cudaEventRecord(ctx->events[13], ctx->stream));
+  launch_batch<1>(ctx, dlist.p + nlarge, nsmall, counter.p + 1, tri_work.p, grid_small);
+  if (timing) QD_CUDA(cudaEventRecord(ctx->events[14], ctx->stream));
   QD_CUDA(cudaMemcpyAsync(out, dout.p, (size_t)ninst * 8 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (timing) {
+    float a = 0.f, b = 0.f;
+    QD_CUDA(cudaEventElapsedTime(&a, ctx->events[12], ctx->events[13]));
+    QD_CUDA(cudaEventElapsedTime(&b, ctx->events[13], ctx->events[14]));
+    std::fprintf(stderr, "[qd timing] batch: %d large on %d clusters %.3f ms, %d small on %d CTAs %.3f ms\n", nlarge,
+                 grid_large / kClusterCtas, a, nsmall, grid_small, b);
+  }
 }
 
 }  // namespace qd
