@@ -310,8 +310,34 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const B
           double dacc = 0.0;
           float acc = 0.f;
           int cnt = 0;
-#pragma unroll 4
-          for (int64_t i = q0 + lane; i < q1; i += 32) {
+          int64_t i = q0 + lane;
+          for (; i + 96 < q1; i += 128) {  // four float4 pairs in flight per lane
+            const float4 x0 = vj4[i], y0 = w4[i], x1 = vj4[i + 32], y1 = w4[i + 32];
+            const float4 x2 = vj4[i + 64], y2 = w4[i + 64], x3 = vj4[i + 96], y3 = w4[i + 96];
+            acc = fmaf(x0.x, y0.x, acc);
+            acc = fmaf(x0.y, y0.y, acc);
+            acc = fmaf(x0.z, y0.z, acc);
+            acc = fmaf(x0.w, y0.w, acc);
+            acc = fmaf(x1.x, y1.x, acc);
+            acc = fmaf(x1.y, y1.y, acc);
+            acc = fmaf(x1.z, y1.z, acc);
+            acc = fmaf(x1.w, y1.w, acc);
+            acc = fmaf(x2.x, y2.x, acc);
+            acc = fmaf(x2.y, y2.y, acc);
+            acc = fmaf(x2.z, y2.z, acc);
+            acc = fmaf(x2.w, y2.w, acc);
+            acc = fmaf(x3.x, y3.x, acc);
+            acc = fmaf(x3.y, y3.y, acc);
+            acc = fmaf(x3.z, y3.z, acc);
+            acc = fmaf(x3.w, y3.w, acc);
+            cnt += 4;
+            if (cnt >= kChunk / 4) {
+              dacc += (double)acc;
+              acc = 0.f;
+              cnt = 0;
+            }
+          }
+          for (; i < q1; i += 32) {
             const float4 x = vj4[i], y = w4[i];
             acc = fmaf(x.x, y.x, acc);
             acc = fmaf(x.y, y.y, acc);
@@ -340,7 +366,28 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const B
         }
         __syncthreads();
         float4* wm4 = reinterpret_cast<float4*>(w);
-        for (int64_t i = q0 + threadIdx.x; i < q1; i += blockDim.x) {
+        const int64_t bs = blockDim.x;
+        int64_t i = q0 + threadIdx.x;
+        for (; i + bs < q1; i += 2 * bs) {  // two float4 of w per thread: two independent chains
+          float4 x = wm4[i], u = wm4[i + bs];
+#pragma unroll 4
+          for (int j = 0; j < k; ++j) {
+            const float c = -(float)S.h[j];
+            const float4* vj4 = reinterpret_cast<const float4*>(V + (int64_t)j * I.ld);
+            const float4 y = vj4[i], z = vj4[i + bs];
+            x.x = fmaf(c, y.x, x.x);
+            x.y = fmaf(c, y.y, x.y);
+            x.z = fmaf(c, y.z, x.z);
+            x.w = fmaf(c, y.w, x.w);
+            u.x = fmaf(c, z.x, u.x);
+            u.y = fmaf(c, z.y, u.y);
+            u.z = fmaf(c, z.z, u.z);
+            u.w = fmaf(c, z.w, u.w);
+          }
+          wm4[i] = x;
+          wm4[i + bs] = u;
+        }
+        for (; i < q1; i += bs) {
           float4 x = wm4[i];
 #pragma unroll 4
           for (int j = 0; j < k; ++j) {
