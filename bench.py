@@ -303,8 +303,13 @@ def gpu_arm(args, rank, world, local):
     info = A.qd_ham_info()
     A.call("qd_ham_get_info", H.handle, C.byref(info))
     if info.product_kernel == 120:
-        kernel_name, spmv_name = "spmv_fx_dots_kernel<true>", "uniform_coupling_fixed_point_sums_fused_dots"
+        kernel_name = "spmv_fx_dots_kernel<true>"
+        spmv_name = "uniform_coupling_fixed_point_sums_sliced_columns_fused_dots"
         traffic = profile_traffic("spmv_fx_dots_xxz_L24")
+    elif info.product_kernel == 121:
+        kernel_name = "spmv_fx_slots_dots_kernel<true>"
+        spmv_name = "uniform_coupling_fixed_point_sums_columns_from_terms_fused_dots"
+        traffic = None
     else:
         kernel_name, spmv_name = "spmv_rowexact_kernel<double,double>", "csr_row_exact_fp64"
         traffic = profile_traffic("spmv_csr_f64_xxz_L24")

@@ -1,6 +1,8 @@
 // fxsum.cu -- building the uniform-coupling form and its product (fxsum.cuh).
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "fxsum.cuh"
@@ -93,6 +95,8 @@ static int fx_grid(Ctx* ctx, int64_t n) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)ctx->num_sms * 8));
 }
 
+static void build_sell(Ctx* ctx, FxForm& f, int64_t n);
+
 bool ham_build_fx(qd_ham* H) {
   if (H->fx_state != 0) return H->fx_state > 0;
   H->fx_state = -1;
@@ -146,16 +150,45 @@ bool ham_build_fx(qd_ham* H) {
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  build_sell(ctx, *fx, n);
   H->fx = std::move(fx);
   H->fx_state = 1;
   return true;
 }
 
 // ---------------------------------------------------------------- product
-// w_r = s * (d_r x_r + c 2^-F sum_k X_k): thread per row, columns and the
-// 16-byte fixed-point gathers four at a time, one FP64 rounding of the sum.
-__global__ void __launch_bounds__(256) spmv_fx_kernel(int64_t n, const int32_t* __restrict__ rowptr,
-                                                      const int32_t* __restrict__ colidx,
+// Column layout of the product: the rows in slices of 32 (a warp's rows),
+// entry k of row 32 s + l at sell_off[s] + 128 (k / 4) + 4 l + k % 4, so
+// that lane l loads four of its columns with one 16-byte load and the warp's
+// 32 loads are one contiguous 512-byte run; a slice is as wide as its longest
+// row, rounded up to 4 (26 % padding at L = 24), and sell_len holds each
+// row's own count, so padding is never gathered.  Within a row the columns
+// keep their gather order.
+
+// Sum of the row's fixed-point gathers: four columns per 16-byte load, four
+// predicated gathers in flight.
+__device__ __forceinline__ __int128 sell_row_sum(const int4* __restrict__ c4, int e, const __int128* __restrict__ X) {
+  __int128 s = 0;
+  for (int k = 0; k < e; k += 4) {
+    const int4 cc = __ldcs(c4 + 8 * k);  // group k / 4 starts 32 int4 further on
+    __int128 x0 = X[cc.x], x1 = 0, x2 = 0, x3 = 0;
+    if (k + 1 < e) x1 = X[cc.y];
+    if (k + 2 < e) x2 = X[cc.z];
+    if (k + 3 < e) x3 = X[cc.w];
+    s += (x0 + x1) + (x2 + x3);
+  }
+  return s;
+}
+
+__device__ __forceinline__ const int4* sell_row(const int64_t* __restrict__ soff, const int32_t* __restrict__ scol,
+                                                int64_t r) {
+  return reinterpret_cast<const int4*>(scol + __ldg(soff + (r >> 5))) + (r & 31);
+}
+
+// w_r = s * (d_r x_r + c 2^-F sum_k X_k), one FP64 rounding of the sum.
+__global__ void __launch_bounds__(256) spmv_fx_kernel(int64_t n, const int64_t* __restrict__ soff,
+                                                      const int32_t* __restrict__ scol,
+                                                      const uint8_t* __restrict__ slen,
                                                       const double* __restrict__ diag,
                                                       const double* __restrict__ x, const __int128* __restrict__ X,
                                                       double* __restrict__ y, double cF, const double* scale_dev,
@@ -167,16 +200,7 @@ __global__ void __launch_bounds__(256) spmv_fx_kernel(int64_t n, const int32_t* 
   const double sc = scale_dev ? *scale_dev : 1.0;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-    const int b = __ldg(rowptr + r), e = __ldg(rowptr + r + 1);
-    __int128 acc = 0;
-    int k = b;
-    for (; k + 4 <= e; k += 4) {
-      const int c0 = __ldcs(colidx + k), c1 = __ldcs(colidx + k + 1), c2 = __ldcs(colidx + k + 2),
-                c3 = __ldcs(colidx + k + 3);
-      const __int128 x0 = X[c0], x1 = X[c1], x2 = X[c2], x3 = X[c3];
-      acc += (x0 + x1) + (x2 + x3);
-    }
-    for (; k < e; ++k) acc += X[__ldcs(colidx + k)];
+    const __int128 acc = sell_row_sum(sell_row(soff, scol, r), __ldcs(slen + r), X);
     y[r] = sc * fma(cF, (double)acc, __ldcs(diag + r) * __ldg(x + r));
   }
 }
@@ -191,8 +215,8 @@ __global__ void __launch_bounds__(256) spmv_fx_kernel(int64_t n, const int32_t* 
 // gathered fixed-point vector is loaded and stored with evict-first hints so
 // that the 16-byte-per-row vector X stays in L2 for the gathers.
 template <bool kHas2>
-__global__ void __launch_bounds__(256) spmv_fx_dots_kernel(
-    int64_t n, const int32_t* __restrict__ rowptr, const int32_t* __restrict__ colidx,
+__global__ void __launch_bounds__(256, 6) spmv_fx_dots_kernel(
+    int64_t n, const int64_t* __restrict__ soff, const int32_t* __restrict__ scol, const uint8_t* __restrict__ slen,
     const double* __restrict__ diag, const double* __restrict__ x, const __int128* __restrict__ X,
     const double* __restrict__ V2, double* __restrict__ y, double cF, const double* s1, const double* s2,
     const int* stop, int step, double* beta, double* alpha, Tri<double>* dots, GridRed<Tri<double>> red) {
@@ -204,16 +228,7 @@ __global__ void __launch_bounds__(256) spmv_fx_dots_kernel(
   Tri<double> acc = vzero(Tri<double>{});
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
-    const int b = __ldcs(rowptr + r), e = __ldcs(rowptr + r + 1);
-    __int128 s = 0;
-    int k = b;
-    for (; k + 4 <= e; k += 4) {
-      const int c0 = __ldcs(colidx + k), c1 = __ldcs(colidx + k + 1), c2 = __ldcs(colidx + k + 2),
-                c3 = __ldcs(colidx + k + 3);
-      const __int128 x0 = X[c0], x1 = X[c1], x2 = X[c2], x3 = X[c3];
-      s += (x0 + x1) + (x2 + x3);
-    }
-    for (; k < e; ++k) s += X[__ldcs(colidx + k)];
+    const __int128 s = sell_row_sum(sell_row(soff, scol, r), __ldcs(slen + r), X);
     const double xr = __ldcs(x + r);
     const double w = sc * fma(cF, (double)s, __ldcs(diag + r) * xr);
     __stcs(y + r, w);
@@ -232,6 +247,53 @@ __global__ void __launch_bounds__(256) spmv_fx_dots_kernel(
     *beta = bt;
     *alpha = (*s1) * t;
   }
+}
+
+__global__ void sell_width_kernel(int64_t n, const int32_t* rowptr, int64_t* width, uint8_t* len) {
+  const int64_t nsl = (n + 31) / 32;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < nsl; s += (int64_t)gridDim.x * blockDim.x) {
+    int w = 0;
+    for (int64_t r = s * 32; r < std::min<int64_t>(n, s * 32 + 32); ++r) {
+      const int l = rowptr[r + 1] - rowptr[r];
+      len[r] = (uint8_t)l;
+      w = max(w, l);
+    }
+    width[s] = (int64_t)((w + 3) / 4) * 128;  // groups of 4 entries per lane
+  }
+}
+
+__global__ void sell_fill_kernel(int64_t n, const int32_t* rowptr, const int32_t* colidx, const int64_t* off,
+                                 int32_t* scol) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t base = off[r >> 5] + 4 * (r & 31);
+    for (int k = rowptr[r]; k < rowptr[r + 1]; ++k) {
+      const int j = k - rowptr[r];
+      scol[base + 128 * (int64_t)(j >> 2) + (j & 3)] = colidx[k];
+    }
+  }
+}
+
+// The slice layout from the row-ordered columns (rows hold at most 128 of them).
+static void build_sell(Ctx* ctx, FxForm& f, int64_t n) {
+  const int64_t nsl = (n + 31) / 32;
+  f.sell_off.alloc(nsl + 1);
+  f.sell_len.alloc(n + 32);
+  DBuf<int64_t> width(nsl + 1);
+  QD_CUDA(cudaMemsetAsync(width.p, 0, (nsl + 1) * 8, ctx->stream));
+  sell_width_kernel<<<fx_grid(ctx, nsl), 256, 0, ctx->stream>>>(n, f.rowptr.p, width.p, f.sell_len.p);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  exclusive_scan_i64(ctx, width.p, f.sell_off.p, nsl + 1);
+  int64_t total = 0;
+  QD_CUDA(cudaMemcpyAsync(&total, f.sell_off.p + nsl, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  f.sell_cols = total;
+  f.sell_col.alloc(total + 128);
+  QD_CUDA(cudaMemsetAsync(f.sell_col.p, 0, (total + 128) * 4, ctx->stream));
+  sell_fill_kernel<<<fx_grid(ctx, n), 256, 0, ctx->stream>>>(n, f.rowptr.p, f.colidx.p, f.sell_off.p, f.sell_col.p);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
 static int fx_dots_grid(Ctx* ctx, int64_t n) {
@@ -256,11 +318,13 @@ void launch_fx_dots(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x,
     return;
   }
   if (V2)
-    spmv_fx_dots_kernel<true><<<g, 256, 0, ctx->stream>>>(H->dim, f.rowptr.p, f.colidx.p, f.diag.p, x, X, V2, y, cF,
-                                                           s1, s2, stop, step, beta, alpha, dots, red);
+    spmv_fx_dots_kernel<true><<<g, 256, 0, ctx->stream>>>(H->dim, f.sell_off.p, f.sell_col.p, f.sell_len.p, f.diag.p,
+                                                           x, X, V2, y, cF, s1, s2, stop, step, beta, alpha, dots,
+                                                           red);
   else
-    spmv_fx_dots_kernel<false><<<g, 256, 0, ctx->stream>>>(H->dim, f.rowptr.p, f.colidx.p, f.diag.p, x, X, x, y,
-                                                            cF, s1, s1, stop, step, beta, alpha, dots, red);
+    spmv_fx_dots_kernel<false><<<g, 256, 0, ctx->stream>>>(H->dim, f.sell_off.p, f.sell_col.p, f.sell_len.p, f.diag.p,
+                                                            x, X, x, y, cF, s1, s1, stop, step, beta, alpha, dots,
+                                                            red);
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
 }
@@ -279,7 +343,7 @@ void launch_fx(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x, cons
   }
   const double cF = std::ldexp(f.c, -f.F);
   spmv_fx_kernel<<<(unsigned)std::max<int64_t>(1, ceil_div(H->dim, 256)), 256, 0, ctx->stream>>>(
-      H->dim, f.rowptr.p, f.colidx.p, f.diag.p, x, X, y, cF, scale_dev, stop, step);
+      H->dim, f.sell_off.p, f.sell_col.p, f.sell_len.p, f.diag.p, x, X, y, cF, scale_dev, stop, step);
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
 }

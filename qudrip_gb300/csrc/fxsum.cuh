@@ -66,8 +66,8 @@ struct Rank32 {
 };
 
 struct FxForm {
-  DBuf<int32_t> rowptr;  // dim + 1 (off-diagonal entries only)
-  DBuf<int32_t> colidx;  // off-diagonal columns of each row in gather order (fx_fill_kernel)
+  DBuf<int32_t> rowptr;  // dim + 1 (off-diagonal entries only), row by row: the source of the
+  DBuf<int32_t> colidx;  // slice layout and of the slot check; columns in gather order (fx_fill_kernel)
   DBuf<double> diag;     // d_r (0 where the CSR has no diagonal entry)
   double c = 0.0;        // the common off-diagonal value
   int F = 0;             // fixed-point scale 2^F
@@ -85,6 +85,12 @@ struct FxForm {
   DBuf<uint32_t> basis32;  // the sector's basis in 32 bits
   DBuf<uint32_t> rtab;     // byte tables of Rank32
   Rank32 rank{};
+  // the columns as the product reads them: 32-row slices, entry k of row 32 s + l
+  // at sell_off[s] + 128 (k / 4) + 4 l + k % 4 (fxsum.cu), the row's count in sell_len
+  int64_t sell_cols = 0;  // stored slots, padding included
+  DBuf<int64_t> sell_off;
+  DBuf<int32_t> sell_col;
+  DBuf<uint8_t> sell_len;
 };
 
 #ifdef __CUDACC__

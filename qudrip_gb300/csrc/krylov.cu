@@ -529,8 +529,9 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
     *bytes_per_launch = (double)n * (8.0 + (H->mf_real ? 8.0 : 16.0) + 2.0 * (double)vb);
   if (mfx)  // 32-bit state, diagonal, x, its fixed-point copy once, y, v2
     *bytes_per_launch = (double)n * (4.0 + 8.0 + 8.0 + 16.0 + 8.0 + 8.0);
-  if (fx)  // columns, row pointers (int32), diagonal, x, its fixed-point copy, y (+ v2 for the fused dots)
-    *bytes_per_launch = (double)H->fx->nnz * 4.0 + (double)(n + 1) * 4.0 +
+  if (fx)  // slice columns (padding included), slice offsets, row counts, diagonal, x, its fixed-point copy, y
+           // (+ v2 for the fused dots)
+    *bytes_per_launch = (double)H->fx->sell_cols * 4.0 + (double)((n + 31) / 32 + 1) * 8.0 + (double)n +
                         (double)n * (8.0 + 8.0 + 16.0 + 8.0 + (spmv == QD_SPMV_CSR ? 8.0 : 0.0));
   if (slots)  // 32-bit state, diagonal, x, its fixed-point copy once, y (+ v2)
     *bytes_per_launch = (double)n * (4.0 + 8.0 + 8.0 + 16.0 + 8.0 + (spmv == QD_SPMV_CSR ? 8.0 : 0.0));

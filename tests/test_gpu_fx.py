@@ -47,10 +47,13 @@ def test_fixed_point_product_timing_and_applicability(ctx):
     ms, nb = C.c_double(), C.c_double()
     A.call("qd_ham_time_spmv", H.handle, 120, 5, C.byref(ms), C.byref(nb))
     assert ms.value > 0
-    info = A.qd_ham_info()
-    A.call("qd_ham_get_info", H.handle, info)
-    nnz_off = info.nnz - sec.dim  # every row of the periodic XXZ chain has a diagonal entry
-    assert nb.value == nnz_off * 4 + (sec.dim + 1) * 4 + sec.dim * 40
+    # columns in 32-row slices, each slice as wide as its longest row rounded up to 4
+    ptr, col, val = H.csr()
+    rows = np.repeat(np.arange(sec.dim), np.diff(ptr))
+    off = np.bincount(rows[(col != rows) & (val != 0)], minlength=sec.dim)
+    pad = np.concatenate([off, np.zeros(-sec.dim % 32, dtype=off.dtype)]).reshape(-1, 32).max(axis=1)
+    cols = int(((pad + 3) // 4 * 128).sum())
+    assert nb.value == cols * 4 + ((sec.dim + 31) // 32 + 1) * 8 + sec.dim + sec.dim * 40
     # Hubbard hopping carries both signs (Jordan-Wigner): the form does not apply
     spec2, ham2 = chains.hubbard_chain(4, 2, 2, 4.0, -1.0, periodic=True)
     sec2, H2 = gpu_objects(spec2, ham2)
