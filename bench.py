@@ -297,18 +297,24 @@ def gpu_arm(args, rank, world, local):
     # Algorithmic bytes of one L=24 matvec (the unit of the metric): the FP64
     # CSR figure nnz*(8+4) + (dim+1)*4 + dim*(8+8) = 492,861,828 B, whatever
     # format the kernel reads (the uniform-coupling form reads fewer bytes for
-    # the same unit; its own byte count is reported beside).
-    unit_bytes = H.nnz * 12 + (dim + 1) * 4 + dim * 16
-    achieved = unit_bytes / (avg_ms.value * 1e-3) / 1e9
+    # the same unit; its own byte count is reported beside).  Where the whole
+    # Lanczos step is one launch the unit is one step: the matrix, v1 and v2
+    # read once, v_k written once (w never leaves the chip):
+    # nnz*12 + (dim+1)*4 + dim*24 = 514,494,324 B.
     info = A.qd_ham_info()
     A.call("qd_ham_get_info", H.handle, C.byref(info))
+    one_launch = info.step_launches == 1
+    unit_bytes = H.nnz * 12 + (dim + 1) * 4 + dim * (24 if one_launch else 16)
+    achieved = unit_bytes / (avg_ms.value * 1e-3) / 1e9
     if info.product_kernel == 120:
-        kernel_name = "spmv_fx_dots_kernel<true>"
-        spmv_name = "uniform_coupling_fixed_point_sums_sliced_columns_fused_dots"
-        traffic = profile_traffic("spmv_fx_dots_xxz_L24")
+        kernel_name = "lz_fx_step_kernel<SellRows,true>" if one_launch else "spmv_fx_dots_kernel<true>"
+        spmv_name = ("uniform_coupling_fixed_point_sums_sliced_columns_one_launch_step" if one_launch else
+                     "uniform_coupling_fixed_point_sums_sliced_columns_fused_dots")
+        traffic = profile_traffic("lz_fx_step_xxz_L24" if one_launch else "spmv_fx_dots_xxz_L24")
     elif info.product_kernel == 121:
-        kernel_name = "spmv_fx_slots_dots_kernel<true>"
-        spmv_name = "uniform_coupling_fixed_point_sums_columns_from_terms_fused_dots"
+        kernel_name = "lz_fx_step_kernel<SlotRows,true>" if one_launch else "spmv_fx_slots_dots_kernel<true>"
+        spmv_name = ("uniform_coupling_fixed_point_sums_columns_from_terms_one_launch_step" if one_launch else
+                     "uniform_coupling_fixed_point_sums_columns_from_terms_fused_dots")
         traffic = None
     else:
         kernel_name, spmv_name = "spmv_rowexact_kernel<double,double>", "csr_row_exact_fp64"

@@ -165,6 +165,10 @@ typedef struct {
   int32_t max_row_nnz;
   int32_t has_matrix_free; /* 1 if qd_ham_build_matrix_free succeeded */
   int32_t product_kernel;  /* product the real Lanczos path launches (codes of qd_ham_set_spmv_kernel) */
+  int32_t step_launches;   /* kernel launches per Lanczos step of the last real solve on the      */
+                           /* uniform-coupling form: 1 (product, dots, update and norm in one    */
+                           /* cooperative launch) or 2 (QD_LANCZOS_STEP=split, or a step too big */
+                           /* to be resident at once); 0 before such a solve                    */
 } qd_ham_info;
 
 qd_status qd_ham_lower(qd_sector *sec, const qd_term *terms, int nterms,

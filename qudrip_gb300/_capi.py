@@ -66,7 +66,7 @@ class qd_term(C.Structure):
 class qd_ham_info(C.Structure):
     _fields_ = [("dim", C.c_int64), ("nnz", C.c_int64), ("flags", C.c_int32),
                 ("max_row_nnz", C.c_int32), ("has_matrix_free", C.c_int32),
-                ("product_kernel", C.c_int32)]
+                ("product_kernel", C.c_int32), ("step_launches", C.c_int32)]
 
 
 class qd_lanczos_opts(C.Structure):

@@ -316,6 +316,7 @@ qd_status qd_ham_get_info(qd_ham* ham, qd_ham_info* info) {
     info->product_kernel = ham->spmv_variant;
     if ((ham->flags & QD_HAM_REAL) && ham->fx_allowed && ham_build_fx(ham))
       info->product_kernel = (ham->fx->use_slots && ham->fx->slots_state > 0) ? kSpmvFxSlots : kSpmvFx;
+    if (ham->fx && ham->fx->step_fused) info->step_launches = ham->fx->step_fused > 0 ? 1 : 2;
   });
 }
 

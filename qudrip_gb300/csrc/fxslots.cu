@@ -18,6 +18,7 @@
 #include <memory>
 #include <vector>
 
+#include "fxstep.cuh"
 #include "ham.cuh"
 #include "krylov.cuh"
 
@@ -84,8 +85,7 @@ struct SlotSmem {
   const FxSlot* slots;
   const int2* dt;
 };
-__device__ __forceinline__ SlotSmem stage_slots(const FxSlotArgs& A) {
-  extern __shared__ __align__(16) unsigned char fxs_smem[];
+__device__ __forceinline__ SlotSmem stage_slots(const FxSlotArgs& A, unsigned char* fxs_smem) {
   uint4* runs = reinterpret_cast<uint4*>(fxs_smem);
   FxSlot* slots = reinterpret_cast<FxSlot*>(fxs_smem + (size_t)A.nrun * sizeof(uint4));
   int2* dt = reinterpret_cast<int2*>(fxs_smem + (size_t)A.nrun * sizeof(uint4) + (size_t)A.nslot * sizeof(FxSlot));
@@ -96,6 +96,11 @@ __device__ __forceinline__ SlotSmem stage_slots(const FxSlotArgs& A) {
   for (int i = threadIdx.x; i < A.ndtab; i += blockDim.x) dt[i] = A.dtab[i];
   __syncthreads();
   return SlotSmem{runs, slots, dt};
+}
+
+__device__ __forceinline__ SlotSmem stage_slots(const FxSlotArgs& A) {
+  extern __shared__ __align__(16) unsigned char fxs_dyn_smem[];
+  return stage_slots(A, fxs_dyn_smem);
 }
 
 // Off-diagonal fixed-point sum of row r: the slots four at a time, four
@@ -580,8 +585,11 @@ bool ham_build_mf_fx(qd_ham* H) {
   {
     std::vector<uint4> runs((size_t)f->nrun);
     std::vector<int2> dtab((size_t)f->ndtab);
-    QD_CUDA(cudaMemcpy(runs.data(), f->runs.p, runs.size() * sizeof(uint4), cudaMemcpyDeviceToHost));
-    QD_CUDA(cudaMemcpy(dtab.data(), f->dtab.p, dtab.size() * sizeof(int2), cudaMemcpyDeviceToHost));
+    QD_CUDA(cudaMemcpyAsync(runs.data(), f->runs.p, runs.size() * sizeof(uint4), cudaMemcpyDeviceToHost,
+                            H->ctx->stream));
+    QD_CUDA(cudaMemcpyAsync(dtab.data(), f->dtab.p, dtab.size() * sizeof(int2), cudaMemcpyDeviceToHost,
+                            H->ctx->stream));
+    QD_CUDA(cudaStreamSynchronize(H->ctx->stream));
     std::vector<std::vector<int64_t>> flips(runs.size());
     for (size_t q = 0; q < runs.size(); ++q) flips[q].assign((size_t)runs[q].y + 1, -1);
     // recover each run slot's flips from its entries: a pattern with weight 1 took one transition
@@ -644,6 +652,24 @@ void launch_fx_slots(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x
                                                                                     scale_dev, stop, step);
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
+}
+
+// Rows of the slot form for the one-launch step (fxstep.cuh): the tables go
+// into shared memory after the w columns.
+struct SlotRowsBound {
+  FxSlotArgs A;
+  SlotSmem S;
+  const __int128* X;
+  __device__ __int128 row_sum(int64_t r) const { return slot_sum(A, S, X, __ldcs(A.basis + r), (int)r); }
+};
+struct SlotRows {
+  FxSlotArgs A;
+  const __int128* X;
+  __device__ SlotRowsBound bind(unsigned char* smem) const { return SlotRowsBound{A, stage_slots(A, smem), X}; }
+};
+
+bool launch_fx_slots_step(Ctx* ctx, const qd_ham* H, const FxForm& f, const FxStepArgs& a, int grid) {
+  return fx_step_launch(ctx, SlotRows{slot_args(H, f), a.X}, a, grid, slot_smem(f));
 }
 
 void launch_fx_slots_dots(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x, const __int128* X,

@@ -1,0 +1,222 @@
+// fxstep.cuh -- one Lanczos step of the uniform-coupling form in one launch.
+//
+// A step of sparse_algorithm.hpp:395-425 is w = H v1; alpha, beta from
+// <v2,w>, <v1,w>, <v1,v2>; v_k = (w - beta v2) - alpha v1; n_k = ||v_k||.
+// Split in two launches (the fused product and dots, then the update) the
+// step writes w to HBM and reads it back, and pays a launch boundary with its
+// ramp and tail.  Here one cooperative launch does both halves: every thread
+// keeps the w of its own rows in shared memory (rows r = gtid + i * stride,
+// slot i * 256 + tid), the block that completes the grid reduction of the
+// three dots publishes alpha and beta and bumps an epoch word, every block
+// waits for the epoch (a bounded wait), and then updates the same rows it
+// produced (in adjacent pairs, for 16-byte accesses): reads v1, v2, writes
+// v_k, its fixed-point copy for the next product, and its share of ||v_k||^2.
+//
+// Per-element arithmetic is that of spmv_fx_dots_kernel + lz_update_kernel,
+// and the dots use the same grid, row order and reduction tree, so alpha,
+// beta and v_k carry the same bits as the two-launch step; only the norm's
+// reduction tree differs.
+#pragma once
+
+#include "fxsum.cuh"
+#include "vec.cuh"
+
+namespace qd {
+
+// Polls of the epoch word before a block gives up on the others (with the
+// back-off below, about a second; a healthy step waits a few microseconds).
+constexpr unsigned kStepSpinLimit = 1u << 22;
+
+struct FxStepArgs {
+  int64_t n;
+  const double* diag;
+  const double* x;      // V1, unnormalised (s1 = 1 / ||V1||)
+  const __int128* X;    // fixed-point copy of V1
+  const double* V2;     // V2 (kHas2), unnormalised (s2 = 1 / ||V2||)
+  double cF;            // c 2^-F
+  const double* s1;
+  const double* s2;
+  int* stop;
+  int step;
+  double* beta;
+  double* alpha;
+  Tri<double>* dots;
+  GridRed<Tri<double>> red;
+  unsigned* epoch;      // bumped once per launch by the block that publishes alpha and beta
+  double* Vk;
+  double* nrm2;
+  double* nrm;
+  double* sk;
+  GridRed<double> rd;
+  __int128* Xk;
+  int F;
+  int* ovf;             // ovf[0]: an element left the fixed-point range; ovf[1]: a wait ran out
+  int rows;             // rows per thread: the length of each thread's w column in shared memory
+};
+
+// Src supplies a row's fixed-point off-diagonal sum: bind(smem) once per
+// block (every thread calls it; it may stage tables in smem and ends with a
+// block barrier) returns an object whose row_sum(r) gives the row's sum.
+template <class Src, bool kHas2>
+__global__ void __launch_bounds__(256, 6) lz_fx_step_kernel(Src src, FxStepArgs a) {
+  if (a.stop) {
+    const int st = *a.stop;
+    if (st != 0 && st < a.step) return;
+  }
+  extern __shared__ __align__(16) unsigned char fx_step_smem[];
+  double* wst = reinterpret_cast<double*>(fx_step_smem);
+  __shared__ unsigned e0;
+  __shared__ int waited_out;
+  __shared__ double ab[2];
+  if (threadIdx.x == 0) {
+    e0 = *reinterpret_cast<volatile unsigned*>(a.epoch);
+    waited_out = 0;
+  }
+  const auto& rows = src.bind(fx_step_smem + (size_t)a.rows * 256 * sizeof(double));
+  __syncthreads();
+
+  // first half: w = s1 (d x + c 2^-F sum X) and the three dots
+  const double sc = *a.s1;
+  Tri<double> acc = vzero(Tri<double>{});
+  // row indices fit in 32 bits (the columns are int32); 32-bit indices keep
+  // the loop within the 40 registers of six resident blocks per SM
+  const int n = (int)a.n;
+  const int stride = (int)(gridDim.x * blockDim.x);
+  double* wp = wst + threadIdx.x;
+  for (int r = (int)(blockIdx.x * blockDim.x + threadIdx.x); r < n; r += stride, wp += 256) {
+    const __int128 s = rows.row_sum(r);
+    const double xr = __ldcs(a.x + r);
+    const double w = sc * fma(a.cF, (double)s, __ldcs(a.diag + r) * xr);
+    *wp = w;
+    acc.b = fma(xr, w, acc.b);
+    if (kHas2) {
+      const double v2 = __ldcs(a.V2 + r);
+      acc.a = fma(v2, w, acc.a);
+      acc.c = fma(xr, v2, acc.c);
+    }
+  }
+  if (grid_sum(acc, a.red, a.dots) && threadIdx.x == 0) {
+    const Tri<double> d = *a.dots;
+    const double bt = kHas2 ? (*a.s2) * d.a : 0.0;
+    double t = d.b;
+    if (kHas2) t = fma(-(bt * (*a.s2)), d.c, t);
+    *a.beta = bt;
+    *a.alpha = (*a.s1) * t;
+    __threadfence();
+    atomicAdd(a.epoch, 1u);
+  }
+  if (threadIdx.x == 0) {
+    unsigned polls = 0;
+    while (*reinterpret_cast<volatile unsigned*>(a.epoch) == e0) {
+      if (++polls > kStepSpinLimit) {
+        waited_out = 1;
+        atomicExch(a.ovf + 1, 1);
+        break;
+      }
+      __nanosleep(200);
+    }
+    __threadfence();
+    ab[0] = __ldcg(a.alpha);
+    ab[1] = __ldcg(a.beta);
+  }
+  __syncthreads();
+
+  // second half: v_k = (w - (beta s2) V2) - (alpha s1) V1 on the same rows
+  double acc0 = 0.0;
+  int out = 0;
+  if (!waited_out) {
+    const double al = (*a.s1) * ab[0];
+    const double bt = kHas2 ? (*a.s2) * ab[1] : 0.0;
+    // The block's rows of pass i are 256 consecutive rows; here thread t takes
+    // the adjacent pair 2 (t % 128) + {0, 1} of the passes i = t / 128 (mod 2),
+    // with 16-byte loads and stores, two passes per iteration.
+    const int m2 = (threadIdx.x & 127) * 2;
+    const int base = (int)(blockIdx.x * blockDim.x) + m2;
+    int i = threadIdx.x >> 7;
+    for (; i + 2 < a.rows; i += 4) {
+      const int ra = base + i * stride, rb = ra + 2 * stride;
+      if (rb + 1 >= n) break;
+      double2 oa = *reinterpret_cast<const double2*>(wst + i * 256 + m2);
+      double2 ob = *reinterpret_cast<const double2*>(wst + (i + 2) * 256 + m2);
+      const double2 qa = __ldcs(reinterpret_cast<const double2*>(a.x + ra));
+      const double2 qb = __ldcs(reinterpret_cast<const double2*>(a.x + rb));
+      if (kHas2) {
+        const double2 pa = __ldcs(reinterpret_cast<const double2*>(a.V2 + ra));
+        const double2 pb = __ldcs(reinterpret_cast<const double2*>(a.V2 + rb));
+        oa = make_double2(fma(-bt, pa.x, oa.x), fma(-bt, pa.y, oa.y));
+        ob = make_double2(fma(-bt, pb.x, ob.x), fma(-bt, pb.y, ob.y));
+      }
+      oa = make_double2(fma(-al, qa.x, oa.x), fma(-al, qa.y, oa.y));
+      ob = make_double2(fma(-al, qb.x, ob.x), fma(-al, qb.y, ob.y));
+      __stcs(reinterpret_cast<double2*>(a.Vk + ra), oa);
+      __stcs(reinterpret_cast<double2*>(a.Vk + rb), ob);
+      a.Xk[ra] = fx_from_double(oa.x, a.F, &out);
+      a.Xk[ra + 1] = fx_from_double(oa.y, a.F, &out);
+      a.Xk[rb] = fx_from_double(ob.x, a.F, &out);
+      a.Xk[rb + 1] = fx_from_double(ob.y, a.F, &out);
+      acc0 = fma(oa.x, oa.x, acc0);
+      acc0 = fma(oa.y, oa.y, acc0);
+      acc0 = fma(ob.x, ob.x, acc0);
+      acc0 = fma(ob.y, ob.y, acc0);
+    }
+    for (; i < a.rows; i += 2) {
+      const int r = base + i * stride;
+      for (int u = 0; u < 2 && r + u < n; ++u) {
+        double o = wst[i * 256 + m2 + u];
+        if (kHas2) o = fma(-bt, a.V2[r + u], o);
+        o = fma(-al, a.x[r + u], o);
+        a.Vk[r + u] = o;
+        a.Xk[r + u] = fx_from_double(o, a.F, &out);
+        acc0 = fma(o, o, acc0);
+      }
+    }
+  }
+  if (out) a.ovf[0] = 1;
+  // every block arrives here, waited out or not, so the ticket counts stay whole
+  if (grid_sum(acc0, a.rd, a.nrm2) && threadIdx.x == 0) {
+    const double nr = sqrt(*a.nrm2);
+    *a.nrm = nr;
+    *a.sk = 1.0 / nr;
+    if (nr < 1e-10 && a.stop && *a.stop == 0) *a.stop = a.step;  // sparse_algorithm.hpp:421
+  }
+}
+
+// Launch one step on `grid` blocks (the grid of the two-launch product, so
+// that the dots keep their reduction tree) as a cooperative launch, which
+// makes every block resident at once.  Returns false, launching nothing, when
+// the w columns and the source's tables do not leave room for the whole grid
+// on the device at once; the caller then runs the two-launch step.
+template <class Src>
+bool fx_step_launch(Ctx* ctx, const Src& src, FxStepArgs a, int grid, size_t table_smem) {
+  static int coop = -1;
+  if (coop < 0) {
+    int v = 0;
+    QD_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrCooperativeLaunch, ctx->device));
+    coop = v;
+  }
+  const int64_t per = (int64_t)grid * 256;
+  if (!coop || a.n <= 0 || a.n > INT32_MAX - per) return false;
+  a.rows = (int)((a.n + per - 1) / per);
+  const size_t smem = (size_t)a.rows * 256 * sizeof(double) + table_smem;
+  if (smem > 200 * 1024) return false;
+  auto kern = a.V2 ? lz_fx_step_kernel<Src, true> : lz_fx_step_kernel<Src, false>;
+  if (smem > 48 * 1024) QD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int occ = 0;
+  QD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, 256, smem));
+  if ((int64_t)occ * ctx->num_sms < grid) return false;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = ctx->stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  QD_CUDA(cudaLaunchKernelEx(&cfg, kern, src, a));
+  QD_LAUNCHED(ctx);
+  return true;
+}
+
+}  // namespace qd

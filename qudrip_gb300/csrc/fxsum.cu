@@ -5,6 +5,7 @@
 #include <cstdlib>
 #include <cstring>
 
+#include "fxstep.cuh"
 #include "fxsum.cuh"
 #include "ham.cuh"
 #include "krylov.cuh"
@@ -166,16 +167,22 @@ bool ham_build_fx(qd_ham* H) {
 // keep their gather order.
 
 // Sum of the row's fixed-point gathers: four columns per 16-byte load, four
-// predicated gathers in flight.
+// predicated gathers in flight, and the next group's columns loaded before
+// the current group's gathers.  The first group is loaded before the row's
+// count is known: a row with no columns reads four padding entries (the
+// column array carries 128 entries of tail padding, zeros).
 __device__ __forceinline__ __int128 sell_row_sum(const int4* __restrict__ c4, int e, const __int128* __restrict__ X) {
   __int128 s = 0;
+  int4 cc = __ldcs(c4);
   for (int k = 0; k < e; k += 4) {
-    const int4 cc = __ldcs(c4 + 8 * k);  // group k / 4 starts 32 int4 further on
+    int4 nc = cc;
+    if (k + 4 < e) nc = __ldcs(c4 + 8 * (k + 4));  // group k / 4 starts 32 int4 further on
     __int128 x0 = X[cc.x], x1 = 0, x2 = 0, x3 = 0;
     if (k + 1 < e) x1 = X[cc.y];
     if (k + 2 < e) x2 = X[cc.z];
     if (k + 3 < e) x3 = X[cc.w];
     s += (x0 + x1) + (x2 + x3);
+    cc = nc;
   }
   return s;
 }
@@ -327,6 +334,31 @@ void launch_fx_dots(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x,
                                                             red);
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
+}
+
+// Rows of the stored-column form for the one-launch step (fxstep.cuh).
+struct SellRows {
+  const int64_t* soff;
+  const int32_t* scol;
+  const uint8_t* slen;
+  const __int128* X;
+  __device__ const SellRows& bind(unsigned char*) const { return *this; }
+  __device__ __int128 row_sum(int64_t r) const { return sell_row_sum(sell_row(soff, scol, r), __ldcs(slen + r), X); }
+};
+
+bool launch_fx_step(Ctx* ctx, const qd_ham* H, const FxForm& f, FxStepArgs a) {
+  a.n = H->dim;
+  a.diag = f.diag.p;
+  a.cF = std::ldexp(f.c, -f.F);
+  a.F = f.F;
+  const int g = fx_dots_grid(ctx, H->dim);
+  bool ok = false;
+  if (g <= kMaxGrid)
+    ok = (f.slots_state > 0 && f.use_slots)
+             ? launch_fx_slots_step(ctx, H, f, a, g)
+             : fx_step_launch(ctx, SellRows{f.sell_off.p, f.sell_col.p, f.sell_len.p, a.X}, a, g, 0);
+  f.step_fused = ok ? 1 : -1;
+  return ok;
 }
 
 // X = fixed-point copy of x (v_0 of a Lanczos run).

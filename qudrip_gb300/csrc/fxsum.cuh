@@ -88,6 +88,7 @@ struct FxForm {
   // the columns as the product reads them: 32-row slices, entry k of row 32 s + l
   // at sell_off[s] + 128 (k / 4) + 4 l + k % 4 (fxsum.cu), the row's count in sell_len
   int64_t sell_cols = 0;  // stored slots, padding included
+  mutable int step_fused = 0;  // the last Lanczos step on this form: 1 one launch (fxstep.cuh), -1 two
   DBuf<int64_t> sell_off;
   DBuf<int32_t> sell_col;
   DBuf<uint8_t> sell_len;

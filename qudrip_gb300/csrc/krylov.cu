@@ -23,6 +23,7 @@
 #include <cstring>
 #include <vector>
 
+#include "fxstep.cuh"
 #include "krylov.cuh"
 #include "spmv.cuh"
 #include "tridiag.cuh"
@@ -425,6 +426,24 @@ void state_norm2_eval(qd_ham* H, const cplx* psi, double* n2, cplx* e) {
 }
 
 // The product the real Lanczos path launches, timed back to back.
+// The one-launch step of the uniform-coupling form is the default;
+// QD_LANCZOS_STEP=split keeps the product and the update in two launches.
+// (read per run; a captured recurrence keeps the form it was captured with)
+static bool fx_one_launch_step() {
+  const char* e = std::getenv("QD_LANCZOS_STEP");
+  return !(e && std::strcmp(e, "split") == 0);
+}
+
+// Overflow flag of a fixed-point run (nonzero: rerun on the FP64 product);
+// a bounded device wait that ran out is an error.
+static int fx_flags(Ctx* ctx, const int* flags) {
+  int f[2] = {0, 0};
+  QD_CUDA(cudaMemcpyAsync(f, flags, sizeof(f), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  QD_REQUIRE(!f[1], QD_ERR_TIMEOUT, "a Lanczos step's blocks did not meet within the wait limit");
+  return f[0];
+}
+
 void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per_launch) {
   Ctx* ctx = H->ctx;
   Workspace& W = ham_workspace(H);
@@ -465,7 +484,40 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   const bool slots = fx && H->fx->use_slots && H->fx->slots_state > 0;
   DBuf<__int128> X((fx || mfx) ? n + 32 : 1);
   if (fx || mfx) QD_CUDA(cudaMemsetAsync(X.p, 0, X.bytes(), ctx->stream));
+  // what the Lanczos recurrence launches on the uniform-coupling form: the
+  // whole step in one launch (product, dots, update, fixed-point copy, norm)
+  const FxForm* step_form = mfx ? H->mfx.get() : ((fx && spmv == QD_SPMV_CSR) ? H->fx.get() : nullptr);
+  if (!fx_one_launch_step()) step_form = nullptr;
+  DBuf<__int128> X2(step_form ? n + 32 : 1);
+  DBuf<unsigned> ep(1);
+  DBuf<int> flags(2);
+  QD_CUDA(cudaMemsetAsync(ep.p, 0, sizeof(unsigned), ctx->stream));
+  QD_CUDA(cudaMemsetAsync(flags.p, 0, 2 * sizeof(int), ctx->stream));
+  bool stepped = false;
   auto launch = [&]() {
+    if (step_form) {
+      double* d = (double*)scal.p;
+      FxStepArgs a{};
+      a.x = (const double*)x.p;
+      a.X = X.p;
+      a.V2 = (const double*)z.p;
+      a.s1 = s1;
+      a.s2 = s1;
+      a.beta = d + 1;
+      a.alpha = d + 2;
+      a.dots = reinterpret_cast<Tri<double>*>(d + 6);
+      a.red = W.red_tri<double>(2);
+      a.epoch = ep.p;
+      a.Vk = (double*)t.p;
+      a.nrm2 = d + 3;
+      a.nrm = d + 4;
+      a.sk = d + 5;
+      a.rd = W.red_d_flat(3);
+      a.Xk = X2.p;
+      a.ovf = flags.p;
+      stepped = launch_fx_step(ctx, H, *step_form, a);
+      if (stepped) return;
+    }
     if (mfx) {
       double* d = (double*)scal.p;
       launch_fx_dots(ctx, H, *H->mfx, (const double*)x.p, X.p, (const double*)z.p, (double*)y.p, s1, s1, nullptr,
@@ -535,6 +587,12 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
                         (double)n * (8.0 + 8.0 + 16.0 + 8.0 + (spmv == QD_SPMV_CSR ? 8.0 : 0.0));
   if (slots)  // 32-bit state, diagonal, x, its fixed-point copy once, y (+ v2)
     *bytes_per_launch = (double)n * (4.0 + 8.0 + 8.0 + 16.0 + 8.0 + (spmv == QD_SPMV_CSR ? 8.0 : 0.0));
+  if (stepped)  // one Lanczos step: w stays on chip; v_k and its fixed-point copy are written
+    *bytes_per_launch += (double)n * (8.0 + 16.0 - 8.0);
+  int fl[2] = {0, 0};
+  QD_CUDA(cudaMemcpyAsync(fl, flags.p, sizeof(fl), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  QD_REQUIRE(!fl[1], QD_ERR_TIMEOUT, "a timed step's blocks did not meet within the wait limit");
 }
 
 // ---------------------------------------------------------------- Lanczos
@@ -545,6 +603,11 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int k_
                         bool mf, int fxk = 0, const FxForm* form = nullptr) {
   Ctx* ctx = H->ctx;
   const int64_t n = H->dim;
+  // requests of the serving loop share the device with other lanes' kernels,
+  // and a cooperative launch waits for room for its whole grid: they keep the
+  // two-launch step
+  const bool one_launch = fxk == 1 && fx_one_launch_step() && !H->one_shot;
+  if (fxk == 1 && !one_launch) form->step_fused = -1;
   for (int k = k_first; k <= k_last; ++k) {
     const VV* V1 = B.V.p + (int64_t)(k - 1) * B.ld;
     const VV* V2 = (k >= 2) ? B.V.p + (int64_t)(k - 2) * B.ld : nullptr;
@@ -554,8 +617,31 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int k_
     // K1: w = s1 * H V1 (CSR, fixed-point uniform-coupling form, or matrix-free)
     __int128* Xprev = (fxk == 1) ? B.X.p + (int64_t)((k - 1) & 1) * B.ld : nullptr;
     __int128* Xnext = (fxk == 1) ? B.X.p + (int64_t)(k & 1) * B.ld : nullptr;
-    if constexpr (std::is_same<VV, double>::value) {  // product fused with the step's inner products
-      if (fxk == 1)
+    if constexpr (std::is_same<VV, double>::value) {
+      if (one_launch) {  // the whole step in one launch (fxstep.cuh)
+        FxStepArgs a{};
+        a.x = V1;
+        a.X = Xprev;
+        a.V2 = V2;
+        a.s1 = s1;
+        a.s2 = s2;
+        a.stop = B.stop.p;
+        a.step = k;
+        a.beta = B.beta.p + k;
+        a.alpha = B.alpha.p + k;
+        a.dots = B.dots.p + k;
+        a.red = W.red_tri<double>(2);
+        a.epoch = B.epoch.p;
+        a.Vk = Vk;
+        a.nrm2 = B.nrm2.p + k;
+        a.nrm = B.nrm.p + k;
+        a.sk = B.scl.p + k;
+        a.rd = W.red_d_flat(3);
+        a.Xk = Xnext;
+        a.ovf = B.ovf.p;
+        if (launch_fx_step(ctx, H, *form, a)) continue;
+      }
+      if (fxk == 1)  // product fused with the step's inner products, then the update
         launch_fx_dots(ctx, H, *form, V1, Xprev, V2, B.w.p, s1, s2, B.stop.p, k, B.beta.p + k, B.alpha.p + k,
                        B.dots.p + k,
                        W.red_tri<double>(2));
@@ -627,14 +713,14 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
   fxk = form ? 1 : 0;
   const bool fx = fxk == 1;
   const int fxF = fx ? form->F : 0;
-  const int kind = (mf ? 1 : 0) + 2 * fxk;
+  const int kind = (mf ? 1 : 0) + 2 * fxk + ((fx && fx_one_launch_step() && !H->one_shot) ? 4 : 0);
   if (B.kind != kind) {
     B.drop_graph();
     B.kind = kind;
   }
   if (fx) {
-    B.ensure_fx();
-    QD_CUDA(cudaMemsetAsync(B.ovf.p, 0, sizeof(int), ctx->stream));
+    B.ensure_fx(ctx->stream);
+    QD_CUDA(cudaMemsetAsync(B.ovf.p, 0, 2 * sizeof(int), ctx->stream));
     if constexpr (std::is_same<VV, double>::value) launch_fx_shadow(ctx, n, B.V.p, B.X.p, fxF, B.ovf.p);
   }
   const int steps = (o.add_dim > 0 && o.add_dim < kdim) ? o.add_dim : kdim;  // add_dim of an incremental start
@@ -648,9 +734,7 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
   W.lz_mf = mf;
   W.lz_fxk = fxk;
   if (fx) {
-    int ov = 0;
-    QD_CUDA(cudaMemcpyAsync(&ov, B.ovf.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    QD_CUDA(cudaStreamSynchronize(ctx->stream));
+    const int ov = fx_flags(ctx, B.ovf.p);
     if (ov) {  // a vector left the fixed-point range: redo the solve on the FP64 CSR product
       H->fx_allowed = false;
       lanczos_ground_impl<MV, VV>(H, psi, psi_nrm2, o, evals_out, res);
@@ -711,10 +795,11 @@ static void lanczos_finish(qd_ham* H, cplx* psi, const double* psi_nrm2, const q
     QD_LAUNCHED(ctx);
     QD_CUDA(cudaMemsetAsync(B.stop.p, 0, sizeof(int), ctx->stream));
     if (fx) {
-      QD_CUDA(cudaMemsetAsync(B.ovf.p, 0, sizeof(int), ctx->stream));
+      QD_CUDA(cudaMemsetAsync(B.ovf.p, 0, 2 * sizeof(int), ctx->stream));
       if constexpr (std::is_same<VV, double>::value) launch_fx_shadow(ctx, n, B.V.p, B.X.p, fxF, B.ovf.p);
     }
     lanczos_run<MV, VV>(H, vals, B, 1, act, W, mf, fxk, form);
+    if (fx) fx_flags(ctx, B.ovf.p);
     matvecs += act;
   }
   // psi = sum_k y_k v_k = sum_k (y_k s_k) V[k]
@@ -758,9 +843,7 @@ static void lanczos_extend_impl(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, 
     B.done += add;
   }
   if (W.lz_fxk == 1) {
-    int ov = 0;
-    QD_CUDA(cudaMemcpyAsync(&ov, B.ovf.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    QD_CUDA(cudaStreamSynchronize(ctx->stream));
+    const int ov = fx_flags(ctx, B.ovf.p);
     QD_REQUIRE(!ov, QD_ERR_OVERFLOW, "a Lanczos vector left the fixed-point range; restart the solve");
   }
   qd_lanczos_opts o2 = o;

@@ -27,14 +27,17 @@ struct LanczosBuffers {
   DBuf<double> nrm, nrm2, y, scl;  // scl[k] = 1 / ||V[k]|| (basis stored unnormalised)
   DBuf<int> stop;
   DBuf<__int128> X;  // fixed-point copies of the two newest basis vectors (uniform-coupling product)
-  DBuf<int> ovf;
+  DBuf<int> ovf;         // [0] a vector left the fixed-point range, [1] a bounded device wait ran out
+  DBuf<unsigned> epoch;  // barrier word of the one-launch step (fxstep.cuh)
   cudaGraphExec_t exec = nullptr;
-  int kind = 0;  // product the captured graph launches (0 CSR, 1 matrix-free, 2 fixed-point)
+  int kind = 0;  // product the captured graph launches (0 CSR, 1 matrix-free, 2 fixed-point, +4 one-launch step)
   int done = 0;  // Lanczos steps run on the stored basis (incremental solves continue from here)
-  void ensure_fx() {
+  void ensure_fx(cudaStream_t s) {  // stream-ordered: a legacy-stream call would wait for every lane
     if (!X.p) {
       X.alloc((size_t)2 * ld);
-      ovf.alloc(1);
+      ovf.alloc(2);
+      epoch.alloc(1);
+      QD_CUDA(cudaMemsetAsync(epoch.p, 0, sizeof(unsigned), s));
     }
   }
   int64_t graph_kernels = 0;
@@ -144,6 +147,11 @@ void launch_fx_slots(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x
 void launch_fx_slots_dots(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x, const __int128* X,
                           const double* V2, double* y, const double* s1, const double* s2, const int* stop, int step,
                           double* beta, double* alpha, Tri<double>* dots, GridRed<Tri<double>> red, int grid);
+struct FxStepArgs;
+// One Lanczos step of the uniform-coupling form in one cooperative launch
+// (fxstep.cuh); false when it does not fit on the device at once.
+bool launch_fx_step(Ctx* ctx, const qd_ham* H, const FxForm& f, FxStepArgs a);
+bool launch_fx_slots_step(Ctx* ctx, const qd_ham* H, const FxForm& f, const FxStepArgs& a, int grid);
 template <typename VV>
 void launch_mf(Ctx* ctx, qd_ham* H, const VV* x, VV* y, double scale, const double* scale_dev, const int* stop,
                int step);

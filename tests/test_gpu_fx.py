@@ -129,7 +129,8 @@ def test_columns_on_the_fly_timing_and_fallback(ctx):
     assert ms.value > 0 and nb.value == sec.dim * (4 + 8 + 8 + 16 + 8)
     A.call("qd_ham_set_spmv_kernel", H.handle, A.QD_SPMV_FX_SLOTS)
     A.call("qd_ham_time_spmv", H.handle, A.QD_SPMV_CSR, 5, C.byref(ms), C.byref(nb))  # what Lanczos launches
-    assert nb.value == sec.dim * (4 + 8 + 8 + 16 + 8 + 8)
+    # the whole Lanczos step in one launch: w stays on chip, v_k (8) and its fixed-point copy (16) are written
+    assert nb.value == sec.dim * (4 + 8 + 8 + 16 + 8 + 8) + sec.dim * 16
     # a term on 7 sites is beyond the compiled form: the stored columns stay, 121 is refused, 120 runs
     from qudrip_gb300.operators import II, SectorSpec, getBoseGate, getEmptyOperator, getNset, getQbits
     pre = getQbits(12)
@@ -148,3 +149,29 @@ def test_columns_on_the_fly_timing_and_fallback(ctx):
         with pytest.raises(A.QDError) as e:
             A.call("qd_ham_set_spmv_kernel", H2.handle, A.QD_SPMV_FX_SLOTS)
         assert e.value.code == A.QD_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("L,fields,kernel", [(16, None, None), (14, "random", None), (14, None, 121)])
+def test_one_launch_step_matches_two_launch_step(ctx, monkeypatch, L, fields, kernel):
+    """The default Lanczos step of the uniform-coupling form is one cooperative launch (product, dots,
+    update, norm); QD_LANCZOS_STEP=split runs the product with its dots and the update as two launches.
+    alpha, beta and v_k carry the same bits; only the norm's reduction order differs."""
+    h = np.random.default_rng(L).uniform(-1, 1, L) if fields else None
+    spec, ham = chains.xxz_chain(L, 1.0, 0.7, periodic=True, fields=h)
+    v0 = q.start_vector(q.Sector(spec.index, spec.constraints).dim, 5)
+    sec, H = gpu_objects(spec, ham)
+    r1, psi1 = solve(sec, H, v0, 80, kernel=kernel)
+    info = A.qd_ham_info()
+    A.call("qd_ham_get_info", H.handle, C.byref(info))
+    assert info.step_launches == 1
+    monkeypatch.setenv("QD_LANCZOS_STEP", "split")
+    sec2, H2 = gpu_objects(spec, ham)
+    r2, psi2 = solve(sec2, H2, v0, 80, kernel=kernel)
+    A.call("qd_ham_get_info", H2.handle, C.byref(info))
+    assert info.step_launches == 2
+    assert r1.act_dim == r2.act_dim and r1.matvecs == r2.matvecs
+    assert abs(r1.ritz_value - r2.ritz_value) <= 1e-13 * abs(r2.ritz_value)
+    ov = abs(np.vdot(psi1, psi2)) / (np.linalg.norm(psi1) * np.linalg.norm(psi2))
+    assert ov >= 1 - 1e-10
+    o = O.Ham(O.Sector(spec), ham).lanczos_ground(v0, 80)
+    assert abs(r1.ritz_value - o["ritz"]) <= 1e-10 * abs(o["ritz"])
