@@ -300,7 +300,7 @@ def gpu_arm(args, rank, world, local):
     # the same unit; its own byte count is reported beside).  Where the whole
     # Lanczos step is one launch the unit is one step: the matrix, v1 and v2
     # read once, v_k written once (w never leaves the chip):
-    # nnz*12 + (dim+1)*4 + dim*24 = 514,494,324 B.
+    # nnz*12 + (dim+1)*4 + dim*24 = 514,495,076 B.
     info = A.qd_ham_info()
     A.call("qd_ham_get_info", H.handle, C.byref(info))
     one_launch = info.step_launches == 1
