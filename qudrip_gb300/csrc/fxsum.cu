@@ -174,6 +174,7 @@ bool ham_build_fx(qd_ham* H) {
 __device__ __forceinline__ __int128 sell_row_sum(const int4* __restrict__ c4, int e, const __int128* __restrict__ X) {
   __int128 s = 0;
   int4 cc = __ldcs(c4);
+#pragma unroll 1
   for (int k = 0; k < e; k += 4) {
     int4 nc = cc;
     if (k + 4 < e) nc = __ldcs(c4 + 8 * (k + 4));  // group k / 4 starts 32 int4 further on
