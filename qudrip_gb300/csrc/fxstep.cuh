@@ -188,12 +188,11 @@ __global__ void __launch_bounds__(256, 6) lz_fx_step_kernel(Src src, FxStepArgs 
 // on the device at once; the caller then runs the two-launch step.
 template <class Src>
 bool fx_step_launch(Ctx* ctx, const Src& src, FxStepArgs a, int grid, size_t table_smem) {
-  static int coop = -1;
-  if (coop < 0) {
+  static const int coop = [&] {  // once per process (thread-safe initialisation)
     int v = 0;
-    QD_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrCooperativeLaunch, ctx->device));
-    coop = v;
-  }
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrCooperativeLaunch, ctx->device) != cudaSuccess) v = 0;
+    return v;
+  }();
   const int64_t per = (int64_t)grid * 256;
   if (!coop || a.n <= 0 || a.n > INT32_MAX - per) return false;
   a.rows = (int)((a.n + per - 1) / per);
