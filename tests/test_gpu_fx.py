@@ -175,3 +175,23 @@ def test_one_launch_step_matches_two_launch_step(ctx, monkeypatch, L, fields, ke
     assert ov >= 1 - 1e-10
     o = O.Ham(O.Sector(spec), ham).lanczos_ground(v0, 80)
     assert abs(r1.ritz_value - o["ritz"]) <= 1e-10 * abs(o["ritz"])
+
+
+def test_large_sector_takes_the_two_launch_step(ctx):
+    """XXZ L=26 (dim 10,400,600): the one-launch step would keep 45 rows of w per thread in shared
+    memory (90 KB per block), room for two of its 912 blocks per SM, so it cannot be resident at once
+    and the recurrence runs the product and the update as two launches; the result agrees with the
+    FP64 CSR product."""
+    spec, ham = chains.xxz_chain(26, 1.0, 1.0, periodic=True)
+    sec, H = gpu_objects(spec, ham)
+    assert sec.dim == 10400600
+    v0 = q.start_vector(sec.dim, 3)
+    r_fx, psi_fx = solve(sec, H, v0, 30)
+    info = A.qd_ham_info()
+    A.call("qd_ham_get_info", H.handle, C.byref(info))
+    assert info.product_kernel == A.QD_SPMV_FX and info.step_launches == 2
+    r_csr, psi_csr = solve(sec, H, v0, 30, kernel=110)
+    assert r_fx.act_dim == r_csr.act_dim == 30
+    assert abs(r_fx.ritz_value - r_csr.ritz_value) <= 1e-12 * abs(r_csr.ritz_value)
+    ov = abs(np.vdot(psi_fx, psi_csr)) / (np.linalg.norm(psi_fx) * np.linalg.norm(psi_csr))
+    assert ov >= 1 - 1e-10
