@@ -1,5 +1,6 @@
 """Uniform-coupling product with exact fixed-point sums (kernel code 120) vs the FP64 CSR path and the oracle."""
 import ctypes as C
+import os
 
 import numpy as np
 import pytest
@@ -12,6 +13,12 @@ from qudrip_gb300 import chains
 from test_gpu_parity import gpu_objects
 
 pytestmark = pytest.mark.gpu
+
+
+def one_launch_extra():
+    """Bytes per row the one-launch Lanczos step adds to the product's count (v_k 8 and its fixed-point
+    copy 16 written, w 8 not); 0 when QD_LANCZOS_STEP=split keeps the step in two launches."""
+    return 0 if os.environ.get("QD_LANCZOS_STEP") == "split" else 16
 
 
 def solve(sec, H, v0, kry, kernel=None):
@@ -130,7 +137,7 @@ def test_columns_on_the_fly_timing_and_fallback(ctx):
     A.call("qd_ham_set_spmv_kernel", H.handle, A.QD_SPMV_FX_SLOTS)
     A.call("qd_ham_time_spmv", H.handle, A.QD_SPMV_CSR, 5, C.byref(ms), C.byref(nb))  # what Lanczos launches
     # the whole Lanczos step in one launch: w stays on chip, v_k (8) and its fixed-point copy (16) are written
-    assert nb.value == sec.dim * (4 + 8 + 8 + 16 + 8 + 8) + sec.dim * 16
+    assert nb.value == sec.dim * (4 + 8 + 8 + 16 + 8 + 8) + sec.dim * one_launch_extra()
     # a term on 7 sites is beyond the compiled form: the stored columns stay, 121 is refused, 120 runs
     from qudrip_gb300.operators import II, SectorSpec, getBoseGate, getEmptyOperator, getNset, getQbits
     pre = getQbits(12)
