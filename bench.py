@@ -11,8 +11,11 @@ vector) with the Hamiltonian and start vector already in HBM.
   e2e      the same metric through the public API with host buffers: each step
            uploads the start vector from pinned memory, solves, evaluates
            psi.eval and downloads the Ritz vector
-  roofline achieved HBM GB/s of the CSR product kernel: algorithmic bytes
-           nnz*(8+4) + (dim+1)*8 + 2*dim*8 per launch / CUDA-event time
+  roofline achieved HBM GB/s of the kernel the recurrence launches, per launch
+           over its CUDA-event time: for the one-launch Lanczos step (the
+           default for uniform couplings) the step's algorithmic bytes
+           nnz*(8+4) + (dim+1)*4 + dim*24 (matrix, v1, v2, v_k); for a product
+           launched alone one FP64 CSR matvec, nnz*(8+4) + (dim+1)*4 + dim*16
   cpu_baseline  the CPU oracle port (the reference's CSC column-push product,
            complex128, one core like the reference) on a bounded sample
 
