@@ -467,16 +467,17 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const B
 // Launches kernel C over `count` instances of `list` with `grid` CTAs
 // (clusters of C CTAs for C > 1).
 template <int C>
-static void launch_batch(Ctx* ctx, const BatchInst* list, int count, unsigned* counter, double* tri_work, int grid) {
+static void launch_batch(Ctx* ctx, cudaStream_t stream, const BatchInst* list, int count, unsigned* counter,
+                         double* tri_work, int grid) {
   if (count <= 0) return;
   if constexpr (C == 1) {
-    batch_lanczos_kernel<1><<<grid, kBatchThreads, 0, ctx->stream>>>(list, count, counter, tri_work);
+    batch_lanczos_kernel<1><<<grid, kBatchThreads, 0, stream>>>(list, count, counter, tri_work);
   } else {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3(kBatchThreads);
     cfg.dynamicSmemBytes = 0;
-    cfg.stream = ctx->stream;
+    cfg.stream = stream;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = C;
@@ -585,21 +586,52 @@ void batch_lanczos(Ctx* ctx, qd_ham* const* hams, const double* const* v0s, int 
   const int nsmall = ninst - nlarge;
   const int grid_large = nlarge ? kClusterCtas * std::min(nlarge, nclusters) : 0;
   const int grid_small = nsmall ? std::min(nsmall, 2 * ctx->num_sms) : 0;
-  DBuf<double> tri_work((size_t)std::max(std::max(grid_large, grid_small), 1) * 8 * (kBatchMaxSteps + 2));
+  // one scratch region per CTA of either launch (they may run at the same time)
+  DBuf<double> tri_work((size_t)std::max(grid_large + grid_small, 1) * 8 * (kBatchMaxSteps + 2));
+  double* tri_small = tri_work.p + (size_t)grid_large * 8 * (kBatchMaxSteps + 2);
+  // With both classes present the cluster launch goes on a high-priority side
+  // stream and the single-CTA launch beside it on the context's stream: the
+  // clusters are placed first, and single CTAs take the SM slots the clusters
+  // leave (and free at the end).  Every instance is computed by its own CTAs
+  // in a fixed order, so the results do not depend on the overlap.
+  struct Side {
+    cudaStream_t s = nullptr;
+    cudaEvent_t in = nullptr, done = nullptr;
+    ~Side() {
+      if (in) cudaEventDestroy(in);
+      if (done) cudaEventDestroy(done);
+      if (s) cudaStreamDestroy(s);
+    }
+  } side;
+  cudaStream_t large_stream = ctx->stream;
+  if (nlarge > 0 && nsmall > 0) {
+    int least = 0, greatest = 0;
+    QD_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    QD_CUDA(cudaStreamCreateWithPriority(&side.s, cudaStreamNonBlocking, greatest));
+    QD_CUDA(cudaEventCreateWithFlags(&side.in, cudaEventDisableTiming));
+    QD_CUDA(cudaEventCreateWithFlags(&side.done, cudaEventDisableTiming));
+    QD_CUDA(cudaEventRecord(side.in, ctx->stream));  // the list, the start vectors and the counters are in place
+    QD_CUDA(cudaStreamWaitEvent(side.s, side.in, 0));
+    large_stream = side.s;
+  }
   const bool timing = std::getenv("QD_TIMING") != nullptr;
   if (timing) QD_CUDA(cudaEventRecord(ctx->events[12], ctx->stream));
-  launch_batch<kClusterCtas>(ctx, dlist.p, nlarge, counter.p, tri_work.p, grid_large);
-  if (timing) QD_CUDA(cudaEventRecord(ctx->events[13], ctx->stream));
-  launch_batch<1>(ctx, dlist.p + nlarge, nsmall, counter.p + 1, tri_work.p, grid_small);
+  launch_batch<kClusterCtas>(ctx, large_stream, dlist.p, nlarge, counter.p, tri_work.p, grid_large);
+  launch_batch<1>(ctx, ctx->stream, dlist.p + nlarge, nsmall, counter.p + 1, tri_small, grid_small);
   if (timing) QD_CUDA(cudaEventRecord(ctx->events[14], ctx->stream));
+  if (side.s) {
+    QD_CUDA(cudaEventRecord(side.done, side.s));
+    QD_CUDA(cudaStreamWaitEvent(ctx->stream, side.done, 0));
+  }
+  if (timing) QD_CUDA(cudaEventRecord(ctx->events[13], ctx->stream));
   QD_CUDA(cudaMemcpyAsync(out, dout.p, (size_t)ninst * 8 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
   if (timing) {
     float a = 0.f, b = 0.f;
     QD_CUDA(cudaEventElapsedTime(&a, ctx->events[12], ctx->events[13]));
-    QD_CUDA(cudaEventElapsedTime(&b, ctx->events[13], ctx->events[14]));
-    std::fprintf(stderr, "[qd timing] batch: %d large on %d clusters %.3f ms, %d small on %d CTAs %.3f ms\n", nlarge,
-                 grid_large / kClusterCtas, a, nsmall, grid_small, b);
+    QD_CUDA(cudaEventElapsedTime(&b, ctx->events[12], ctx->events[14]));
+    std::fprintf(stderr, "[qd timing] batch: %d large on %d clusters, %d small on %d CTAs: all done at %.3f ms, "
+                 "small done at %.3f ms\n", nlarge, grid_large / kClusterCtas, nsmall, grid_small, a, b);
   }
 }
 
