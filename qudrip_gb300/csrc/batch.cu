@@ -5,7 +5,10 @@
 //   * small instances: one CTA owns one instance at a time and takes the next
 //     one from an atomic counter;
 //   * large instances (dim >= kClusterMinDim): a thread-block cluster of
-//     kClusterCtas CTAs owns one instance; each CTA keeps a slice of the rows
+//     8, 4 or 2 CTAs owns one instance (per call, the largest size at which
+//     every large instance of the call is resident at once, else 2: more
+//     instances side by side beat wider clusters once the device is full, and
+//     an instance's bits depend on this size); each CTA keeps a slice of the rows
 //     of every vector, and the inner products are combined through
 //     distributed shared memory (each CTA adds the CTAs' partials in rank
 //     order, so every CTA holds the same bits) between hardware cluster
@@ -47,7 +50,7 @@ namespace qd {
 constexpr int kBatchThreads = 512;  // two CTAs per SM
 constexpr int kBatchMaxSteps = 256;
 constexpr int kChunk = 64;  // FP32 partial sums cover at most this many elements
-constexpr int kClusterCtas = 8;          // CTAs of a cluster that shares one large instance
+constexpr int kClusterCtasMax = 8;  // CTAs of a cluster that shares one large instance: 8, 4 or 2 per call
 constexpr int64_t kClusterMinDim = 32768;
 
 struct BlockScratch {
@@ -559,7 +562,15 @@ void batch_lanczos(Ctx* ctx, qd_ham* const* hams, const double* const* v0s, int 
   std::vector<BatchInst> list(ninst);
   int nlarge = 0;
   for (int q = 0; q < ninst; ++q) nlarge += (hams[order[q]]->dim >= kClusterMinDim) ? 1 : 0;
-  const int nclusters = resident_clusters<kClusterCtas>(ctx);
+  // cluster size: the largest whose resident clusters hold every large instance at once, else 2
+  int ctas = 2, nclusters = resident_clusters<2>(ctx);
+  if (resident_clusters<8>(ctx) >= nlarge) {
+    ctas = 8;
+    nclusters = resident_clusters<8>(ctx);
+  } else if (resident_clusters<4>(ctx) >= nlarge) {
+    ctas = 4;
+    nclusters = resident_clusters<4>(ctx);
+  }
   if (nclusters < 1) nlarge = 0;  // no cluster fits: every instance on one CTA
   for (int q = 0; q < ninst; ++q) {
     const int i = order[q];
@@ -584,7 +595,7 @@ void batch_lanczos(Ctx* ctx, qd_ham* const* hams, const double* const* v0s, int 
   DBuf<unsigned> counter(2);
   QD_CUDA(cudaMemsetAsync(counter.p, 0, 2 * sizeof(unsigned), ctx->stream));
   const int nsmall = ninst - nlarge;
-  const int grid_large = nlarge ? kClusterCtas * std::min(nlarge, nclusters) : 0;
+  const int grid_large = nlarge ? ctas * std::min(nlarge, nclusters) : 0;
   const int grid_small = nsmall ? std::min(nsmall, 2 * ctx->num_sms) : 0;
   // one scratch region per CTA of either launch (they may run at the same time)
   DBuf<double> tri_work((size_t)std::max(grid_large + grid_small, 1) * 8 * (kBatchMaxSteps + 2));
@@ -616,7 +627,9 @@ void batch_lanczos(Ctx* ctx, qd_ham* const* hams, const double* const* v0s, int 
   }
   const bool timing = std::getenv("QD_TIMING") != nullptr;
   if (timing) QD_CUDA(cudaEventRecord(ctx->events[12], ctx->stream));
-  launch_batch<kClusterCtas>(ctx, large_stream, dlist.p, nlarge, counter.p, tri_work.p, grid_large);
+  if (ctas == 8) launch_batch<8>(ctx, large_stream, dlist.p, nlarge, counter.p, tri_work.p, grid_large);
+  else if (ctas == 4) launch_batch<4>(ctx, large_stream, dlist.p, nlarge, counter.p, tri_work.p, grid_large);
+  else launch_batch<2>(ctx, large_stream, dlist.p, nlarge, counter.p, tri_work.p, grid_large);
   launch_batch<1>(ctx, ctx->stream, dlist.p + nlarge, nsmall, counter.p + 1, tri_small, grid_small);
   if (timing) QD_CUDA(cudaEventRecord(ctx->events[14], ctx->stream));
   if (side.s) {
@@ -631,7 +644,7 @@ void batch_lanczos(Ctx* ctx, qd_ham* const* hams, const double* const* v0s, int 
     QD_CUDA(cudaEventElapsedTime(&a, ctx->events[12], ctx->events[13]));
     QD_CUDA(cudaEventElapsedTime(&b, ctx->events[12], ctx->events[14]));
     std::fprintf(stderr, "[qd timing] batch: %d large on %d clusters, %d small on %d CTAs: all done at %.3f ms, "
-                 "small done at %.3f ms\n", nlarge, grid_large / kClusterCtas, nsmall, grid_small, a, b);
+                 "small done at %.3f ms (%d-CTA clusters)\n", nlarge, grid_large / ctas, nsmall, grid_small, a, b, ctas);
   }
 }
 

@@ -59,9 +59,10 @@ def test_batch_small_spaces_break_down(ctx):
 
 
 def test_batch_cluster_instances_match_fp64(ctx):
-    """Instances of dim >= 32768 run on 8-CTA thread-block clusters (row slices, inner products
-    combined through distributed shared memory); mixed in one call with single-CTA instances, every
-    refined energy stays within 1e-8 of the FP64 Lanczos of the same start vector."""
+    """Instances of dim >= 32768 run on thread-block clusters (row slices, inner products combined
+    through distributed shared memory; 8-CTA clusters for a call with this few of them); mixed in one
+    call with single-CTA instances, every refined energy stays within 1e-8 of the FP64 Lanczos of the
+    same start vector."""
     inst = [(18, np.random.default_rng(1).uniform(-2, 2, 18)), (12, np.random.default_rng(2).uniform(-2, 2, 12)),
             (18, np.random.default_rng(3).uniform(-2, 2, 18)), (14, np.random.default_rng(4).uniform(-2, 2, 14))]
     hams, v0s, ref = [], [], []
@@ -84,3 +85,30 @@ def test_batch_cluster_instances_match_fp64(ctx):
     # the same instances alone give the same bits as in the mix
     alone = q.batch_lanczos(hams[:1], v0s[:1], 80)
     assert np.array_equal(alone[0, :5], out[0, :5])
+
+
+def test_batch_many_large_instances_take_small_clusters(ctx):
+    """A call with more large instances than 4-CTA clusters can hold at once runs them on 2-CTA
+    clusters (more instances side by side); a sample of the energies stays within 1e-8 of the FP64
+    Lanczos, and the call's instances agree with the same instances in a call of two (8-CTA
+    clusters) to the same tolerance."""
+    n = 160
+    rng = np.random.default_rng(11)
+    hams, v0s = [], []
+    for i in range(n):
+        spec, ham = chains.xxz_chain(18, 1.0, 1.0, True, rng.uniform(-2, 2, 18))
+        sec = q.Sector(spec.index, spec.constraints)
+        H = sec.lower(ham)
+        H._keep = sec
+        hams.append(H)
+        v0s.append(q.start_vector(sec.dim, 500 + i))
+    out = q.batch_lanczos(hams, v0s, 80)
+    few = q.batch_lanczos(hams[:2], v0s[:2], 80)
+    for i in (0, 1, 77, 159):
+        psi = q.getState(hams[i]._keep, 1)
+        psi.set(0, v0s[i])
+        e = q.LanczosSolver(hams[i]._keep, 80).getGroundState(hams[i], psi, 0).ritz_value
+        assert abs(out[i, 1] - e) <= DE_TOL * abs(e), (i, out[i], e)
+        assert out[i, 3] == 80 and out[i, 4] == 0
+    for i in (0, 1):
+        assert abs(out[i, 1] - few[i, 1]) <= DE_TOL * abs(few[i, 1])
