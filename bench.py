@@ -475,17 +475,18 @@ def matrix_free_leg(ctx, H, sec, psi, ritz_csr):
                                              "diagonal 8 B/row")}
 
 
-def batched_sweep(ctx, n_inst=512, steps=80, seed=2024):
-    """Disorder sweep: n_inst random-field XXZ chains, L uniform in {14,16,18,20}, Sz=0,
-    Jz=1, h_i ~ U[-2,2]; mixed-precision batched solve vs the plain FP64 solver run
-    instance by instance.  Returns solves/s of both forms and the energy deviations."""
+def batched_sweep(ctx, n_inst=512, steps=80, seed=2024, chain_L=None):
+    """Disorder sweep: n_inst random-field XXZ chains, L uniform in {14,16,18,20} (or all
+    of length chain_L), Sz=0, Jz=1, h_i ~ U[-2,2]; mixed-precision batched solve vs the
+    plain FP64 solver run instance by instance.  Returns solves/s of both forms and the
+    energy deviations."""
     import qudrip_gb300 as q
     from qudrip_gb300 import chains
     rng = np.random.Generator(np.random.PCG64(seed))
     t0 = time.perf_counter()
     hams, v0s, dims = [], [], []
     for i in range(n_inst):
-        L = int(rng.choice([14, 16, 18, 20]))
+        L = int(rng.choice([14, 16, 18, 20])) if chain_L is None else int(chain_L)
         h = rng.uniform(-2.0, 2.0, L)
         spec, ham = chains.xxz_chain(L, 1.0, 1.0, True, h)
         sec = q.Sector(spec.index, spec.constraints, ctx=ctx)
@@ -518,7 +519,8 @@ def batched_sweep(ctx, n_inst=512, steps=80, seed=2024):
     ctx.sync()
     plain_s = time.perf_counter() - t0
     rel = np.abs(out[:, 1] - plain_e) / np.abs(plain_e)
-    return {"workload": f"{n_inst} random-field XXZ chains L in {{14,16,18,20}}, {steps} Lanczos steps",
+    lset = "{14,16,18,20}" if chain_L is None else "{%d}" % chain_L
+    return {"workload": f"{n_inst} random-field XXZ chains L in {lset}, {steps} Lanczos steps",
             "mixed_solves_per_s": n_inst / mixed_s, "plain_fp64_solves_per_s": n_inst / plain_s,
             "speedup": plain_s / mixed_s, "max_rel_dE": float(rel.max()), "median_rel_dE": float(np.median(rel)),
             "lowering_s_all_instances": lower_s, "mixed_form": "fp32 products/basis, fp64 accumulation, "
@@ -702,6 +704,8 @@ def main():
     ap.add_argument("--serve-only", action="store_true", help="only run the serving mix")
     ap.add_argument("--batch-only", type=int, default=None, metavar="N",
                     help="only run the batched disorder sweep with N instances")
+    ap.add_argument("--batch-L", type=int, default=None, metavar="L",
+                    help="with --batch-only: every chain of length L instead of L in {14,16,18,20}")
     ap.add_argument("--serve-requests", type=int, default=400)
     args = ap.parse_args()
     rank, world, local = dist_env()
@@ -714,7 +718,7 @@ def main():
         return 0
     if args.batch_only is not None:
         import qudrip_gb300 as q
-        print(json.dumps(batched_sweep(q.Context(local), n_inst=args.batch_only)))
+        print(json.dumps(batched_sweep(q.Context(local), n_inst=args.batch_only, chain_L=args.batch_L)))
         return 0
     return gpu_arm(args, rank, world, local)
 
