@@ -351,15 +351,17 @@ void ham_apply_c(qd_ham* H, const cplx* x, cplx* y) {
 cplx state_eval(qd_ham* H, const cplx* psi) {
   Ctx* ctx = H->ctx;
   Workspace& W = ham_workspace(H);
-  DBuf<cplx> tmp(H->dim + 1);
-  DBuf<cplx> out(1);
+  if (W.eval_y.n < (size_t)H->dim + 1) W.eval_y.alloc(H->dim + 1);
+  if (!W.eval_out.p) W.eval_out.alloc(1);
   // psi^dagger (H psi): the product and the dot in one pass
   if (H->flags & QD_HAM_REAL)
-    launch_spmv<double, cplx>(ctx, H, H->vals_r.p, psi, tmp.p, 1.0, psi, W.red_c(0), out.p, nullptr, 0, -1);
+    launch_spmv<double, cplx>(ctx, H, H->vals_r.p, psi, W.eval_y.p, 1.0, psi, W.red_c(0), W.eval_out.p, nullptr, 0,
+                              -1);
   else
-    launch_spmv<cplx, cplx>(ctx, H, H->vals_c.p, psi, tmp.p, 1.0, psi, W.red_c(0), out.p, nullptr, 0, -1);
+    launch_spmv<cplx, cplx>(ctx, H, H->vals_c.p, psi, W.eval_y.p, 1.0, psi, W.red_c(0), W.eval_out.p, nullptr, 0,
+                            -1);
   cplx h;
-  QD_CUDA(cudaMemcpyAsync(&h, out.p, sizeof(cplx), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(&h, W.eval_out.p, sizeof(cplx), cudaMemcpyDeviceToHost, ctx->stream));
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
   return h;
 }

@@ -109,6 +109,9 @@ struct Workspace {
   DBuf<unsigned> tickets;
   LanczosBuffers<double> lz_d;
   LanczosBuffers<cplx> lz_c;
+  // H psi and the result of state_eval, kept between calls (a device allocation
+  // and free per call would wait for the whole device)
+  DBuf<cplx> eval_y, eval_out;
 
   explicit Workspace(Ctx* c);
   GridRed<double> red_d(int slot);
