@@ -878,9 +878,11 @@ void lanczos_ground(qd_ham* H, cplx* psi, const qd_lanczos_opts& o, double* eval
   QD_REQUIRE(o.krylov_dim >= 1 && o.krylov_dim <= 4096, QD_ERR_INVALID, "krylov_dim must be in 1..4096");
   QD_REQUIRE(n >= 1, QD_ERR_INVALID, "empty sector");
   Workspace& W = ham_workspace(H);
-  // ||psi||^2 and whether the start vector is real
-  DBuf<double> nrm2(1);
-  DBuf<int> has_im(1);
+  // ||psi||^2 and whether the start vector is real (buffers kept in the workspace)
+  if (!W.start_nrm2.p) W.start_nrm2.alloc(1);
+  if (!W.start_has_im.p) W.start_has_im.alloc(1);
+  DBuf<double>& nrm2 = W.start_nrm2;
+  DBuf<int>& has_im = W.start_has_im;
   QD_CUDA(cudaMemsetAsync(has_im.p, 0, sizeof(int), ctx->stream));
   colnorm_kernel<<<vec_grid(ctx, n), kVecThreads, 0, ctx->stream>>>(n, psi, nrm2.p, W.red_d(0), has_im.p);
   QD_CHECK_LAUNCH();

@@ -112,6 +112,8 @@ struct Workspace {
   // H psi and the result of state_eval, kept between calls (a device allocation
   // and free per call would wait for the whole device)
   DBuf<cplx> eval_y, eval_out;
+  DBuf<double> start_nrm2;  // ||v0||^2 of the last ground-state solve (read by its first kernels)
+  DBuf<int> start_has_im;
 
   explicit Workspace(Ctx* c);
   GridRed<double> red_d(int slot);
