@@ -52,6 +52,9 @@ struct FxStepArgs {
   int F;
   int* ovf;             // ovf[0]: an element left the fixed-point range; ovf[1]: a wait ran out
   int rows;             // rows per thread: the length of each thread's w column in shared memory
+  unsigned spin_limit;  // polls before a block gives up (0: kStepSpinLimit)
+  int hold_epoch;       // test control: the publishing block does not bump the epoch, so every
+                        // block's wait runs out after spin_limit polls
 };
 
 // Src supplies a row's fixed-point off-diagonal sum: bind(smem) once per
@@ -103,12 +106,13 @@ __global__ void __launch_bounds__(256, 6) lz_fx_step_kernel(Src src, FxStepArgs 
     *a.beta = bt;
     *a.alpha = (*a.s1) * t;
     __threadfence();
-    atomicAdd(a.epoch, 1u);
+    if (!a.hold_epoch) atomicAdd(a.epoch, 1u);
   }
   if (threadIdx.x == 0) {
+    const unsigned limit = a.spin_limit ? a.spin_limit : kStepSpinLimit;
     unsigned polls = 0;
     while (*reinterpret_cast<volatile unsigned*>(a.epoch) == e0) {
-      if (++polls > kStepSpinLimit) {
+      if (++polls > limit) {
         waited_out = 1;
         atomicExch(a.ovf + 1, 1);
         break;

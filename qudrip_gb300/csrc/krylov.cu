@@ -436,6 +436,18 @@ static bool fx_one_launch_step() {
   return !(e && std::strcmp(e, "split") == 0);
 }
 
+// Test control of the one-launch step's bounded grid barrier:
+// QD_STEP_WAIT_OUT=<polls> (1 .. 2^20) keeps the publishing block from bumping
+// the epoch and lets every block give up after <polls> polls, so each step's
+// wait runs out and the solve returns QD_ERR_TIMEOUT with the kernel finished.
+// Read per solve; 0 when unset.
+static unsigned step_wait_out_polls() {
+  const char* e = std::getenv("QD_STEP_WAIT_OUT");
+  if (!e) return 0;
+  const long v = std::strtol(e, nullptr, 10);
+  return v > 0 ? (unsigned)std::min<long>(v, 1L << 20) : 0u;
+}
+
 // Overflow flag of a fixed-point run (nonzero: rerun on the FP64 product);
 // a bounded device wait that ran out is an error.
 static int fx_flags(Ctx* ctx, const int* flags) {
@@ -641,6 +653,8 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int k_
         a.rd = W.red_d_flat(3);
         a.Xk = Xnext;
         a.ovf = B.ovf.p;
+        a.spin_limit = step_wait_out_polls();
+        a.hold_epoch = a.spin_limit != 0;
         if (launch_fx_step(ctx, H, *form, a)) continue;
       }
       if (fxk == 1)  // product fused with the step's inner products, then the update
@@ -715,7 +729,8 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
   fxk = form ? 1 : 0;
   const bool fx = fxk == 1;
   const int fxF = fx ? form->F : 0;
-  const int kind = (mf ? 1 : 0) + 2 * fxk + ((fx && fx_one_launch_step() && !H->one_shot) ? 4 : 0);
+  const bool one_launch = fx && fx_one_launch_step() && !H->one_shot;
+  const int kind = (mf ? 1 : 0) + 2 * fxk + (one_launch ? 4 : 0) + ((one_launch && step_wait_out_polls()) ? 8 : 0);
   if (B.kind != kind) {
     B.drop_graph();
     B.kind = kind;

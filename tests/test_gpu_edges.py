@@ -91,3 +91,37 @@ def test_argument_limits(ctx):
         psi.eval(1, H)  # time slot outside the state
     with pytest.raises(A.QDError):
         A.call("qd_ham_set_spmv_kernel", H.handle, 99)
+
+
+def test_step_barrier_wait_runs_out_and_next_solve_is_unchanged(ctx, monkeypatch):
+    """The one-launch Lanczos step's grid barrier is a bounded wait.  With the
+    test control QD_STEP_WAIT_OUT the publishing block holds the epoch back, so
+    every block gives up after a few polls, skips its update and still joins the
+    norm's reduction: the kernel returns and the solve reports QD_ERR_TIMEOUT.
+    The next solve on the same operator carries the bits of one on a fresh
+    operator."""
+    spec, ham = chains.xxz_chain(16)  # uniform couplings: the one-launch step
+    sec = sector(spec)
+    v0 = q.start_vector(sec.dim, 5)
+
+    def solve(H):
+        psi = q.getState(sec, 1)
+        psi.set(0, v0)
+        r = q.Arnoldi.getLanczosSolver(sec, 40).getGroundState(H, psi(0), 0)
+        return r, psi.get(0)
+
+    H = sec.lower(ham)
+    r0, p0 = solve(H)
+    import ctypes as C
+    info = A.qd_ham_info()
+    A.call("qd_ham_get_info", H.handle, C.byref(info))
+    assert info.step_launches == 1
+    monkeypatch.setenv("QD_STEP_WAIT_OUT", "8")
+    with pytest.raises(A.QDError) as e:
+        solve(H)
+    assert e.value.code == A.QD_ERR_TIMEOUT
+    monkeypatch.delenv("QD_STEP_WAIT_OUT")
+    r1, p1 = solve(H)
+    r2, p2 = solve(sec.lower(ham))
+    assert r1.ritz_value == r0.ritz_value == r2.ritz_value
+    assert np.array_equal(p1, p0) and np.array_equal(p2, p0)
