@@ -27,6 +27,7 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -233,7 +234,11 @@ def reference_arm(args, rank, world):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
         "data": "synthetic (seeded uniform[-1,1] start vector)",
         "config": {"workload": "xxz_chain_L24_periodic_Sz0_lanczos", "L": L, "dim": H.dim, "nnz": H.nnz,
-                   "krylov_dim_sample": kry, "spmv": "csc_column_push_complex128", "threads": nthreads},
+                   "krylov_dim_sample": kry, "spmv": "csc_column_push_complex128", "threads": nthreads,
+                   "compared_as": "matvecs/s: the reference's State is complex128, so each product here is a "
+                                  "complex128 CSC column push (about 4x the flops and 1.7x the bytes of the GPU "
+                                  "arm's real FP64 product); each solve runs krylov_dim=4 (a bounded sample), the "
+                                  "GPU arm krylov_dim=100"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                          "sample": f"each step: {nthreads} concurrent Lanczos solves (one per host thread) with "
                                    f"krylov_dim={kry} at L=24 on one shared CSC matrix (CPU restatement of the "
@@ -332,7 +337,7 @@ def gpu_arm(args, rank, world, local):
     A.call("qd_host_alloc", dim * 16, C.byref(ho))
     dptr = C.cast(hb, C.POINTER(C.c_double))
     optr = C.cast(ho, C.POINTER(C.c_double))
-    e_steps = max(1, min(args.steps, 5))
+    e_steps = args.steps  # the same step count as the device-timed value
 
     def e2e_step():
         A.call("qd_state_upload", psi.handle, 0, dptr)
@@ -528,7 +533,7 @@ def batched_sweep(ctx, n_inst=512, steps=80, seed=2024, chain_L=None):
             "plain_form": "fp64 Lanczos (reference algorithm), one solve after another"}
 
 
-def trajectory_ensemble(ctx, with_oracle=True):
+def trajectory_ensemble(ctx, with_oracle=True, ntraj=4096, nsteps=1000):
     """Dissipative Hubbard chain: L=8, N_up=N_dn=4 (dim 4900), t=1, U=4, open, jumps
     sqrt(gamma) n_{i,s} on all 16 site-spins, gamma=0.1, 4096 trajectories, m=30,
     dt=0.01, T=10; observable <n_{i,up} n_{i,dn}>(t).  Starts from the ground state of
@@ -536,7 +541,7 @@ def trajectory_ensemble(ctx, with_oracle=True):
     import qudrip_gb300 as q
     from qudrip_gb300 import chains
     from qudrip_gb300.operators import getHopFermiGate
-    Lh, gamma, dt, nsteps, ntraj, m, seed = 8, 0.1, 0.01, 1000, 4096, 30, 4242
+    Lh, gamma, dt, m, seed = 8, 0.1, 0.01, 30, 4242
     spec, ham = chains.hubbard_chain(Lh, 4, 4, 4.0, -1.0)
     sec = q.Sector(spec.index, spec.constraints, ctx=ctx)
     H = sec.lower(ham)
@@ -555,9 +560,14 @@ def trajectory_ensemble(ctx, with_oracle=True):
     t0 = time.perf_counter()
     mean, err, st = q.traj_run(Heff, psi0, ntraj, nsteps, dt, gamma, seed, m, chan, obs)
     wall = time.perf_counter() - t0
-    out = {"workload": "dissipative Hubbard L=8 (dim 4900), 4096 trajectories x 1000 steps, m=30, dt=0.01",
-           "trajectory_steps_per_s": ntraj * nsteps / wall, "wall_s": wall,
-           "propagator_ms": st.propagator_ms, "ensemble_ms": st.ensemble_ms, "jumps": int(st.jumps),
+    form = {0: "resident: one CTA per trajectory, operator and complex64 vectors in shared memory, "
+               "truncated Taylor exp(-i dt (H - mu)) with the degree from its remainder bound",
+            1: "FP64 Arnoldi exponential per trajectory and step (batched kernel)"}[int(st.path)]
+    out = {"workload": f"dissipative Hubbard L=8 (dim 4900), {ntraj} trajectories x {nsteps} steps, m=30, dt=0.01",
+           "trajectory_steps_per_s": ntraj * nsteps / wall, "wall_s": wall, "form": form,
+           "products_per_step": int(st.products),
+           "products_per_s": ntraj * nsteps * int(st.products) / (st.ensemble_ms * 1e-3),
+           "setup_ms": st.setup_ms, "ensemble_ms": st.ensemble_ms, "jumps": int(st.jumps),
            "docc_t0": float(mean[0].mean()), "docc_T": float(mean[-1].mean()),
            "docc_T_stderr": float(err[-1].mean())}
     if with_oracle:
@@ -634,8 +644,9 @@ def serve_stream(mode, reqs, **opts):
                 r = reqs[i]
                 if r["kind"] == "ground":
                     rid = srv.submit_ground(r["spec"], r["ham"], 100, seed=r["seed"], tag=i)
-                else:
-                    rid = srv.submit_evolve(r["spec"], r["ham"], 0.05, 100, m=16, seed=r["seed"], tag=i)
+                else:  # keep the evolved state to compare the two forms in 2-norm
+                    rid = srv.submit_evolve(r["spec"], r["ham"], 0.05, 100, m=16, seed=r["seed"], tag=i,
+                                            want_state=True, dim_hint=math.comb(r["L"], r["L"] // 2))
                 ids[rid] = i
                 i += 1
             wait_ms = 1 if i < len(reqs) else 50
@@ -673,7 +684,10 @@ def serving_mix(n_req=400, rate=200.0, seed=77, **opts):
                 if idx:
                     sv = [out[i]["t_done"] - out[i]["t_admit"] for i in idx]
                     service[f"{kind}_L{L}"] = round(1e3 * float(np.median(sv)), 2)
-        summary[mode] = {"service_p50_ms": service, "solves_per_s": n_req / (t_last - t_first), "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+        busy = {kind: round(sum(out[i]["t_done"] - out[i]["t_admit"] for i in range(n_req)
+                                if reqs[i]["kind"] == kind), 3) for kind in ("ground", "evolve")}
+        summary[mode] = {"service_p50_ms": service, "service_s_total_by_kind": busy,
+                         "solves_per_s": n_req / (t_last - t_first), "p50_ms": 1e3 * float(np.percentile(lat, 50)),
                          "p99_ms": 1e3 * float(np.percentile(lat, 99)), "failed": bad, "by_kind": by_kind,
                          "batches": st["batches"], "batched": st["batched"], "max_active": st["max_active"],
                          "bytes_peak": st["bytes_peak"], "budget": st["budget"]}
@@ -681,8 +695,11 @@ def serving_mix(n_req=400, rate=200.0, seed=77, **opts):
           for i in range(n_req) if reqs[i]["kind"] == "ground"]
     dEv = [abs(results["mixed"][i]["energy"] - results["plain"][i]["energy"]) / abs(results["plain"][i]["energy"])
            for i in range(n_req) if reqs[i]["kind"] == "evolve"]
+    dpsi = [float(np.linalg.norm(results["mixed"][i]["state"] - results["plain"][i]["state"]))
+            for i in range(n_req) if reqs[i]["kind"] == "evolve"]
     summary["max_rel_dE_ground_mixed_vs_plain"] = float(max(dE)) if dE else None
     summary["max_rel_dE_evolved_mixed_vs_plain"] = float(max(dEv)) if dEv else None
+    summary["max_l2_dpsi_evolved_mixed_vs_plain"] = max(dpsi) if dpsi else None
     summary["speedup_solves_per_s"] = summary["mixed"]["solves_per_s"] / summary["plain"]["solves_per_s"]
     return summary
 
@@ -707,6 +724,8 @@ def main():
     ap.add_argument("--batch-L", type=int, default=None, metavar="L",
                     help="with --batch-only: every chain of length L instead of L in {14,16,18,20}")
     ap.add_argument("--serve-requests", type=int, default=400)
+    ap.add_argument("--traj-only", type=int, nargs=2, default=None, metavar=("NTRAJ", "NSTEPS"),
+                    help="only run the trajectory ensemble with NTRAJ trajectories of NSTEPS steps")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
@@ -715,6 +734,11 @@ def main():
         return spmv_only(args, local)
     if args.serve_only:
         print(json.dumps(serving_mix(args.serve_requests)))
+        return 0
+    if args.traj_only is not None:
+        import qudrip_gb300 as q
+        print(json.dumps(trajectory_ensemble(q.Context(local), with_oracle=False, ntraj=args.traj_only[0],
+                                             nsteps=args.traj_only[1])))
         return 0
     if args.batch_only is not None:
         import qudrip_gb300 as q

@@ -291,6 +291,35 @@ qd_status qd_arnoldi_evolve(qd_ham *ham, qd_state *psi, int t_in, int t_out,
                             double h, int m, int *act_dim);
 
 /* ------------------------------------------------------------------ */
+/* Arnoldi ground state (non-Hermitian solver, incremental)            */
+/*   replaces Arnoldi::getSolver(index, kry_dim).getGroundState(H, psi,*/
+/*   tstp, add_dim) -- ArnoldiSolver<T,0>: getGroundState             */
+/*   (sparse_algorithm.hpp:564-585), updateKrylovRepr (:521-546),     */
+/*   expandBasis<0> (:372-393), getState<herm 0> (:447-453)           */
+/* The basis grows by full orthogonalisation of H v_{k-1} against every */
+/* previous vector (two classical Gram-Schmidt passes; the reference's  */
+/* modified Gram-Schmidt up to rounding); the breaking step (norm <     */
+/* 1e-10) counts.  As the reference's SelfAdjointEigenSolver, the       */
+/* eigensolve reads the Arnoldi matrix's lower triangle: the real parts */
+/* of <v_i, H v_i> and the sub-diagonal norms.  psi(:, t) is the start  */
+/* vector on entry and the Ritz vector V z_0 on exit; evals_out (may be */
+/* NULL, krylov_dim doubles) receives act_dim ascending eigenvalues.    */
+/* opts->krylov_dim is kry_dim, opts->add_dim the steps of this call    */
+/* (0 or -1: up to kry_dim); spmv and ritz are ignored (CSR products).  */
+/* res->err is |lambda_0| (a fresh solve) or, after qd_arnoldi_extend,  */
+/* |lambda_0 - previous lambda_0|; front ends compute error() over the  */
+/* convergeEV eigenvalues from evals_out.                               */
+/* ------------------------------------------------------------------ */
+qd_status qd_arnoldi_ground(qd_ham *ham, qd_state *psi, int t, const qd_lanczos_opts *opts,
+                            double *evals_out, qd_lanczos_result *res);
+/* A later getGroundState(H, psi, tstp, add_dim) on the same solver: grows
+ * the last qd_arnoldi_ground on this operator (same krylov_dim) by
+ * opts->add_dim steps from its stored basis and writes the new Ritz vector;
+ * a space that reached krylov_dim or closed by breakdown does not grow. */
+qd_status qd_arnoldi_extend(qd_ham *ham, qd_state *psi, int t, const qd_lanczos_opts *opts,
+                            double *evals_out, qd_lanczos_result *res);
+
+/* ------------------------------------------------------------------ */
 /* Batched mixed-precision Lanczos ground states                      */
 /*   many independent getGroundState solves (sparse_algorithm.hpp:    */
 /*   564-585) in one persistent launch                                 */
@@ -325,11 +354,17 @@ qd_status qd_krylov_evolve_batch(qd_ham *ham, const double *d_X, int64_t ldx,
 /*   :520-529, no-jump generator :514-517, channel search :565-577)    */
 /* heff must be the no-jump generator H - (i/2) gamma sum_j n_j of the  */
 /* jump operators L_j = sqrt(gamma) n_{chan_bits[j]}.  Every trajectory  */
-/* starts from psi0 (host complex128), runs nsteps steps of length dt    */
-/* (m Krylov vectors tabulate exp(-i heff dt) once), draws its random    */
-/* numbers from Philox4x32-10 keyed by (seed, trajectory, step), and     */
-/* records <n_{obs_a[k]} n_{obs_b[k]}> after every step.  obs_mean and   */
-/* obs_stderr receive (nsteps+1) x nobs doubles (row = step).           */
+/* starts from psi0 (host complex128), runs nsteps steps of length dt,   */
+/* draws its random numbers from Philox4x32-10 keyed by (seed,           */
+/* trajectory, step), and records <n_{obs_a[k]} n_{obs_b[k]}> after      */
+/* every step.  obs_mean and obs_stderr receive (nsteps+1) x nobs        */
+/* doubles (row = step).  Where heff has dim <= 5120 on at most 32 bits  */
+/* and one off-diagonal value +-c, each trajectory runs in one SM's      */
+/* shared memory (complex64 vectors, exp(-i heff dt) by a truncated      */
+/* Taylor series whose degree and sub-steps follow the series' remainder */
+/* bound, at most m-1 products per sub-step); otherwise every step is an */
+/* FP64 Arnoldi exponential with m vectors per trajectory.  The          */
+/* environment variable QD_TRAJ_ARNOLDI=1 selects the second form.       */
 /* ------------------------------------------------------------------ */
 typedef struct {
   int32_t ntraj;
@@ -348,9 +383,10 @@ typedef struct {
 
 typedef struct {
   int64_t jumps;        /* jumps over all trajectories */
-  double propagator_ms; /* tabulation of exp(-i heff dt) */
+  double setup_ms;      /* building and uploading the resident form */
   double ensemble_ms;   /* the nsteps steps of all trajectories */
-  double reserved;
+  int32_t path;         /* 0: resident Taylor kernel, 1: FP64 Arnoldi steps */
+  int32_t products;     /* sparse products per trajectory step (Taylor terms x sub-steps, or m - 1) */
 } qd_traj_stats;
 
 qd_status qd_traj_run(qd_ham *heff, const qd_traj_desc *desc, const double *psi0,

@@ -676,18 +676,59 @@ class LanczosSolver {
 
 class ArnoldiSolver {
  public:
-  ArnoldiSolver(const SubIndex&, int kry_dim) : kry_dim_(kry_dim) {}
+  ArnoldiSolver(const SubIndex&, int kry_dim) : kry_dim_(kry_dim), evs_(1, 0.0) {}
   void evolve(const SpMatrix& H, State& psi, int tstp, double h, int kry_dim_rt = 0) {
     int act = 0;
     check(qd_arnoldi_evolve(H.handle(), psi.handle(), tstp, tstp + 1, h, kry_dim_rt ? kry_dim_rt : kry_dim_, &act),
           "evolve");
     act_ = act;
   }
+  // number of tracked eigenvalues and their initial values (sparse_algorithm.hpp:494-500)
+  void convergeEV(int N, double iv = 0.0) {
+    if (!(N < kry_dim_)) throw Error(QD_ERR_INVALID, "convergeEV: N must be below kry_dim");
+    evs_.assign((size_t)N, iv);
+  }
+  // Incremental Arnoldi ground state (sparse_algorithm.hpp:564-585): the first call
+  // starts from psi(tstp) and runs add_dim steps (all kry_dim for -1); later calls
+  // grow the same Krylov space; a full or closed space returns at once.
+  void getGroundState(const SpMatrix& H, State& psi, int tstp, int add_dim = -1) {
+    if (gs_act_ >= kry_dim_ || gs_closed_) return;
+    qd_lanczos_opts o{};
+    o.krylov_dim = kry_dim_;
+    o.spmv = QD_SPMV_CSR;
+    o.ritz = QD_RITZ_STORED_BASIS;
+    o.add_dim = add_dim > 0 ? add_dim : 0;
+    evals_.assign((size_t)kry_dim_, 0.0);
+    if (gs_act_ == 0)
+      check(qd_arnoldi_ground(H.handle(), psi.handle(), tstp, &o, evals_.data(), &res_), "getGroundState");
+    else
+      check(qd_arnoldi_extend(H.handle(), psi.handle(), tstp, &o, evals_.data(), &res_), "getGroundState");
+    gs_act_ = act_ = res_.act_dim;
+    gs_closed_ = res_.breakdown != 0;
+    evals_.resize((size_t)act_);
+    const size_t m = std::min(evs_.size(), (size_t)act_);
+    double e2 = 0.0;
+    for (size_t i = 0; i < m; ++i) e2 += (evals_[i] - evs_[i]) * (evals_[i] - evs_[i]);
+    err_ = std::sqrt(e2);
+    for (size_t i = 0; i < m; ++i) evs_[i] = evals_[i];
+  }
+  double error() const { return err_; }
   int act_dim() const { return act_; }
+  const std::vector<double>& eigenvalues() const { return evals_; }
+  void storeE(const std::string& fname) const {
+    std::ofstream f(fname);
+    for (double e : evals_) f << e << "\n";
+  }
 
  private:
   int kry_dim_;
   int act_ = 0;
+  int gs_act_ = 0;
+  bool gs_closed_ = false;
+  double err_ = 0.0;
+  std::vector<double> evs_;
+  qd_lanczos_result res_{};
+  std::vector<double> evals_;
 };
 
 inline LanczosSolver getLanczosSolver(const SubIndex& index, int kry_dim) { return LanczosSolver(index, kry_dim); }

@@ -75,6 +75,7 @@ def lib():
                 "qdo_arnoldi_evolve": (C.c_int, [_P, _DP, C.c_double, C.c_int, _DP, _IP, _I64P]),
                 "qdo_hermitian_lanczos_ground": (C.c_int, [_P, _DP, C.c_int, _DP, _DP, _IP, _DP,
                                                            _I64P]),
+                "qdo_arnoldi_ground": (C.c_int, [_P, _DP, C.c_int, _DP, _DP, _IP, _I64P, _DP]),
             }
             for name, (res, args) in sig.items():
                 fn = getattr(L, name)
@@ -178,6 +179,21 @@ class Ham:
         if rc != 0:
             raise RuntimeError(f"oracle evolve failed: {rc}")
         return out, act.value
+
+    def arnoldi_ground(self, psi0, steps: int):
+        """Arnoldi::getSolver(...).getGroundState after `steps` Krylov steps in all."""
+        psi0 = as_complex(psi0)
+        psi = np.empty_like(psi0)
+        evals = np.empty(steps)
+        act = C.c_int(0)
+        mv = C.c_int64(0)
+        energy = np.zeros(2)
+        rc = lib().qdo_arnoldi_ground(self.ptr, _dp(psi0), steps, _dp(psi), _dp(evals), C.byref(act),
+                                      C.byref(mv), _dp(energy))
+        if rc != 0:
+            raise RuntimeError(f"oracle arnoldi ground state failed: {rc}")
+        return dict(psi=psi, evals=evals[:act.value].copy(), act_dim=act.value, matvecs=mv.value,
+                    energy=complex(energy[0], energy[1]))
 
     def hermitian_lanczos_ground(self, psi0, kry_dim: int):
         psi0 = as_complex(psi0)

@@ -706,6 +706,76 @@ extern "C" int qdo_arnoldi_evolve(const qdo_ham* H, const double* psi_in, double
 }
 
 // ===========================================================================
+// Arnoldi ground state: Arnoldi::getSolver(index, kry_dim).getGroundState(H,
+// psi, t[, add_dim]) -- ArnoldiSolver<T, herm=0> (sparse_algorithm.hpp:475-604):
+//   initKrylov :514-519; updateKrylovRepr :521-546 with expandBasis<0>
+//   :372-393 (modified Gram-Schmidt of H v_{idx-1} against every previous
+//   vector; stop at ||w|| < eps keeping the breaking step); getGroundState
+//   :564-585 runs SelfAdjointEigenSolver on KR[0:act, 0:act], which reads the
+//   lower triangle only: the real parts of the diagonal <v_i, H v_i> and the
+//   sub-diagonal norms (real), i.e. a symmetric tridiagonal matrix (its
+//   Householder step is the identity there); getState<herm 0> :447-453 forms
+//   psi = V[:, 0:act] z_0 from the lowest eigenvector z_0.
+// A solve grown by several calls of add_dim steps each performs the same
+// operations in the same order as one call of their total (expandBasis<0>
+// continues from the stored basis), so `steps` here is the dimension reached.
+// ===========================================================================
+extern "C" int qdo_arnoldi_ground(const qdo_ham* H, const double* psi0, int steps, double* psi_out,
+                                  double* evals_out, int* act_dim_out, int64_t* matvecs_out, double* energy_out) {
+  const int64_t n = H->dim;
+  if (steps < 1 || n < 1) return QD_ERR_INVALID;
+  std::vector<std::vector<cd>> V(steps + 1, std::vector<cd>(n, cd(0.0, 0.0)));
+  const cd* p = reinterpret_cast<const cd*>(psi0);
+  const double nrm0 = std::sqrt(norm2(p, n));
+  for (int64_t k = 0; k < n; ++k) V[0][k] = cd(p[k].real() / nrm0, p[k].imag() / nrm0);
+  std::vector<cd> hv;
+  int64_t matvecs = 0;
+  int idx;
+  for (idx = 1; idx <= steps; ++idx) {
+    spmv_csc(H, V[idx - 1].data(), V[idx].data());
+    ++matvecs;
+    for (int i = 0; i < idx; ++i) {
+      const cd nh = dotc(V[i].data(), V[idx].data(), n);
+      for (int64_t k = 0; k < n; ++k) V[idx][k] = csub(V[idx][k], cmul(nh, V[i][k]));
+      hv.push_back(nh);
+    }
+    const double nr = std::sqrt(norm2(V[idx].data(), n));
+    for (int64_t k = 0; k < n; ++k) V[idx][k] = cd(V[idx][k].real() / nr, V[idx][k].imag() / nr);
+    hv.push_back(cd(nr, 0.0));
+    if (nr < kEps) {
+      ++idx;
+      break;
+    }
+  }
+  const int act = idx - 1;
+  // KR column i: h entries j = 0..i+1 (j = i+1 is the norm), the last column j = 0..act-1
+  std::vector<cd> KR((size_t)act * (act + 1), cd(0.0, 0.0));
+  size_t hp = 0;
+  for (int i = 0; i < act - 1; ++i)
+    for (int j = 0; j <= i + 1; ++j) KR[(size_t)i * (act + 1) + j] = hv[hp++];
+  for (int j = 0; j <= act - 1; ++j) KR[(size_t)(act - 1) * (act + 1) + j] = hv[hp++];
+  std::vector<double> d(act), e(act > 1 ? act - 1 : 1), ev(act), z((size_t)act * act);
+  for (int i = 0; i < act; ++i) d[i] = KR[(size_t)i * (act + 1) + i].real();
+  for (int i = 0; i + 1 < act; ++i) e[i] = KR[(size_t)i * (act + 1) + i + 1].real();
+  if (qdo_tridiag_eig(act, d.data(), e.data(), ev.data(), z.data()) != 0) return QD_ERR_INVALID;
+  cd* out = reinterpret_cast<cd*>(psi_out);
+  for (int64_t k = 0; k < n; ++k) {
+    cd s(0.0, 0.0);
+    for (int j = 0; j < act; ++j) s = cadd(s, cmul(V[j][k], cd(z[j], 0.0)));
+    out[k] = s;
+  }
+  if (evals_out) std::memcpy(evals_out, ev.data(), act * sizeof(double));
+  *act_dim_out = act;
+  if (matvecs_out) *matvecs_out = matvecs;
+  if (energy_out) {
+    const cd E = eval_left(H, out);
+    energy_out[0] = E.real();
+    energy_out[1] = E.imag();
+  }
+  return 0;
+}
+
+// ===========================================================================
 // Hermitian::LanczosSolver::getGroundState (sparse_algorithm.hpp:287-301):
 // getKrylovReprAd (:72-122) builds tridiag(a, b) with two products per step,
 // the dense eigensolver picks the lowest eigenvector, getKrylovGS (:206-238)

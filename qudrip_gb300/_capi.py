@@ -87,8 +87,8 @@ class qd_traj_desc(C.Structure):
 
 
 class qd_traj_stats(C.Structure):
-    _fields_ = [("jumps", C.c_int64), ("propagator_ms", C.c_double), ("ensemble_ms", C.c_double),
-                ("reserved", C.c_double)]
+    _fields_ = [("jumps", C.c_int64), ("setup_ms", C.c_double), ("ensemble_ms", C.c_double),
+                ("path", C.c_int32), ("products", C.c_int32)]
 
 
 QD_REQ_GROUND = 0
@@ -191,6 +191,8 @@ _SIGNATURES = {
     "qd_lanczos_ground": [_P, _P, C.c_int, C.POINTER(qd_lanczos_opts), _DP,
                           C.POINTER(qd_lanczos_result)],
     "qd_lanczos_extend": [_P, _P, C.c_int, C.POINTER(qd_lanczos_opts), _DP, C.POINTER(qd_lanczos_result)],
+    "qd_arnoldi_ground": [_P, _P, C.c_int, C.POINTER(qd_lanczos_opts), _DP, C.POINTER(qd_lanczos_result)],
+    "qd_arnoldi_extend": [_P, _P, C.c_int, C.POINTER(qd_lanczos_opts), _DP, C.POINTER(qd_lanczos_result)],
     "qd_hermitian_lanczos_ground": [_P, _P, C.c_int, C.c_int, _DP, C.POINTER(qd_lanczos_result)],
     "qd_lanczos_evolve": [_P, _P, C.c_int, C.c_int, C.c_double, C.c_int, C.c_int, C.POINTER(C.c_int)],
     "qd_seeded_start": [C.c_uint64, C.c_int64, _DP],

@@ -532,6 +532,29 @@ qd_status qd_lanczos_extend(qd_ham* ham, qd_state* psi, int t, const qd_lanczos_
   });
 }
 
+static void arnoldi_ground_call(qd_ham* ham, qd_state* psi, int t, const qd_lanczos_opts* opts, double* evals_out,
+                                qd_lanczos_result* res, bool extend) {
+  QD_REQUIRE(ham && psi && opts && res, QD_ERR_INVALID, "null argument");
+  QD_REQUIRE(t >= 0 && t < psi->nt, QD_ERR_INVALID, "bad column");
+  QD_REQUIRE(psi->dim == ham->dim, QD_ERR_INVALID, "dimension mismatch");
+  DeviceGuard dg(ham->ctx->device);
+  const double prev = (extend && ham->arnoldi_gs) ? ham->arnoldi_gs_ritz : 0.0;
+  std::memset(res, 0, sizeof(*res));
+  arnoldi_ground(ham, psi->col(t), opts->krylov_dim, opts->add_dim, extend, evals_out, res);
+  res->err = std::fabs(res->ritz_value - prev);
+  ham->arnoldi_gs_ritz = res->ritz_value;
+}
+
+qd_status qd_arnoldi_ground(qd_ham* ham, qd_state* psi, int t, const qd_lanczos_opts* opts, double* evals_out,
+                            qd_lanczos_result* res) {
+  return guard([&] { arnoldi_ground_call(ham, psi, t, opts, evals_out, res, false); });
+}
+
+qd_status qd_arnoldi_extend(qd_ham* ham, qd_state* psi, int t, const qd_lanczos_opts* opts, double* evals_out,
+                            qd_lanczos_result* res) {
+  return guard([&] { arnoldi_ground_call(ham, psi, t, opts, evals_out, res, true); });
+}
+
 qd_status qd_hermitian_lanczos_ground(qd_ham* ham, qd_state* psi, int t, int kry_dim, double* evals_out,
                                       qd_lanczos_result* res) {
   return guard([&] {
@@ -587,12 +610,15 @@ qd_status qd_traj_run(qd_ham* heff, const qd_traj_desc* desc, const double* psi0
     DeviceGuard dg(heff->ctx->device);
     int64_t jumps = 0;
     double t[2] = {0, 0};
-    traj_run(heff, *desc, psi0, obs_mean, obs_stderr, &jumps, t);
+    int path[2] = {0, 0};
+    traj_run(heff, *desc, psi0, obs_mean, obs_stderr, &jumps, t, path);
     if (stats) {
       std::memset(stats, 0, sizeof(*stats));
       stats->jumps = jumps;
-      stats->propagator_ms = t[0];
+      stats->setup_ms = t[0];
       stats->ensemble_ms = t[1];
+      stats->path = path[0];
+      stats->products = path[1];
     }
   });
 }

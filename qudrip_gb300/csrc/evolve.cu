@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "dense.h"
+#include "tridiag.cuh"
 #include "evolve.cuh"
 #include "krylov.cuh"
 #include "spmv.cuh"
@@ -255,6 +256,193 @@ void arnoldi_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int 
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
   if (act_out) *act_out = act;
 }
+
+// ---------------------------------------------------------------- Arnoldi ground state
+// ArnoldiSolver<T, herm=0>::getGroundState (sparse_algorithm.hpp:564-585) with
+// updateKrylovRepr (:521-546) and expandBasis<0> (:372-393): the basis grows by
+// full orthogonalisation against every previous vector (here classical
+// Gram-Schmidt applied twice, the multi-dot over 32-vector chunks), the breaking
+// step (||w|| < 1e-10) counts, and the ground state comes from the reference's
+// SelfAdjointEigenSolver on the Arnoldi matrix's lower triangle: the real parts
+// of the diagonal <v_i, H v_i> and the sub-diagonal norms, a symmetric
+// tridiagonal matrix (for Hermitian H the same matrix as the full projection).
+// psi = V[:, :act] z_0 (getState<herm 0>, :447-453).
+
+// w -= sum_{j<J} c_j V_j for any J (coefficients staged 128 at a time);
+// hcol[j] (+)= c_j by block 0
+__global__ void __launch_bounds__(kEvThreads) gs_update_long_kernel(int64_t n, const cplx* __restrict__ V,
+                                                                    int64_t ld, int J, const cplx* c,
+                                                                    cplx* __restrict__ w, cplx* hcol, int first_pass,
+                                                                    const int* stop, int step) {
+  if (ev_stopped(stop, step)) return;
+  __shared__ cplx s_c[128];
+  if (blockIdx.x == 0)
+    for (int j = threadIdx.x; j < J; j += blockDim.x) hcol[j] = first_pass ? c[j] : vadd(hcol[j], c[j]);
+  for (int j0 = 0; j0 < J; j0 += 128) {
+    const int jc = min(128, J - j0);
+    __syncthreads();
+    if (threadIdx.x < jc) s_c[threadIdx.x] = c[j0 + threadIdx.x];
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+      cplx wi = w[i];
+      for (int j = 0; j < jc; ++j) wi = vsubmul(wi, s_c[j], V[(int64_t)(j0 + j) * ld + i]);
+      w[i] = wi;
+    }
+  }
+}
+
+// out = sum_{j<a} e_j V_j for any a
+__global__ void __launch_bounds__(kEvThreads) ev_combine_long_kernel(int64_t n, const cplx* __restrict__ V, int64_t ld,
+                                                                     int a, const cplx* e, cplx* __restrict__ out) {
+  __shared__ cplx s_e[128];
+  for (int j0 = 0; j0 < a; j0 += 128) {
+    const int jc = min(128, a - j0);
+    __syncthreads();
+    if (threadIdx.x < jc) s_e[threadIdx.x] = e[j0 + threadIdx.x];
+    __syncthreads();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+      cplx acc = (j0 == 0) ? mkc(0.0, 0.0) : out[i];
+      for (int j = 0; j < jc; ++j) acc = vfma(s_e[j], V[(int64_t)(j0 + j) * ld + i], acc);
+      out[i] = acc;
+    }
+  }
+}
+
+void ArnoldiGround::ensure(int64_t n_, int kdim_, int grid, cudaStream_t stream) {
+  if (n_ == n && kdim_ == kdim && grid <= grid_cap) return;
+  n = n_;
+  kdim = kdim_;
+  ld = (n + 31) / 32 * 32;
+  ldh = kdim + 1;
+  grid_cap = std::max(grid, 1);
+  V.alloc((size_t)(kdim + 1) * ld);
+  w.alloc(ld);
+  proj.alloc(kdim + 1);
+  hcol.alloc((size_t)(kdim + 1) * ldh);
+  nrm.alloc(kdim + 2);
+  nrm2.alloc(kdim + 2);
+  stop.alloc(1);
+  e.alloc(kdim + 1);
+  partials.alloc((size_t)grid_cap * 32);
+  rpart.alloc(kMaxGrid);
+  tickets.alloc(4);
+  QD_CUDA(cudaMemsetAsync(tickets.p, 0, 4 * sizeof(unsigned), stream));
+}
+
+template <typename MV>
+static void arnoldi_ground_steps(qd_ham* H, const MV* vals, ArnoldiGround& B, int first, int last) {
+  Ctx* ctx = H->ctx;
+  Workspace& W = ham_workspace(H);
+  const int64_t n = B.n;
+  const int g = ev_grid(ctx, n);
+  for (int idx = first; idx <= last; ++idx) {
+    const cplx* vprev = B.V.p + (int64_t)(idx - 1) * B.ld;
+    launch_spmv<MV, cplx>(ctx, H, vals, vprev, B.w.p, 1.0, nullptr, W.red_c(0), nullptr, B.stop.p, idx, -1);
+    cplx* hcol = B.hcol.p + (int64_t)(idx - 1) * B.ldh;
+    for (int pass = 0; pass < 2; ++pass) {
+      for (int j0 = 0; j0 < idx; j0 += 32) {
+        multidot_kernel<32><<<g, kEvThreads, 0, ctx->stream>>>(n, B.V.p + (int64_t)j0 * B.ld, B.ld,
+                                                                std::min(32, idx - j0), B.w.p, B.partials.p,
+                                                                B.tickets.p, B.proj.p + j0, B.stop.p, idx);
+        QD_CHECK_LAUNCH();
+        QD_LAUNCHED(ctx);
+      }
+      gs_update_long_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, idx, B.proj.p, B.w.p, hcol, pass == 0,
+                                                                B.stop.p, idx);
+      QD_CHECK_LAUNCH();
+      QD_LAUNCHED(ctx);
+    }
+    ev_norm_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, B.w.p, B.nrm2.p + idx, B.nrm.p + idx,
+                                                       GridRed<double>{B.rpart.p, B.tickets.p + 1}, B.stop.p, idx);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+    ev_scale_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, B.w.p, B.nrm.p + idx, B.V.p + (int64_t)idx * B.ld,
+                                                        B.stop.p, idx);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+  }
+}
+
+void arnoldi_ground(qd_ham* H, cplx* psi, int kdim, int add_dim, bool extend, double* evals_out,
+                    qd_lanczos_result* res) {
+  Ctx* ctx = H->ctx;
+  const int64_t n = H->dim;
+  QD_REQUIRE(kdim >= 1 && kdim <= 4096, QD_ERR_INVALID, "krylov_dim must be in 1..4096");
+  QD_REQUIRE(n >= 1, QD_ERR_INVALID, "empty sector");
+  const int g = ev_grid(ctx, n);
+  if (extend) {
+    QD_REQUIRE(H->arnoldi_gs && H->arnoldi_gs->open && H->arnoldi_gs->kdim == kdim, QD_ERR_INVALID,
+               "no open Arnoldi ground-state solve of krylov_dim %d on this operator", kdim);
+  } else {
+    if (!H->arnoldi_gs) H->arnoldi_gs.reset(new ArnoldiGround());
+    ArnoldiGround& B = *H->arnoldi_gs;
+    B.ensure(n, kdim, g, ctx->stream);
+    B.act = 0;
+    B.open = true;
+    B.broke = false;
+    // initKrylov: v_0 = psi / ||psi||
+    ev_norm_only_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, psi, B.nrm2.p, GridRed<double>{B.rpart.p, B.tickets.p + 1});
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+    double n0 = 0.0;
+    QD_CUDA(cudaMemcpyAsync(&n0, B.nrm2.p, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    QD_CUDA(cudaStreamSynchronize(ctx->stream));
+    QD_REQUIRE(n0 > 0.0, QD_ERR_INVALID, "start vector is zero");
+    ev_init_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, psi, B.nrm2.p, B.V.p);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+    QD_CUDA(cudaMemsetAsync(B.stop.p, 0, sizeof(int), ctx->stream));
+  }
+  ArnoldiGround& B = *H->arnoldi_gs;
+  // updateKrylovRepr: add_dim = -1 (here <= 0) or past kry_dim -> up to kry_dim
+  int steps = (add_dim <= 0 || B.act + add_dim > kdim) ? kdim - B.act : add_dim;
+  if (B.broke) steps = 0;  // a space that closed does not grow
+  const int first = B.act + 1;
+  if (steps > 0) {
+    if (H->flags & QD_HAM_REAL)
+      arnoldi_ground_steps<double>(H, H->vals_r.p, B, first, B.act + steps);
+    else
+      arnoldi_ground_steps<cplx>(H, H->vals_c.p, B, first, B.act + steps);
+  }
+  int stop = 0;
+  QD_CUDA(cudaMemcpyAsync(&stop, B.stop.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  const int act_prev = B.act;
+  if (steps > 0) {
+    B.act = stop ? stop : B.act + steps;  // expandBasis<0>: the breaking step counts
+    B.broke = stop != 0;
+  }
+  const int act = B.act;
+  QD_REQUIRE(act >= 1, QD_ERR_INVALID, "no Krylov step was run");
+  // lower triangle of KR[:act, :act]: Re <v_i, H v_i> and ||w_{i+1}||
+  std::vector<cplx> hc((size_t)act * B.ldh);
+  std::vector<double> nrm(act + 1);
+  QD_CUDA(cudaMemcpyAsync(hc.data(), B.hcol.p, hc.size() * sizeof(cplx), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(nrm.data(), B.nrm.p, (act + 1) * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::vector<double> d(act), e(act), ev(act), y(act);
+  for (int i = 0; i < act; ++i) {
+    d[i] = hc[(size_t)i * B.ldh + i].re;
+    e[i] = (i + 1 < act) ? nrm[i + 1] : 0.0;
+  }
+  QD_REQUIRE(tridiag_lowest<double>(act, d.data(), e.data(), ev.data(), y.data()) == 0, QD_ERR_INVALID,
+             "tridiagonal eigensolver did not converge");
+  std::vector<cplx> yc(act);
+  for (int j = 0; j < act; ++j) yc[j] = mkc(y[j], 0.0);
+  QD_CUDA(cudaMemcpyAsync(B.e.p, yc.data(), act * sizeof(cplx), cudaMemcpyHostToDevice, ctx->stream));
+  ev_combine_long_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, act, B.e.p, psi);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (evals_out) std::memcpy(evals_out, ev.data(), act * sizeof(double));
+  res->act_dim = act;
+  res->breakdown = B.broke ? 1 : 0;
+  res->matvecs = act - act_prev;
+  res->ritz_value = ev[0];
+  res->err = std::fabs(ev[0]);
+}
+
+void ArnoldiGroundDeleter::operator()(ArnoldiGround* b) const { delete b; }
 
 void ArnoldiDeleter::operator()(ArnoldiBuffers* b) const { delete b; }
 

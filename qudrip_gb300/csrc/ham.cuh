@@ -25,6 +25,10 @@ struct ArnoldiBuffers;
 struct ArnoldiDeleter {
   void operator()(ArnoldiBuffers* b) const;
 };
+struct ArnoldiGround;
+struct ArnoldiGroundDeleter {
+  void operator()(ArnoldiGround* b) const;
+};
 
 struct GateDev {
   int kind, site, site_b, string;
@@ -108,6 +112,8 @@ struct qd_ham {
   bool one_shot = false;    // solved once (a served request): launch directly instead of capturing a graph
   std::unique_ptr<qd::Workspace, qd::WorkspaceDeleter> ws;  // solver buffers, reused across calls
   std::unique_ptr<qd::ArnoldiBuffers, qd::ArnoldiDeleter> arnoldi;
+  std::unique_ptr<qd::ArnoldiGround, qd::ArnoldiGroundDeleter> arnoldi_gs;  // Arnoldi ground-state solve
+  double arnoldi_gs_ritz = 0.0;  // its last lowest eigenvalue (the error of a grown solve)
 };
 
 namespace qd {

@@ -127,6 +127,7 @@ void ham_scale(qd_ham* H, cplx s) {
   // every form derived from the values goes
   H->ws.reset();
   H->arnoldi.reset();
+  H->arnoldi_gs.reset();
   H->fx.reset();
   H->fx_state = 0;
   H->mfx.reset();

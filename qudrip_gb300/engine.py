@@ -370,12 +370,62 @@ class LanczosSolver:
 
 
 class ArnoldiSolver:
-    """Arnoldi::getSolver(index, kry_dim) -- ArnoldiSolver<T, herm=0> (real-time steps)."""
+    """Arnoldi::getSolver(index, kry_dim) -- ArnoldiSolver<T, herm=0>: Krylov real-time
+    steps (evolve) and the incremental Arnoldi ground state (getGroundState).
+
+    getGroundState(H, psi, tstp, add_dim) keeps its Krylov space between calls
+    as the reference solver does: the first call starts from psi(tstp) and
+    runs add_dim steps of full orthogonalisation (all kry_dim for -1), later
+    calls grow the same space (qd_arnoldi_extend) until kry_dim or a
+    breakdown; psi(tstp) receives the Ritz vector each time.  error() is the
+    change of the lowest N eigenvalues since the previous call, N and the
+    initial values set by convergeEV(N, iv) (sparse_algorithm.hpp:494-500,
+    564-585), the loop of programs/two_liquid_sq.cpp:464-476."""
 
     def __init__(self, index: Sector, kry_dim: int):
         self.index = index
         self.kry_dim = kry_dim
         self._act = 0
+        self._gs_act = 0
+        self._gs_full = False
+        self._evals = np.empty(0)
+        self._err = 0.0
+        self._evs = np.zeros(1)
+        self.result = None
+
+    def convergeEV(self, N: int, iv: float = 0.0) -> None:
+        if not N < self.kry_dim:
+            raise ValueError("convergeEV: N must be below kry_dim")
+        self._evs = np.full(N, float(iv))
+
+    def getGroundState(self, H: Hamiltonian, psi: State, tstp: int, add_dim: int = -1):
+        if self._gs_act >= self.kry_dim or self._gs_full:
+            return self.result
+        opts = A.qd_lanczos_opts(self.kry_dim, A.QD_SPMV_CSR, A.QD_RITZ_STORED_BASIS, add_dim if add_dim > 0 else 0)
+        evals = np.empty(self.kry_dim, dtype=np.float64)
+        res = A.qd_lanczos_result()
+        name = "qd_arnoldi_ground" if self._gs_act == 0 else "qd_arnoldi_extend"
+        A.call(name, H.handle, psi.handle, tstp, C.byref(opts), evals.ctypes.data_as(C.POINTER(C.c_double)),
+               C.byref(res))
+        self._gs_act = self._act = res.act_dim
+        self._gs_full = bool(res.breakdown)
+        self._evals = evals[:res.act_dim].copy()
+        m = min(len(self._evs), res.act_dim)
+        self._err = float(np.sqrt(np.sum((self._evals[:m] - self._evs[:m]) ** 2)))
+        self._evs[:m] = self._evals[:m]
+        self.result = res
+        return res
+
+    def error(self) -> float:
+        return self._err
+
+    def eigenvalues(self) -> np.ndarray:
+        return self._evals
+
+    def storeE(self, fname: str) -> None:
+        with open(fname, "w") as f:
+            for e in self._evals:
+                f.write(f"{e:.6g}\n")
 
     def evolve(self, H: Hamiltonian, psi: State, tstp: int, h: float, kry_dim_rt: int = 0) -> None:
         """psi(tstp + 1) = exp(-i H h) psi(tstp) / ||psi(tstp)|| (sparse_algorithm.hpp:548-562)."""
