@@ -150,3 +150,31 @@ def test_oracle_lanczos_breakdown_small_space():
     H = O.Ham(sec, ham)
     r = H.lanczos_ground(np.array([1.0, 0.3]), 10)
     assert r["breakdown"] == 1 and r["act_dim"] == 1
+
+
+def test_trajectory_ensemble_fixture_consistent():
+    """tests/golden/traj_ensemble_L8.json (the FP64 oracle ensemble the device ensemble is
+    compared with): every trajectory starts in the ground state, so at t=0 the mean is that
+    state's <n_{i,up} n_{i,dn}> with zero spread; later means are probabilities with small errors."""
+    import json
+    import os
+    import scipy.sparse.linalg as sla
+    import oracle as O
+    from qudrip_gb300 import chains
+    with open(os.path.join(os.path.dirname(__file__), "golden", "traj_ensemble_L8.json")) as f:
+        g = json.load(f)
+    L = g["L"]
+    spec, ham = chains.hubbard_chain(L, g["Nup"], g["Ndo"], g["U"], g["thop"])
+    osec = O.Sector(spec)
+    H = O.Ham(osec, ham).scipy().tocsr()
+    w, v = sla.eigsh(H.real, k=1, which="SA", tol=1e-13)
+    assert abs(w[0] - g["ground_energy"]) < 1e-10
+    p = np.abs(v[:, 0]) ** 2
+    b = osec.basis()
+    docc0 = [p[(b >> i) & (b >> (i + L)) & 1 == 1].sum() for i in range(L)]
+    mean = np.array(g["mean"])
+    err = np.array(g["stderr"])
+    assert mean.shape == (g["nsteps"] // g["record_every"] + 1, L)
+    assert np.abs(mean[0] - docc0).max() < 1e-9 and np.all(err[0] < 1e-9)
+    assert np.all((mean >= 0) & (mean <= 1)) and np.all(err[1:] > 0) and np.all(err < 0.01)
+    assert g["jumps"] > 0.5 * g["ntraj"] * g["gamma"] * (g["Nup"] + g["Ndo"]) * g["nsteps"] * g["dt"]
