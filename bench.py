@@ -319,6 +319,11 @@ def gpu_arm(args, rank, world, local):
         spmv_name = ("uniform_coupling_fixed_point_sums_sliced_columns_one_launch_step" if one_launch else
                      "uniform_coupling_fixed_point_sums_sliced_columns_fused_dots")
         traffic = profile_traffic("lz_fx_step_xxz_L24" if one_launch else "spmv_fx_dots_xxz_L24")
+    elif info.product_kernel == 122:
+        kernel_name = "lz_fx_step_kernel<BlockRows,true>" if one_launch else "spmv_fx_block_dots_kernel<true>"
+        spmv_name = ("uniform_coupling_fixed_point_sums_block_layout_one_launch_step" if one_launch else
+                     "uniform_coupling_fixed_point_sums_block_layout_fused_dots")
+        traffic = profile_traffic("lz_fx_step_block_xxz_L24" if one_launch else "spmv_fx_block_dots_xxz_L24")
     elif info.product_kernel == 121:
         kernel_name = "lz_fx_step_kernel<SlotRows,true>" if one_launch else "spmv_fx_slots_dots_kernel<true>"
         spmv_name = ("uniform_coupling_fixed_point_sums_columns_from_terms_one_launch_step" if one_launch else

@@ -519,7 +519,8 @@ typedef struct qd_server_opts {
   int32_t large_lanes;  /* lanes for any request (default 3) */
   int32_t batch_lanes;  /* QD_SERVE_MIXED: lanes for batched ground states (default 2) */
   int32_t batch_max;    /* requests per batched launch (default 64) */
-  int32_t reserved0;
+  int32_t batch_min;    /* QD_SERVE_MIXED: a batch lane starts once this many batchable ground states
+                           wait (default 4); fewer go to the small lanes one by one */
   int64_t small_dim;    /* default 65536 */
   int64_t hbm_budget;   /* bytes admitted requests may hold; 0 = 80% of free memory */
   int64_t batch_dim;    /* QD_SERVE_MIXED: ground states with dim <= batch_dim are batched (default 3432) */

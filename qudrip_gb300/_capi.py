@@ -38,6 +38,7 @@ QD_RITZ_STORED_BASIS = 0
 QD_RITZ_SECOND_PASS = 1
 QD_SPMV_FX = 120  # uniform-coupling form with exact fixed-point row sums
 QD_SPMV_FX_SLOTS = 121  # the same with the columns computed on the fly from the terms
+QD_SPMV_FX_BLOCK = 122  # the same on the block layout of the sector (no column read)
 SPMV_KERNELS = {100: "tile", 101: "balanced", 102: "vector2", 103: "vector4", 104: "vector8",
                 105: "scalar", 106: "row4", 107: "row8", 108: "row4_stream", 109: "row8_stream",
                 110: "row_exact", 111: "row_sorted"}
@@ -101,7 +102,7 @@ QD_PATH_BATCH = 1
 
 class qd_server_opts(C.Structure):
     _fields_ = [("mode", C.c_int32), ("small_lanes", C.c_int32), ("large_lanes", C.c_int32),
-                ("batch_lanes", C.c_int32), ("batch_max", C.c_int32), ("reserved0", C.c_int32),
+                ("batch_lanes", C.c_int32), ("batch_max", C.c_int32), ("batch_min", C.c_int32),
                 ("small_dim", C.c_int64), ("hbm_budget", C.c_int64), ("batch_dim", C.c_int64),
                 ("reserved", C.c_int32 * 2)]
 

@@ -315,7 +315,9 @@ qd_status qd_ham_get_info(qd_ham* ham, qd_ham_info* info) {
     info->has_matrix_free = ham->has_mf ? 1 : 0;
     info->product_kernel = ham->spmv_variant;
     if ((ham->flags & QD_HAM_REAL) && ham->fx_allowed && ham_build_fx(ham))
-      info->product_kernel = (ham->fx->use_slots && ham->fx->slots_state > 0) ? kSpmvFxSlots : kSpmvFx;
+      info->product_kernel = (ham->fx->use_blk && ham->fx->blk_state > 0)
+                                 ? kSpmvFxBlock
+                                 : ((ham->fx->use_slots && ham->fx->slots_state > 0) ? kSpmvFxSlots : kSpmvFx);
     if (ham->fx && ham->fx->step_fused) info->step_launches = ham->fx->step_fused > 0 ? 1 : 2;
   });
 }
@@ -500,6 +502,7 @@ qd_status qd_ham_time_spmv(qd_ham* ham, int spmv, int iters, double* avg_ms, dou
   return guard([&] {
     QD_REQUIRE(ham && avg_ms && bytes_per_launch && iters >= 1, QD_ERR_INVALID, "bad argument");
     const bool plain = spmv == QD_SPMV_CSR || spmv == QD_SPMV_MATRIX_FREE || spmv == kSpmvFx || spmv == kSpmvFxSlots ||
+                       spmv == kSpmvFxBlock ||
                        (spmv >= kSpmvTile && spmv <= kSpmvLast);
     const bool fused = spmv >= 2000 + kSpmvTile && spmv <= 2000 + kSpmvLast;
     const bool vec = spmv == 3001 || spmv == 3002;
@@ -625,14 +628,18 @@ qd_status qd_traj_run(qd_ham* heff, const qd_traj_desc* desc, const double* psi0
 
 qd_status qd_ham_set_spmv_kernel(qd_ham* ham, int kernel) {
   return guard([&] {
-    QD_REQUIRE(ham && ((kernel >= kSpmvTile && kernel <= kSpmvLast) || kernel == kSpmvFx || kernel == kSpmvFxSlots),
+    QD_REQUIRE(ham && ((kernel >= kSpmvTile && kernel <= kSpmvLast) || kernel == kSpmvFx || kernel == kSpmvFxSlots ||
+                       kernel == kSpmvFxBlock),
                QD_ERR_INVALID, "unknown product kernel");
     DeviceGuard dg(ham->ctx->device);
-    if (kernel == kSpmvFx || kernel == kSpmvFxSlots) {
+    if (kernel == kSpmvFx || kernel == kSpmvFxSlots || kernel == kSpmvFxBlock) {
       QD_REQUIRE(ham_build_fx(ham), QD_ERR_UNSUPPORTED, "the fixed-point form does not apply to this operator");
-      QD_REQUIRE(kernel == kSpmvFx || ham_build_fx_slots(ham), QD_ERR_UNSUPPORTED,
+      QD_REQUIRE(kernel != kSpmvFxSlots || ham_build_fx_slots(ham), QD_ERR_UNSUPPORTED,
                  "the columns of this operator cannot be computed on the fly (code 121)");
+      QD_REQUIRE(kernel != kSpmvFxBlock || ham_build_fx_block(ham), QD_ERR_UNSUPPORTED,
+                 "this sector or operator has no block layout (code 122)");
       ham->fx->use_slots = (kernel == kSpmvFxSlots);
+      ham->fx->use_blk = (kernel == kSpmvFxBlock);
       ham->fx_allowed = true;
       return;
     }
@@ -662,13 +669,15 @@ qd_status qd_ham_autotune(qd_ham* ham, int iters, int* chosen, double* best_ms) 
     if ((ham->flags & QD_HAM_REAL) && ham_build_fx(ham)) {
       // the fixed-point forms as the recurrence launches them (fused with the step's inner products,
       // which a CSR kernel leaves to a separate pass): a conservative comparison for them
-      const bool slots0 = ham->fx->use_slots;
+      const bool slots0 = ham->fx->use_slots, blk0 = ham->fx->use_blk;
       int fx_pick = 0;
-      for (int v = kSpmvFx; v <= kSpmvFxSlots; ++v) {
+      for (int v = kSpmvFx; v <= kSpmvFxBlock; ++v) {
         if (v == kSpmvFxSlots && !ham_build_fx_slots(ham)) continue;
+        if (v == kSpmvFxBlock && !ham_build_fx_block(ham)) continue;
         double ms = 0;
         ham->fx_allowed = true;
         ham->fx->use_slots = (v == kSpmvFxSlots);
+        ham->fx->use_blk = (v == kSpmvFxBlock);
         time_spmv(ham, QD_SPMV_CSR, iters, &ms, &bytes);
         if (ms < best) {
           best = ms;
@@ -678,6 +687,7 @@ qd_status qd_ham_autotune(qd_ham* ham, int iters, int* chosen, double* best_ms) 
       }
       ham->fx_allowed = fx_pick != 0;
       ham->fx->use_slots = fx_pick ? (fx_pick == kSpmvFxSlots) : slots0;
+      ham->fx->use_blk = fx_pick ? (fx_pick == kSpmvFxBlock) : blk0;
     }
     if (chosen) *chosen = pick;
     if (best_ms) *best_ms = best;

@@ -154,6 +154,10 @@ bool ham_build_fx(qd_ham* H) {
   build_sell(ctx, *fx, n);
   H->fx = std::move(fx);
   H->fx_state = 1;
+  // QD_FX_BLOCK=1 makes the block layout (code 122) the default where the sector and the
+  // terms give it; otherwise the stored columns stay (the autotuner may still pick 122)
+  const char* blk_env = std::getenv("QD_FX_BLOCK");
+  if (blk_env && std::strcmp(blk_env, "1") == 0 && ham_build_fx_block(H)) H->fx->use_blk = true;
   return true;
 }
 
@@ -321,6 +325,10 @@ void launch_fx_dots(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x,
   const double cF = std::ldexp(f.c, -f.F);
   const int g = fx_dots_grid(ctx, H->dim);
   QD_REQUIRE(g <= kMaxGrid, QD_ERR_UNSUPPORTED, "reduction grid exceeds its partials buffer");
+  if (f.blk_state > 0 && f.use_blk) {  // same grid: the same reduction tree as below
+    launch_fx_block_dots(ctx, H, f, x, X, V2, y, s1, s2, stop, step, beta, alpha, dots, red, g);
+    return;
+  }
   if (f.slots_state > 0 && f.use_slots) {  // same grid: the same reduction tree as below
     launch_fx_slots_dots(ctx, H, f, x, X, V2, y, s1, s2, stop, step, beta, alpha, dots, red, g);
     return;
@@ -354,10 +362,14 @@ bool launch_fx_step(Ctx* ctx, const qd_ham* H, const FxForm& f, FxStepArgs a) {
   a.F = f.F;
   const int g = fx_dots_grid(ctx, H->dim);
   bool ok = false;
-  if (g <= kMaxGrid)
-    ok = (f.slots_state > 0 && f.use_slots)
-             ? launch_fx_slots_step(ctx, H, f, a, g)
-             : fx_step_launch(ctx, SellRows{f.sell_off.p, f.sell_col.p, f.sell_len.p, a.X}, a, g, 0);
+  if (g <= kMaxGrid) {
+    if (f.blk_state > 0 && f.use_blk)
+      ok = launch_fx_block_step(ctx, H, f, a);
+    else if (f.slots_state > 0 && f.use_slots)
+      ok = launch_fx_slots_step(ctx, H, f, a, g);
+    else
+      ok = fx_step_launch(ctx, SellRows{f.sell_off.p, f.sell_col.p, f.sell_len.p, a.X}, a, g, 0);
+  }
   f.step_fused = ok ? 1 : -1;
   return ok;
 }
@@ -370,6 +382,10 @@ __global__ void fx_shadow_kernel(int64_t n, const double* x, __int128* X, int F,
 
 void launch_fx(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x, const __int128* X, double* y,
                const double* scale_dev, const int* stop, int step) {
+  if (f.blk_state > 0 && f.use_blk && !scale_dev && !stop) {  // the plain product (timing)
+    launch_fx_block(ctx, H, f, x, X, y);
+    return;
+  }
   if (f.slots_state > 0 && f.use_slots) {
     launch_fx_slots(ctx, H, f, x, X, y, scale_dev, stop, step);
     return;

@@ -89,6 +89,24 @@ struct FxForm {
   // at sell_off[s] + 128 (k / 4) + 4 l + k % 4 (fxsum.cu), the row's count in sell_len
   int64_t sell_cols = 0;  // stored slots, padding included
   mutable int step_fused = 0;  // the last Lanczos step on this form: 1 one launch (fxstep.cuh), -1 two
+  // the block layout (code 122, fxblock.cu): rows grouped by the high part of their state
+  int blk_state = 0;       // 0 not tried, 1 built and checked, -1 not applicable
+  bool use_blk = false;    // the one-launch step (and the plain product) take the block form
+  int blk_lowbits = 0, blk_lstride = 0, blk_hstride = 0, blk_ncross = 0;
+  uint32_t blk_cross[24];  // crossing transitions: support, input pattern, flip
+  DBuf<uint32_t> blk_state32;  // the basis in 32 bits
+  DBuf<int32_t> blk_off;       // first row of each high part's block (-1: none)
+  DBuf<uint16_t> blk_rank;     // rank of each low part among those of its popcount
+  DBuf<uint8_t> blk_ldeg;      // targets of each low part ...
+  DBuf<uint16_t> blk_ladj;     // ... as positions in the block
+  DBuf<uint8_t> blk_hdeg;      // target blocks of each high part ...
+  DBuf<int32_t> blk_hadj;      // ... as their first rows
+  // the staged one-launch step: groups of whole blocks (rows [x, y)), contiguous runs of groups per CTA
+  int blk_part_state = 0;      // 0 not tried, 1 built, -1 the step does not fit
+  int blk_nctas = 0, blk_threads = 0, blk_max_group = 0, blk_max_cta = 0;
+  size_t blk_smem = 0;
+  DBuf<int2> blk_groups;
+  DBuf<int32_t> blk_cta_first;
   DBuf<int64_t> sell_off;
   DBuf<int32_t> sell_col;
   DBuf<uint8_t> sell_len;

@@ -482,20 +482,29 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   // code 1: what the matrix-free Lanczos path launches (the slot form with its dots where it applies)
   const bool mfx = mf && real && H->fx_allowed && ham_build_mf_fx(H);
   // code 0: the product the real Lanczos path launches (the fixed-point form when it applies)
-  const bool fxcode = spmv == kSpmvFx || spmv == kSpmvFxSlots;
+  const bool fxcode = spmv == kSpmvFx || spmv == kSpmvFxSlots || spmv == kSpmvFxBlock;
   const bool fx = real && (fxcode || (spmv == QD_SPMV_CSR && H->fx_allowed)) && ham_build_fx(H);
   QD_REQUIRE(!fxcode || fx, QD_ERR_UNSUPPORTED, "the fixed-point form does not apply to this operator");
   QD_REQUIRE(spmv != kSpmvFxSlots || ham_build_fx_slots(H), QD_ERR_UNSUPPORTED,
              "the columns of this operator cannot be computed on the fly (code 121)");
-  struct SlotChoice {  // 120 / 121 pick the column source for this timing only
+  QD_REQUIRE(spmv != kSpmvFxBlock || ham_build_fx_block(H), QD_ERR_UNSUPPORTED,
+             "this sector or operator has no block layout (code 122)");
+  struct SlotChoice {  // 120 / 121 / 122 pick the column source for this timing only
     FxForm* f;
-    bool saved;
+    bool saved, saved_blk;
     ~SlotChoice() {
-      if (f) f->use_slots = saved;
+      if (f) {
+        f->use_slots = saved;
+        f->use_blk = saved_blk;
+      }
     }
-  } choice{fx ? H->fx.get() : nullptr, fx ? H->fx->use_slots : true};
-  if (fx && fxcode) H->fx->use_slots = (spmv == kSpmvFxSlots);
+  } choice{fx ? H->fx.get() : nullptr, fx ? H->fx->use_slots : true, fx ? H->fx->use_blk : false};
+  if (fx && fxcode) {
+    H->fx->use_slots = (spmv == kSpmvFxSlots);
+    H->fx->use_blk = (spmv == kSpmvFxBlock);
+  }
   const bool slots = fx && H->fx->use_slots && H->fx->slots_state > 0;
+  const bool blk = fx && H->fx->use_blk && H->fx->blk_state > 0;
   DBuf<__int128> X((fx || mfx) ? n + 32 : 1);
   if (fx || mfx) QD_CUDA(cudaMemsetAsync(X.p, 0, X.bytes(), ctx->stream));
   // what the Lanczos recurrence launches on the uniform-coupling form: the
@@ -599,7 +608,7 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
            // (+ v2 for the fused dots)
     *bytes_per_launch = (double)H->fx->sell_cols * 4.0 + (double)((n + 31) / 32 + 1) * 8.0 + (double)n +
                         (double)n * (8.0 + 8.0 + 16.0 + 8.0 + (spmv == QD_SPMV_CSR ? 8.0 : 0.0));
-  if (slots)  // 32-bit state, diagonal, x, its fixed-point copy once, y (+ v2)
+  if (slots || blk)  // 32-bit state, diagonal, x, its fixed-point copy once, y (+ v2)
     *bytes_per_launch = (double)n * (4.0 + 8.0 + 8.0 + 16.0 + 8.0 + (spmv == QD_SPMV_CSR ? 8.0 : 0.0));
   if (stepped)  // one Lanczos step: w stays on chip; v_k and its fixed-point copy are written
     *bytes_per_launch += (double)n * (8.0 + 16.0 - 8.0);
@@ -730,7 +739,10 @@ static void lanczos_ground_impl(qd_ham* H, cplx* psi, const double* psi_nrm2, co
   const bool fx = fxk == 1;
   const int fxF = fx ? form->F : 0;
   const bool one_launch = fx && fx_one_launch_step() && !H->one_shot;
-  const int kind = (mf ? 1 : 0) + 2 * fxk + (one_launch ? 4 : 0) + ((one_launch && step_wait_out_polls()) ? 8 : 0);
+  // the column source of the fixed-point form is part of what a captured recurrence launches
+  const int src = !fx ? 0 : ((form->blk_state > 0 && form->use_blk) ? 2 : ((form->slots_state > 0 && form->use_slots) ? 1 : 0));
+  const int kind = (mf ? 1 : 0) + 2 * fxk + (one_launch ? 4 : 0) + ((one_launch && step_wait_out_polls()) ? 8 : 0) +
+                   16 * src;
   if (B.kind != kind) {
     B.drop_graph();
     B.kind = kind;

@@ -7,8 +7,9 @@
 //     thread.  Small lanes (high stream priority) take requests whose sector
 //     dimension is at most small_dim; large lanes take any request; batch
 //     lanes (mixed form) take every waiting small ground state with a real
-//     start vector at once and run them in one persistent launch
-//     (batch_lanczos, one CTA per instance).  Requests on different lanes
+//     start vector at once, once at least batch_min of them wait, and run
+//     them in one persistent launch (batch_lanczos, one CTA per instance);
+//     below that the small lanes serve them one by one at once.  Requests on different lanes
 //     overlap on the GPU; a request that arrives while others run is taken by
 //     the next lane that frees up (continuous batching, not a queue in front
 //     of a single solver).
@@ -175,11 +176,14 @@ static bool batchable(const qd_server* S, const ServeReq* r) {
          r->real_start && r->d.krylov_dim <= 256;
 }
 
+// Small lanes take every small request, batchable ground states included (a lone
+// small ground state is served at once instead of waiting for a batch); batch
+// lanes take batchable ground states only once batch_min of them wait (take()).
 static bool eligible(const qd_server* S, const ServeReq* r, LaneKind k) {
   const bool small = r->dim_est <= S->o.small_dim;
   switch (k) {
     case kLaneBatch: return batchable(S, r);
-    case kLaneSmall: return small && !batchable(S, r);
+    case kLaneSmall: return small;
     default: return !batchable(S, r);
   }
 }
@@ -190,6 +194,11 @@ static bool eligible(const qd_server* S, const ServeReq* r, LaneKind k) {
 static std::vector<ServeReq*> take(qd_server* S, LaneKind k) {
   std::vector<ServeReq*> got;
   const int cap = (k == kLaneBatch) ? std::max(1, S->o.batch_max) : 1;
+  if (k == kLaneBatch) {
+    int waiting = 0;
+    for (const ServeReq* r : S->pending) waiting += batchable(S, r) ? 1 : 0;
+    if (waiting < std::max(1, S->o.batch_min)) return got;
+  }
   int kdim = -1;
   for (auto it = S->pending.begin(); it != S->pending.end() && (int)got.size() < cap;) {
     ServeReq* r = *it;
@@ -499,6 +508,7 @@ qd_status qd_server_create(qd_ctx* ctx_, const qd_server_opts* opts, qd_server**
     if (o.batch_lanes <= 0) o.batch_lanes = 2;
     if (o.mode == QD_SERVE_PLAIN) o.batch_lanes = 0;
     if (o.batch_max <= 0) o.batch_max = 64;
+    if (o.batch_min <= 0) o.batch_min = 4;
     if (o.small_dim <= 0) o.small_dim = 65536;
     if (o.batch_dim <= 0) o.batch_dim = 3432;
     QD_REQUIRE(o.small_lanes + o.large_lanes + o.batch_lanes <= 64, QD_ERR_INVALID, "at most 64 lanes");

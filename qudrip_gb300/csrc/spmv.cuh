@@ -33,6 +33,7 @@ enum SpmvVariant {
   kSpmvLast = 111,
   kSpmvFx = 120,        // uniform-coupling form, exact fixed-point sums (fxsum.cuh)
   kSpmvFxSlots = 121,   // as 120 with the columns computed on the fly (fxslots.cu)
+  kSpmvFxBlock = 122,   // as 120 on the block layout of the sector, no column read (fxblock.cu)
 };
 
 constexpr int kSpmvWarps = 4;  // warps per block

@@ -696,7 +696,7 @@ class Server:
 
     def __init__(self, mode: str = "mixed", small_lanes: int = 4, large_lanes: int = 3, batch_lanes: int = 2,
                  batch_max: int = 64, small_dim: int = 65536, hbm_budget: int = 0, batch_dim: int = 3432,
-                 ctx: Optional[Context] = None):
+                 batch_min: int = 4, ctx: Optional[Context] = None):
         self.ctx = ctx or default_context()
         o = A.qd_server_opts()
         o.mode = A.QD_SERVE_MIXED if mode == "mixed" else A.QD_SERVE_PLAIN
@@ -704,6 +704,7 @@ class Server:
         o.large_lanes = large_lanes
         o.batch_lanes = batch_lanes
         o.batch_max = batch_max
+        o.batch_min = batch_min
         o.small_dim = small_dim
         o.hbm_budget = hbm_budget
         o.batch_dim = batch_dim

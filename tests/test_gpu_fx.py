@@ -117,7 +117,7 @@ def test_columns_on_the_fly_bit_identical_to_stored_columns(ctx, name):
     columns, and the recurrence launches the same grid and reduction, so the solve is bit-identical."""
     spec, ham = CASES[name]()
     sec, H = gpu_objects(spec, ham)
-    assert product_kernel(H) == A.QD_SPMV_FX  # stored columns by default; 121 where it is chosen
+    assert product_kernel(H) == A.QD_SPMV_FX  # stored columns by default
     v0 = q.start_vector(sec.dim, 17)
     r121, psi121 = solve(sec, H, v0, 60, kernel=A.QD_SPMV_FX_SLOTS)
     r120, psi120 = solve(sec, H, v0, 60, kernel=A.QD_SPMV_FX)
@@ -156,6 +156,39 @@ def test_columns_on_the_fly_timing_and_fallback(ctx):
         with pytest.raises(A.QDError) as e:
             A.call("qd_ham_set_spmv_kernel", H2.handle, A.QD_SPMV_FX_SLOTS)
         assert e.value.code == A.QD_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_block_layout_step_matches_stored_columns(ctx, name):
+    """Code 122: the block layout of the sector (rows grouped by the high part of their state; tables of
+    the low and high parts' targets, checked against the stored columns at build).  Its one-launch step
+    stages each group of whole blocks in shared memory with one bulk copy; every row's product carries
+    code 120's bits, the inner products add in another order, so the solve agrees with code 120's to
+    rounding, and its two-launch step (served requests) is bit-identical to code 120's."""
+    spec, ham = CASES[name]()
+    sec, H = gpu_objects(spec, ham)
+    v0 = q.start_vector(sec.dim, 17)
+    r120, psi120 = solve(sec, H, v0, 60, kernel=A.QD_SPMV_FX)
+    r122, psi122 = solve(sec, H, v0, 60, kernel=A.QD_SPMV_FX_BLOCK)
+    info = A.qd_ham_info()
+    A.call("qd_ham_get_info", H.handle, C.byref(info))
+    assert info.product_kernel == A.QD_SPMV_FX_BLOCK and info.step_launches == 1
+    assert r122.act_dim == r120.act_dim and r122.matvecs == r120.matvecs
+    assert abs(r122.ritz_value - r120.ritz_value) <= 1e-12 * abs(r120.ritz_value)
+    ov = abs(np.vdot(psi122, psi120)) / (np.linalg.norm(psi122) * np.linalg.norm(psi120))
+    assert ov >= 1 - 1e-10
+    o = O.Ham(O.Sector(spec), ham).lanczos_ground(v0, 60)
+    assert abs(r122.ritz_value - o["ritz"]) <= 1e-10 * abs(o["ritz"])
+
+
+def test_block_layout_two_launch_step_bit_identical(ctx, monkeypatch):
+    monkeypatch.setenv("QD_LANCZOS_STEP", "split")
+    spec, ham = chains.xxz_chain(16, 1.0, 0.7, periodic=True)
+    sec, H = gpu_objects(spec, ham)
+    v0 = q.start_vector(sec.dim, 3)
+    r120, psi120 = solve(sec, H, v0, 60, kernel=A.QD_SPMV_FX)
+    r122, psi122 = solve(sec, H, v0, 60, kernel=A.QD_SPMV_FX_BLOCK)
+    assert r122.ritz_value == r120.ritz_value and np.array_equal(psi122, psi120)
 
 
 @pytest.mark.parametrize("L,fields,kernel", [(16, None, None), (14, "random", None), (14, None, 121)])
@@ -197,6 +230,8 @@ def test_large_sector_takes_the_two_launch_step(ctx):
     info = A.qd_ham_info()
     A.call("qd_ham_get_info", H.handle, C.byref(info))
     assert info.product_kernel == A.QD_SPMV_FX and info.step_launches == 2
+    r_blk, psi_blk = solve(sec, H, v0, 30, kernel=A.QD_SPMV_FX_BLOCK)  # the block form's two-launch step
+    assert r_blk.ritz_value == r_fx.ritz_value and np.array_equal(psi_blk, psi_fx)
     r_csr, psi_csr = solve(sec, H, v0, 30, kernel=110)
     assert r_fx.act_dim == r_csr.act_dim == 30
     assert abs(r_fx.ritz_value - r_csr.ritz_value) <= 1e-12 * abs(r_csr.ritz_value)

@@ -179,7 +179,8 @@ def oracle_results(requests):
 
 @pytest.mark.parametrize("mode", ["plain", "mixed"])
 def test_served_results_match_oracle(ctx, requests, oracle_results, mode):
-    out, stats = serve(mode, requests, alone=False)
+    # batch_min=1: the batch lanes take every waiting small ground state, so batched results are checked
+    out, stats = serve(mode, requests, alone=False, batch_min=1)
     assert stats["completed"] == len(requests) and stats["failed"] == 0
     for t, r in enumerate(requests):
         res = out[t]
@@ -214,6 +215,18 @@ def test_each_result_same_alone_and_in_the_mix(ctx, requests, mode):
                 assert np.array_equal(a["state"], b["state"])
         else:  # a lone small ground state may take a grid lane when the batch lanes are busy
             assert abs(a["energy"] - b["energy"]) <= DE_TOL * abs(a["energy"])
+
+
+def test_lone_small_ground_states_skip_the_batch(ctx, requests):
+    """With the default batch_min (4), small ground states that arrive one at a time are served by
+    the small lanes at once (no batch launch); the energies match the batched ones within DE_TOL."""
+    alone, st = serve("mixed", requests, alone=True)
+    assert st["batches"] == 0
+    batched, st_b = serve("mixed", requests, alone=False, batch_min=1)
+    assert st_b["batches"] >= 1
+    for t, r in enumerate(requests):
+        if r["kind"] == "ground":
+            assert abs(alone[t]["energy"] - batched[t]["energy"]) <= DE_TOL * abs(alone[t]["energy"])
 
 
 def test_admission_respects_the_byte_budget(ctx, requests):
