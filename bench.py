@@ -440,6 +440,7 @@ def xy_leg(ctx):
     pm, pb = C.c_double(), C.c_double()
     A.call("qd_ham_time_spmv", H.handle, A.QD_SPMV_CSR, 30, C.byref(pm), C.byref(pb))
     unit_bytes = H.nnz * 12 + (dim + 1) * 4 + dim * 16
+    step_bytes = H.nnz * 12 + (dim + 1) * 4 + dim * 24  # one Lanczos step: v2 read, v_k written too
     hbm_peak, _ = peaks()
     achieved = unit_bytes / (pm.value * 1e-3) / 1e9
     exact = -2.0 * sum(np.cos(np.pi * k / (L + 1)) for k in range(1, L + 1) if np.cos(np.pi * k / (L + 1)) > 0)
@@ -447,6 +448,8 @@ def xy_leg(ctx):
             "nnz": int(H.nnz), "matvecs_per_s": mv / (ms.value * 1e-3), "ms_per_solve": ms.value / n,
             "product_ms": pm.value, "algorithmic_bytes_per_matvec": unit_bytes,
             "achieved_GBps": achieved, "frac_of_measured_hbm": achieved / hbm_peak,
+            "algorithmic_bytes_per_step": step_bytes,
+            "frac_of_measured_hbm_step_bytes": step_bytes / (pm.value * 1e-3) / 1e9 / hbm_peak,
             "ritz_value": r.ritz_value, "free_fermion_E0": exact,
             "rel_dE_vs_free_fermion_E0": abs(r.ritz_value - exact) / abs(exact)}
 
