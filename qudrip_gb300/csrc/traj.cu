@@ -17,9 +17,11 @@
 // GB300 form (resident kernel): one CTA per trajectory at a time, persistent
 // over the ensemble.  H_eff is shared by every trajectory and small (config:
 // Hubbard L=8, dim 4,900, 44,100 stored entries), so each CTA stages it in
-// shared memory once -- rows sorted by length into 32-row slices, each entry a
-// 16-bit column with the sign of the uniform off-diagonal value c in its top
-// bit, the diagonal (shifted by the centre mu of its range) in registers --
+// shared memory once -- rows in 32-row slices with their columns in gather
+// order, each entry a 16-bit column with the sign of the uniform off-diagonal
+// value c in its top bit (a lane's entries 2j and 2j+1 in one 32-bit word;
+// when no entry carries -c the kernel's sums are plain adds), the diagonal
+// (shifted by the centre mu of its range) in registers --
 // together with two complex64 copies of the trajectory's vector.  A step is
 // then K products H - mu of the shared-memory vector (the gathers never leave
 // the SM) summed into the truncated Taylor series of exp(-i tau (H - mu)),
@@ -40,6 +42,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <utility>
 #include <vector>
 
 #include "kbatch.cuh"
@@ -81,7 +84,7 @@ struct TrajResArgs {
   // smem segment sizes (elements)
   int tb_len;         // per vector buffer: n + 1 rounded up to 2 (slot n is a zero)
   int ent_len;        // entries rounded up to 8
-  const uint16_t* ent;   // entry k of slice row l at sdesc.x + 32 k + l: column | sign << 15
+  const uint16_t* ent;   // entry k of slice row l at sdesc.x + 64 (k / 2) + 2 l + k % 2: column | sign << 15
   const uint16_t* rid;   // row of each slot (n: padding)
   const uint32_t* st;    // state bits of each slot
   const int2* sdesc;     // per slice: entry offset, width
@@ -146,6 +149,7 @@ __device__ __forceinline__ void traj_block_sums(const TrajResArgs& A, const Traj
   __syncthreads();
 }
 
+template <bool kSigned>
 __global__ void __launch_bounds__(kTrajMaxWarps * 32, 1) traj_resident_kernel(TrajResArgs A) {
   extern __shared__ __align__(16) unsigned char traj_smem[];
   __shared__ float res[2 + kTrajMaxObs];
@@ -273,25 +277,27 @@ __global__ void __launch_bounds__(kTrajMaxWarps * 32, 1) traj_resident_kernel(Tr
                 const int slot = 32 * s + lane;
                 const int r = M.rid[slot];
                 const int2 sd = M.sd[s];
-                const uint16_t* e = M.ent + sd.x + lane;
+                // a lane's entries 2j and 2j+1 share one 32-bit word (sd.y is even)
+                const uint32_t* e2 = reinterpret_cast<const uint32_t*>(M.ent + sd.x) + lane;
                 float sx = 0.f, sy = 0.f, ux = 0.f, uy = 0.f;
-                int q = 0;
-                for (; q + 1 < sd.y; q += 2) {  // two independent gathers in flight
-                  const uint32_t ev = e[32 * q], fv = e[32 * q + 32];
-                  const float2 x = src[ev & 0x7fffu], y = src[fv & 0x7fffu];
-                  const float sg = __uint_as_float(0x3f800000u | ((ev & 0x8000u) << 16));
-                  const float tg = __uint_as_float(0x3f800000u | ((fv & 0x8000u) << 16));
-                  sx = fmaf(sg, x.x, sx);
-                  sy = fmaf(sg, x.y, sy);
-                  ux = fmaf(tg, y.x, ux);
-                  uy = fmaf(tg, y.y, uy);
-                }
-                if (q < sd.y) {
-                  const uint32_t ev = e[32 * q];
-                  const float2 x = src[ev & 0x7fffu];
-                  const float sg = __uint_as_float(0x3f800000u | ((ev & 0x8000u) << 16));
-                  sx = fmaf(sg, x.x, sx);
-                  sy = fmaf(sg, x.y, sy);
+                for (int q = 0; q < (sd.y >> 1); ++q) {  // two independent gathers in flight
+                  const uint32_t pr = e2[32 * q];
+                  const uint32_t ev = pr & 0xffffu, fv = pr >> 16;
+                  if (kSigned) {
+                    const float2 x = src[ev & 0x7fffu], y = src[fv & 0x7fffu];
+                    const float sg = __uint_as_float(0x3f800000u | ((ev & 0x8000u) << 16));
+                    const float tg = __uint_as_float(0x3f800000u | ((fv & 0x8000u) << 16));
+                    sx = fmaf(sg, x.x, sx);
+                    sy = fmaf(sg, x.y, sy);
+                    ux = fmaf(tg, y.x, ux);
+                    uy = fmaf(tg, y.y, uy);
+                  } else {  // every entry carries +c: plain sums
+                    const float2 x = src[ev], y = src[fv];
+                    sx += x.x;
+                    sy += x.y;
+                    ux += y.x;
+                    uy += y.y;
+                  }
                 }
                 sx += ux;
                 sy += uy;
@@ -331,9 +337,8 @@ __global__ void __launch_bounds__(kTrajMaxWarps * 32, 1) traj_resident_kernel(Tr
   if (tid == 0 && njumps) atomicAdd(A.jumps, njumps);
 }
 
-// The resident form of H_eff built on the host (rows sorted by their count of
-// off-diagonal entries, 32-row slices as wide as their longest row).  Returns
-// false when the operator is outside the form.
+// The resident form of H_eff built on the host (32-row slices as wide as their
+// longest row).  Returns false when the operator is outside the form.
 struct TrajHostForm {
   int n = 0, nsl = 0, nwarps = 0, ent_len = 0;
   std::vector<uint16_t> ent, rid;
@@ -342,9 +347,17 @@ struct TrajHostForm {
   std::vector<float2> dg;
   cplx coff{0.0, 0.0};
   double norm = 0.0;  // bound on ||H - mu||_2: max of the 1- and infinity-norms
+  bool any_neg = false;  // some entry carries -c
 };
 
-static bool traj_build_resident(qd_ham* H, TrajHostForm& F) {
+// Dynamic shared memory of the resident kernel for dim n, nsl slices and ent_len entries.
+static size_t traj_smem_bytes(int n, int nsl, int ent_len) {
+  const size_t tb_len = (size_t)(n + 2) / 2 * 2;
+  return 2 * tb_len * sizeof(float2) + (size_t)ent_len * 2 + (size_t)32 * nsl * 2 + (size_t)32 * nsl * 4 +
+         (size_t)(nsl + (nsl & 1)) * sizeof(int2) + (size_t)kTrajMaxWarps * kTrajRedStride * sizeof(float);
+}
+
+static bool traj_build_resident(qd_ham* H, TrajHostForm& F, size_t max_smem) {
   const int64_t n = H->dim;
   if (n < 1 || n > kTrajMaxDimRes || H->sec->nbits > 32) return false;
   std::vector<int64_t> rp(n + 1);
@@ -381,12 +394,25 @@ static bool traj_build_resident(qd_ham* H, TrajHostForm& F) {
       ++cnt[r];
     }
   }
-  // rows by decreasing entry count (stable), 32-row slices
+  // 32-row slices of the rows in their own order, each row's columns in gather order (by the
+  // highest bit in which the column's state differs from the row's, highest first): rows of one
+  // block of the high bits share their high-bit transitions, so lane l's k-th gather and lane
+  // l+1's hit neighbouring words (no bank conflict), and a row's own value sits at its lane.
+  // Where that layout's padding leaves no room, rows sorted by their entry count instead.
+  F.nsl = (int)((n + 31) / 32);
   std::vector<int> order(n);
   for (int64_t r = 0; r < n; ++r) order[r] = (int)r;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cnt[a] > cnt[b]; });
+  {
+    int64_t slots = 0;
+    for (int s = 0; s < F.nsl; ++s) {
+      int w = 0;
+      for (int l = 0; l < 32 && 32 * s + l < n; ++l) w = std::max(w, cnt[32 * s + l]);
+      slots += 32 * ((w + 1) & ~1);
+    }
+    if (traj_smem_bytes((int)n, F.nsl, (int)((slots + 7) / 8 * 8)) > max_smem)
+      std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cnt[a] > cnt[b]; });
+  }
   F.n = (int)n;
-  F.nsl = (int)((n + 31) / 32);
   F.nwarps = (F.nsl + kTrajRpt - 1) / kTrajRpt;
   F.rid.assign((size_t)32 * F.nsl, (uint16_t)n);
   F.st.assign((size_t)32 * F.nsl, 0u);
@@ -403,7 +429,9 @@ static bool traj_build_resident(qd_ham* H, TrajHostForm& F) {
   const cplx mu{0.5 * (rmin + rmax), 0.5 * (imin + imax)};
   int off = 0;
   for (int s = 0; s < F.nsl; ++s) {
-    const int w = cnt[order[32 * s]];
+    int w = 0;
+    for (int l = 0; l < 32 && 32 * s + l < n; ++l) w = std::max(w, cnt[order[32 * s + l]]);
+    w = (w + 1) & ~1;  // entries in pairs per lane
     F.sdesc[s] = make_int2(off, w);
     off += 32 * w;
   }
@@ -421,15 +449,23 @@ static bool traj_build_resident(qd_ham* H, TrajHostForm& F) {
       F.st[slot] = (uint32_t)basis[r];
       const double dre = d[r].re - mu.re, dim_ = d[r].im - mu.im;
       F.dg[slot] = make_float2((float)dre, (float)dim_);
-      int q = 0;
+      std::vector<std::pair<int, uint16_t>> row;  // (gather key, entry)
       for (int64_t k = rp[r]; k < rp[r + 1]; ++k) {
         const cplx a = v[k];
         if (ci[k] == r || (a.re == 0.0 && a.im == 0.0)) continue;
         const bool neg = !(a.re == c.re && a.im == c.im);
-        F.ent[F.sdesc[s].x + 32 * q + l] = (uint16_t)(ci[k] | (neg ? 0x8000 : 0));
+        const uint64_t dif = basis[r] ^ basis[ci[k]];
+        const int key = dif ? 63 - __builtin_clzll(dif) : -1;
+        row.emplace_back(key, (uint16_t)(ci[k] | (neg ? 0x8000 : 0)));
         colsum[ci[k]] += cabs;
-        ++q;
       }
+      std::stable_sort(row.begin(), row.end(),
+                       [](const std::pair<int, uint16_t>& x, const std::pair<int, uint16_t>& y) {
+                         return x.first > y.first;
+                       });
+      for (size_t q = 0; q < row.size(); ++q)
+        F.ent[F.sdesc[s].x + 64 * (q >> 1) + 2 * l + (q & 1)] = row[q].second;
+      for (const auto& e : row) F.any_neg |= (e.second & 0x8000) != 0;
       const double dd = std::hypot(dre, dim_);
       rowmax = std::max(rowmax, dd + cnt[r] * cabs);
       colsum[r] += dd;
@@ -627,7 +663,10 @@ void traj_run(qd_ham* H, const qd_traj_desc& d, const double* psi0_host, double*
   int64_t tot = 0;
 
   TrajHostForm F;
-  const bool resident = !traj_force_fallback() && traj_build_resident(H, F);
+  int maxsm = 0;
+  QD_CUDA(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+  const size_t smem_cap = (size_t)std::max(maxsm - 1024, 0);
+  const bool resident = !traj_force_fallback() && traj_build_resident(H, F, smem_cap);
   if (path) {
     path[0] = resident ? 0 : 1;
     path[1] = d.m - 1;
@@ -678,20 +717,17 @@ void traj_run(qd_ham* H, const qd_traj_desc& d, const double* psi0_host, double*
     A.psi0 = p0.p;
     A.obs = obs.p;
     A.jumps = jumps_dev.p;
-    const size_t smem = (size_t)2 * A.tb_len * sizeof(float2) + (size_t)A.ent_len * 2 + (size_t)32 * F.nsl * 2 +
-                        (size_t)32 * F.nsl * 4 + (size_t)(F.nsl + (F.nsl & 1)) * sizeof(int2) +
-                        (size_t)kTrajMaxWarps * kTrajRedStride * sizeof(float);
-    int maxsm = 0;
-    QD_CUDA(cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
-    if (smem + 1024 <= (size_t)maxsm) {
-      QD_CUDA(cudaFuncSetAttribute(traj_resident_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const size_t smem = traj_smem_bytes(F.n, F.nsl, A.ent_len);
+    if (smem <= smem_cap) {
+      auto kern = F.any_neg ? traj_resident_kernel<true> : traj_resident_kernel<false>;
+      QD_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       const int threads = 32 * F.nwarps;
       int occ = 0;
-      QD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, traj_resident_kernel, threads, smem));
+      QD_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, threads, smem));
       QD_REQUIRE(occ >= 1, QD_ERR_UNSUPPORTED, "trajectory kernel does not fit an SM");
       const int grid = (int)std::min<int64_t>(d.ntraj, (int64_t)occ * ctx->num_sms);
       QD_CUDA(cudaEventRecord(e1, ctx->stream));
-      traj_resident_kernel<<<grid, threads, smem, ctx->stream>>>(A);
+      kern<<<grid, threads, smem, ctx->stream>>>(A);
       QD_CHECK_LAUNCH();
       QD_LAUNCHED(ctx);
       unsigned long long j = 0;
