@@ -727,6 +727,7 @@ def main():
     ap.add_argument("--product", type=int, default=None, metavar="KERNEL",
                     help="product kernel of the Lanczos solves (qd_ham_set_spmv_kernel code; default: the engine's)")
     ap.add_argument("--serve-only", action="store_true", help="only run the serving mix")
+    ap.add_argument("--xy-only", action="store_true", help="only run the XY chain's Lanczos leg")
     ap.add_argument("--batch-only", type=int, default=None, metavar="N",
                     help="only run the batched disorder sweep with N instances")
     ap.add_argument("--batch-L", type=int, default=None, metavar="L",
@@ -742,6 +743,10 @@ def main():
         return spmv_only(args, local)
     if args.serve_only:
         print(json.dumps(serving_mix(args.serve_requests)))
+        return 0
+    if args.xy_only:
+        import qudrip_gb300 as q
+        print(json.dumps(xy_leg(q.Context(local))))
         return 0
     if args.traj_only is not None:
         import qudrip_gb300 as q

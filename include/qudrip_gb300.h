@@ -329,7 +329,8 @@ qd_status qd_arnoldi_extend(qd_ham *ham, qd_state *psi, int t, const qd_lanczos_
 /* reorthogonalisation pass per step, a device tridiagonal solve and one  */
 /* FP64 Rayleigh-quotient refinement.  out: 8 doubles per instance --     */
 /* lowest Krylov eigenvalue, refined energy, psi^T psi, act_dim,          */
-/* breakdown flag, 3 reserved.                                           */
+/* breakdown flag, the instance's start and end on the device clock    */
+/* (%globaltimer, ns), and the number of CTAs that computed it.         */
 /* ------------------------------------------------------------------ */
 qd_status qd_batch_lanczos(qd_ctx *ctx, int ninst, qd_ham *const *hams,
                            const double *const *v0s, int steps, double *out);

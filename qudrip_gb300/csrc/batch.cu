@@ -66,6 +66,13 @@ struct BlockScratch {
   int idx;
 };
 
+// The device's nanosecond clock (the instance schedule in out[5], out[6]).
+__device__ __forceinline__ unsigned long long batch_clock_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 // FP64 sum over the block of per-thread values; every thread gets the result.
 __device__ double block_sum_all(double v, BlockScratch& S) {
   v = warp_sum(v);
@@ -274,6 +281,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const B
     inst_sync<C>();
     if (idx >= ninst) return;  // the same index in every CTA of the cluster
     const BatchInst I = list[idx];
+    const unsigned long long t_start = batch_clock_ns();
     const int64_t n = I.dim;
     // this CTA's rows: a slice of 32-element multiples (the whole vector for C == 1)
     const int64_t per = ((n + C - 1) / C + 31) / 32 * 32;
@@ -462,6 +470,9 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const B
     if (rank == 0 && threadIdx.x == 0) {
       I.out[1] = num / den;
       I.out[2] = den;
+      I.out[5] = (double)t_start;
+      I.out[6] = (double)batch_clock_ns();
+      I.out[7] = (double)C;
     }
     inst_sync<C>();
   }

@@ -26,6 +26,7 @@
 // every row that its columns are exactly the stored ones.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -156,6 +157,53 @@ __global__ void fx_block_check_kernel(int64_t n, BlockRows B, const int32_t* row
         if (cols[q] == cols[a]) ok = false;
       bool found = false;
       for (int k = b; k < e && !found; ++k) found = colidx[k] == cols[a];
+      if (!found) ok = false;
+    }
+    if (!ok) atomicOr(bad, 1);
+  }
+}
+
+// Without stored columns (the matrix-free form): every row's block-form columns hold exactly the
+// states the operator's transitions reach from the row's state, each once.
+__global__ void fx_block_check_states_kernel(int64_t n, BlockRows B, const uint32_t* trans, int ntrans, int* bad) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const uint32_t s = B.state[r];
+    const uint32_t lmask = (1u << B.lowbits) - 1u;
+    const uint32_t h = s >> B.lowbits, l = s & lmask;
+    const int base = B.off[h];
+    const int i = (int)r - base;
+    int cols[64];
+    int cnt = 0;
+    bool ok = base >= 0 && i >= 0;
+    for (int j = 0; j < B.ldeg[l] && ok; ++j) {
+      if (cnt == 64) ok = false;
+      else cols[cnt++] = base + B.ladj[(size_t)l * B.lstride + j];
+    }
+    for (int j = 0; j < B.hdeg[h] && ok; ++j) {
+      if (cnt == 64) ok = false;
+      else cols[cnt++] = B.hadj[(size_t)h * B.hstride + j] + i;
+    }
+    for (int t = 0; t < B.ncross && ok; ++t) {
+      if ((s & B.cross[3 * t]) != B.cross[3 * t + 1]) continue;
+      const uint32_t c = s ^ B.cross[3 * t + 2];
+      const int ob = B.off[c >> B.lowbits];
+      if (cnt == 64 || ob < 0) ok = false;
+      else cols[cnt++] = ob + B.rank_low[c & lmask];
+    }
+    int want = 0;
+    for (int t = 0; t < ntrans; ++t) want += ((s & trans[3 * t]) == trans[3 * t + 1]) ? 1 : 0;
+    if (ok && cnt != want) ok = false;
+    for (int a = 0; a < cnt && ok; ++a) {
+      if (cols[a] < 0 || cols[a] >= n || cols[a] == (int)r) {
+        ok = false;
+        break;
+      }
+      for (int q = 0; q < a && ok; ++q)
+        if (cols[q] == cols[a]) ok = false;
+      const uint32_t sc = B.state[cols[a]];
+      bool found = false;
+      for (int t = 0; t < ntrans && !found; ++t)
+        found = (s & trans[3 * t]) == trans[3 * t + 1] && (s ^ trans[3 * t + 2]) == sc;
       if (!found) ok = false;
     }
     if (!ok) atomicOr(bad, 1);
@@ -317,7 +365,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) lz_fx_blkstep_kerne
     for (int r = gr.x + (int)threadIdx.x; r < gr.y; r += blockDim.x) {
       const __int128 s = B.row_sum_staged(r, xs, gr.x);
       const double xr = __ldcs(a.x + r);
-      const double w = sc * fma(a.cF, (double)s, __ldcs(a.diag + r) * xr);
+      const double w = sc * fma(a.cF, (double)s, a.diag ? __ldcs(a.diag + r) * xr : 0.0);
       wst[r - crow0] = w;
       acc.b = fma(xr, w, acc.b);
       if (kHas2) {
@@ -411,7 +459,7 @@ static void drop_block(FxForm& f) {
 
 // The tables of the block form for the transitions of value c; false when the
 // sector or the terms do not give this form.
-static bool make_block(qd_ham* H, FxForm& f) {
+static bool make_block(qd_ham* H, FxForm& f, std::vector<uint32_t>* trans_out = nullptr) {
   const SectorView& V = H->sec->view;
   if (!H->from_terms || V.rank_kind != 1 || V.nbits > 32 || H->dim >= (1ll << 31)) return false;
   int lowbits = 0;
@@ -421,7 +469,12 @@ static bool make_block(qd_ham* H, FxForm& f) {
   if (V.nfields == 1) {
     const Field& F = V.fields[0];
     if (F.is_free || F.lo != 0 || F.width != nbits) return false;
-    lowbits = nbits / 2;
+    // a short low half: a block's own values span a few cache lines, so a warp's low-half gathers
+    // touch few lines; the long high half's targets are coalesced runs.  QD_FX_BLOCK_LOW overrides.
+    lowbits = std::min(nbits / 2, 8);
+    const char* el = std::getenv("QD_FX_BLOCK_LOW");
+    if (el) lowbits = std::atoi(el);
+    lowbits = std::max(lowbits, nbits - kBlkMaxBits);
     fmask[0] = (nbits >= 32) ? 0xffffffffu : ((1u << nbits) - 1u);
     fk[0] = F.k;
   } else if (V.nfields == 2) {
@@ -469,6 +522,9 @@ static bool make_block(qd_ham* H, FxForm& f) {
     else cross.push_back(t);
   }
   if ((int)cross.size() > kBlkMaxCross || (low.empty() && high.empty() && cross.empty())) return false;
+  if (trans_out)
+    for (const std::vector<Tr>* L : {&low, &high, &cross})
+      for (const Tr& t : *L) trans_out->insert(trans_out->end(), {t.sup, t.outb, t.flip});
   // ranks of the low parts, blocks of the high parts
   const uint32_t nl = 1u << lowbits, nh = 1u << highbits;
   std::vector<uint16_t> rank_low(nl);
@@ -564,6 +620,11 @@ static bool make_block(qd_ham* H, FxForm& f) {
 }
 
 static bool make_block_part(Ctx* ctx, const qd_ham* H, FxForm& f);
+static bool block_staged() {
+  const char* e = std::getenv("QD_FX_BLOCK_STAGED");
+  return e && std::strcmp(e, "1") == 0;
+}
+
 
 bool ham_build_fx_block(qd_ham* H) {
   FxForm& f = *H->fx;
@@ -589,7 +650,40 @@ bool ham_build_fx_block(qd_ham* H) {
     return false;
   }
   f.blk_state = 1;
-  make_block_part(ctx, H, f);  // the staged step's partition, before any stream capture uses it
+  if (block_staged()) make_block_part(ctx, H, f);  // the staged step's partition, before any stream capture
+  return true;
+}
+
+// The block layout on the form built from the terms alone (the matrix-free Lanczos path), checked
+// against the transitions' target states (there are no stored columns).
+bool ham_build_mf_fx_block(qd_ham* H) {
+  FxForm& f = *H->mfx;
+  if (f.blk_state != 0) return f.blk_state > 0;
+  f.blk_state = -1;
+  std::vector<uint32_t> trans;
+  if (!make_block(H, f, &trans) || trans.empty()) {
+    drop_block(f);
+    return false;
+  }
+  Ctx* ctx = H->ctx;
+  const int64_t n = H->dim;
+  DBuf<uint32_t> dtr(trans.size());
+  DBuf<int> bad(1);
+  QD_CUDA(cudaMemcpyAsync(dtr.p, trans.data(), trans.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+  QD_CUDA(cudaMemsetAsync(bad.p, 0, sizeof(int), ctx->stream));
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)ctx->num_sms * 8));
+  fx_block_check_states_kernel<<<g, 256, 0, ctx->stream>>>(n, block_rows(f, nullptr), dtr.p, (int)(trans.size() / 3),
+                                                          bad.p);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  int b = 1;
+  QD_CUDA(cudaMemcpyAsync(&b, bad.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (b) {
+    drop_block(f);
+    return false;
+  }
+  f.blk_state = 1;
   return true;
 }
 
@@ -685,8 +779,12 @@ static bool make_block_part(Ctx* ctx, const qd_ham* H, FxForm& f) {
   return false;
 }
 
-bool launch_fx_block_step(Ctx* ctx, const qd_ham* H, const FxForm& f, FxStepArgs a) {
+// The one-launch step of the block form: by default the grid, row order and reduction tree of
+// code 120's step (lz_fx_step_kernel), bit-identical to it; QD_FX_BLOCK_STAGED=1 runs the staged
+// step above instead (groups of whole blocks copied into shared memory).
+bool launch_fx_block_step(Ctx* ctx, const qd_ham* H, const FxForm& f, FxStepArgs a, int grid) {
   (void)H;
+  if (!block_staged()) return fx_step_launch(ctx, block_rows(f, a.X), a, grid, 0);
   if (f.blk_part_state <= 0) return false;  // no partition fits: the two-launch step
   BlkPart P;
   P.groups = f.blk_groups.p;

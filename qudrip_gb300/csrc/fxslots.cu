@@ -14,6 +14,7 @@
 // bound by integer issue where code 120 is bound by gather latency.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <vector>
@@ -642,6 +643,10 @@ bool ham_build_mf_fx(qd_ham* H) {
   f->slots_state = 1;
   H->mfx = std::move(f);
   H->mfx_state = 1;
+  // the block layout, where the sector gives it, replaces the slots (faster one-launch step, the
+  // same bits); QD_MF_BLOCK=0 keeps the slots
+  const char* e = std::getenv("QD_MF_BLOCK");
+  if (!(e && std::strcmp(e, "0") == 0) && ham_build_mf_fx_block(H)) H->mfx->use_blk = true;
   return true;
 }
 

@@ -29,7 +29,7 @@ constexpr unsigned kStepSpinLimit = 1u << 22;
 
 struct FxStepArgs {
   int64_t n;
-  const double* diag;
+  const double* diag;   // null: every diagonal entry is 0
   const double* x;      // V1, unnormalised (s1 = 1 / ||V1||)
   const __int128* X;    // fixed-point copy of V1
   const double* V2;     // V2 (kHas2), unnormalised (s2 = 1 / ||V2||)
@@ -89,7 +89,8 @@ __global__ void __launch_bounds__(256, 6) lz_fx_step_kernel(Src src, FxStepArgs 
   for (int r = (int)(blockIdx.x * blockDim.x + threadIdx.x); r < n; r += stride, wp += 256) {
     const __int128 s = rows.row_sum(r);
     const double xr = __ldcs(a.x + r);
-    const double w = sc * fma(a.cF, (double)s, __ldcs(a.diag + r) * xr);
+    const double dx = a.diag ? __ldcs(a.diag + r) * xr : 0.0;
+    const double w = sc * fma(a.cF, (double)s, dx);
     *wp = w;
     acc.b = fma(xr, w, acc.b);
     if (kHas2) {

@@ -34,7 +34,8 @@ __global__ void fx_probe_kernel(int64_t n, const int64_t* rowptr, const int32_t*
 // Per row: off-diagonal count, diagonal value, |row| sum; flags any
 // off-diagonal value other than c.
 __global__ void fx_count_kernel(int64_t n, const int64_t* rowptr, const int32_t* colidx, const double* vals, double c,
-                                int64_t* counts, double* diag, int* mismatch, unsigned long long* rowmax) {
+                                int64_t* counts, double* diag, int* mismatch, unsigned long long* rowmax,
+                                int* diag_nonzero) {
   for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
     int64_t cnt = 0;
     double d = 0.0, abs_sum = 0.0;
@@ -51,6 +52,7 @@ __global__ void fx_count_kernel(int64_t n, const int64_t* rowptr, const int32_t*
     abs_sum += fabs(d);
     counts[r] = cnt;
     diag[r] = d;
+    if (d != 0.0) *diag_nonzero = 1;
     atomicMax(rowmax, (unsigned long long)__double_as_longlong(abs_sum));
   }
 }
@@ -109,6 +111,8 @@ bool ham_build_fx(qd_ham* H) {
   QD_CUDA(cudaMemsetAsync(cand.p, 0xff, sizeof(unsigned long long), ctx->stream));
   QD_CUDA(cudaMemsetAsync(cand.p + 1, 0, sizeof(unsigned long long), ctx->stream));
   QD_CUDA(cudaMemsetAsync(mismatch.p, 0, sizeof(int), ctx->stream));
+  DBuf<int> dnz(1);
+  QD_CUDA(cudaMemsetAsync(dnz.p, 0, sizeof(int), ctx->stream));
   fx_probe_kernel<<<fx_grid(ctx, n), 256, 0, ctx->stream>>>(n, H->rowptr.p, H->colidx.p, H->vals_r.p, cand.p);
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
@@ -121,7 +125,7 @@ bool ham_build_fx(qd_ham* H) {
   DBuf<int64_t> counts(n + 1), off(n + 1);
   fx->diag.alloc(n);
   fx_count_kernel<<<fx_grid(ctx, n), 256, 0, ctx->stream>>>(n, H->rowptr.p, H->colidx.p, H->vals_r.p, c, counts.p,
-                                                            fx->diag.p, mismatch.p, cand.p + 1);
+                                                            fx->diag.p, mismatch.p, cand.p + 1, dnz.p);
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
   QD_CUDA(cudaMemsetAsync(counts.p + n, 0, sizeof(int64_t), ctx->stream));
@@ -132,7 +136,10 @@ bool ham_build_fx(qd_ham* H) {
   QD_CUDA(cudaMemcpyAsync(&mm, mismatch.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   QD_CUDA(cudaMemcpyAsync(&rbits, cand.p + 1, 8, cudaMemcpyDeviceToHost, ctx->stream));
   QD_CUDA(cudaMemcpyAsync(&total, off.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->stream));
+  int diag_nz = 1;
+  QD_CUDA(cudaMemcpyAsync(&diag_nz, dnz.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  fx->diag_zero = diag_nz == 0;
   if (mm || total >= (1ll << 31) || H->max_row_nnz > 128) return false;
   double rowmax = 0.0;
   std::memcpy(&rowmax, &rbits, 8);
@@ -357,14 +364,14 @@ struct SellRows {
 
 bool launch_fx_step(Ctx* ctx, const qd_ham* H, const FxForm& f, FxStepArgs a) {
   a.n = H->dim;
-  a.diag = f.diag.p;
+  a.diag = f.diag_zero ? nullptr : f.diag.p;  // no diagonal (e.g. the XY chain): nothing to read
   a.cF = std::ldexp(f.c, -f.F);
   a.F = f.F;
   const int g = fx_dots_grid(ctx, H->dim);
   bool ok = false;
   if (g <= kMaxGrid) {
     if (f.blk_state > 0 && f.use_blk)
-      ok = launch_fx_block_step(ctx, H, f, a);
+      ok = launch_fx_block_step(ctx, H, f, a, g);
     else if (f.slots_state > 0 && f.use_slots)
       ok = launch_fx_slots_step(ctx, H, f, a, g);
     else

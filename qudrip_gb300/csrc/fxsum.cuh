@@ -70,6 +70,7 @@ struct FxForm {
   DBuf<int32_t> colidx;  // slice layout and of the slot check; columns in gather order (fx_fill_kernel)
   DBuf<double> diag;     // d_r (0 where the CSR has no diagonal entry)
   double c = 0.0;        // the common off-diagonal value
+  bool diag_zero = false;  // every diagonal entry is 0 (the one-launch step reads no diagonal)
   int F = 0;             // fixed-point scale 2^F
   int64_t nnz = 0;
   // columns on the fly (code 121)

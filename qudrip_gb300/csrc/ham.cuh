@@ -129,6 +129,7 @@ void compile_terms(const qd_ham* H, std::vector<MfEntry>& off, std::vector<MfEnt
 void build_tables(const qd_sector* S, MfRank& rk, std::vector<int64_t>& tab);
 bool ham_build_fx_slots(qd_ham* H);
 bool ham_build_fx_block(qd_ham* H);
+bool ham_build_mf_fx_block(qd_ham* H);
 bool ham_build_mf_fx(qd_ham* H);
 bool ham_lower_pull(qd_ham* H);
 void mf_apply_c(qd_ham* H, const cplx* x, cplx* y);

@@ -157,7 +157,7 @@ struct FxStepArgs;
 // (fxstep.cuh); false when it does not fit on the device at once.
 bool launch_fx_step(Ctx* ctx, const qd_ham* H, const FxForm& f, FxStepArgs a);
 bool launch_fx_slots_step(Ctx* ctx, const qd_ham* H, const FxForm& f, const FxStepArgs& a, int grid);
-bool launch_fx_block_step(Ctx* ctx, const qd_ham* H, const FxForm& f, FxStepArgs a);
+bool launch_fx_block_step(Ctx* ctx, const qd_ham* H, const FxForm& f, FxStepArgs a, int grid);
 void launch_fx_block_dots(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x, const __int128* X,
                           const double* V2, double* y, const double* s1, const double* s2, const int* stop, int step,
                           double* beta, double* alpha, Tri<double>* dots, GridRed<Tri<double>> red, int grid);

@@ -280,6 +280,7 @@ __global__ void __launch_bounds__(kTrajMaxWarps * 32, 1) traj_resident_kernel(Tr
                 // a lane's entries 2j and 2j+1 share one 32-bit word (sd.y is even)
                 const uint32_t* e2 = reinterpret_cast<const uint32_t*>(M.ent + sd.x) + lane;
                 float sx = 0.f, sy = 0.f, ux = 0.f, uy = 0.f;
+#pragma unroll 2
                 for (int q = 0; q < (sd.y >> 1); ++q) {  // two independent gathers in flight
                   const uint32_t pr = e2[32 * q];
                   const uint32_t ev = pr & 0xffffu, fv = pr >> 16;

@@ -485,7 +485,8 @@ def batch_lanczos(hams, v0s, steps: int, ctx: Optional[Context] = None) -> np.nd
     """Many ground states in one persistent launch (mixed precision, FP64 refinement).
 
     Returns an (ninst, 8) array: lowest Krylov eigenvalue, refined FP64 energy,
-    psi^T psi, act_dim, breakdown flag, 3 reserved.
+    psi^T psi, act_dim, breakdown flag, start and end of the instance on the device
+    clock (ns), CTAs that computed it.
     """
     n = len(hams)
     ctx = ctx or hams[0].ctx

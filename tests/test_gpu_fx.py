@@ -159,26 +159,32 @@ def test_columns_on_the_fly_timing_and_fallback(ctx):
 
 
 @pytest.mark.parametrize("name", sorted(CASES))
-def test_block_layout_step_matches_stored_columns(ctx, name):
+def test_block_layout_step_matches_stored_columns(ctx, name, monkeypatch):
     """Code 122: the block layout of the sector (rows grouped by the high part of their state; tables of
     the low and high parts' targets, checked against the stored columns at build).  Its one-launch step
-    stages each group of whole blocks in shared memory with one bulk copy; every row's product carries
-    code 120's bits, the inner products add in another order, so the solve agrees with code 120's to
-    rounding, and its two-launch step (served requests) is bit-identical to code 120's."""
+    runs on code 120's grid, row order and reduction tree, so the solve is bit-identical; the staged
+    variant (QD_FX_BLOCK_STAGED=1: each group of whole blocks copied into shared memory by one bulk
+    copy) adds the inner products in another order and agrees to rounding."""
     spec, ham = CASES[name]()
+    v0 = q.start_vector(q.Sector(spec.index, spec.constraints).dim, 17)
     sec, H = gpu_objects(spec, ham)
-    v0 = q.start_vector(sec.dim, 17)
     r120, psi120 = solve(sec, H, v0, 60, kernel=A.QD_SPMV_FX)
     r122, psi122 = solve(sec, H, v0, 60, kernel=A.QD_SPMV_FX_BLOCK)
     info = A.qd_ham_info()
     A.call("qd_ham_get_info", H.handle, C.byref(info))
     assert info.product_kernel == A.QD_SPMV_FX_BLOCK and info.step_launches == 1
-    assert r122.act_dim == r120.act_dim and r122.matvecs == r120.matvecs
-    assert abs(r122.ritz_value - r120.ritz_value) <= 1e-12 * abs(r120.ritz_value)
-    ov = abs(np.vdot(psi122, psi120)) / (np.linalg.norm(psi122) * np.linalg.norm(psi120))
+    assert r122.ritz_value == r120.ritz_value and np.array_equal(psi122, psi120)
+    monkeypatch.setenv("QD_FX_BLOCK_STAGED", "1")
+    sec2, H2 = gpu_objects(spec, ham)
+    r_st, psi_st = solve(sec2, H2, v0, 60, kernel=A.QD_SPMV_FX_BLOCK)
+    A.call("qd_ham_get_info", H2.handle, C.byref(info))
+    assert info.step_launches == 1
+    assert r_st.act_dim == r120.act_dim and r_st.matvecs == r120.matvecs
+    assert abs(r_st.ritz_value - r120.ritz_value) <= 1e-12 * abs(r120.ritz_value)
+    ov = abs(np.vdot(psi_st, psi120)) / (np.linalg.norm(psi_st) * np.linalg.norm(psi120))
     assert ov >= 1 - 1e-10
     o = O.Ham(O.Sector(spec), ham).lanczos_ground(v0, 60)
-    assert abs(r122.ritz_value - o["ritz"]) <= 1e-10 * abs(o["ritz"])
+    assert abs(r_st.ritz_value - o["ritz"]) <= 1e-10 * abs(o["ritz"])
 
 
 def test_block_layout_two_launch_step_bit_identical(ctx, monkeypatch):

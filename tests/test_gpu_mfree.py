@@ -111,9 +111,11 @@ def _mf_bytes(H):
 
 @pytest.mark.parametrize("case", ["xxz16", "xy14_open", "two_species"])
 def test_matrix_free_uniform_form_bit_identical_to_csr(ctx, case):
-    """Uniform couplings on the matrix-free path take the slot form built from the terms alone (no stored
-    matrix: offsets checked on the host against whole-field ranks, rows checked on the device); its
-    recurrence is bit-identical to the stored-matrix forms (codes 120 and 121)."""
+    """Uniform couplings on the matrix-free path take the fixed-point form built from the terms alone (no
+    stored matrix): the block layout of the sector (its tables checked on the device against the
+    transitions' target states), else the slots (offsets checked on the host against whole-field ranks);
+    its recurrence is bit-identical to the stored-matrix forms (codes 120 and 121), and so is the slot
+    form's (QD_MF_BLOCK=0)."""
     from test_gpu_fx import two_species_xy
     spec, ham = {"xxz16": lambda: chains.xxz_chain(16, 1.0, 0.8, periodic=True,
                                                    fields=np.linspace(-1, 1, 16)),
@@ -130,6 +132,14 @@ def test_matrix_free_uniform_form_bit_identical_to_csr(ctx, case):
     r_121, p_121 = _lanczos(sec, H, v0, 80, kernel=A.QD_SPMV_FX_SLOTS)
     assert r_mf.ritz_value == r_120.ritz_value == r_121.ritz_value
     assert np.array_equal(p_mf, p_120) and np.array_equal(p_mf, p_121)
+    import os
+    os.environ["QD_MF_BLOCK"] = "0"
+    try:
+        sec2, H2 = gpu_objects(spec, ham)
+        r_sl, p_sl = _lanczos(sec2, H2, v0, 80, spmv=A.QD_SPMV_MATRIX_FREE)
+    finally:
+        del os.environ["QD_MF_BLOCK"]
+    assert r_sl.ritz_value == r_mf.ritz_value and np.array_equal(p_sl, p_mf)
     o = O.Ham(O.Sector(spec), ham).lanczos_ground(v0, 80)
     assert abs(r_mf.ritz_value - o["ritz"]) <= 1e-10 * abs(o["ritz"])
 
