@@ -50,18 +50,25 @@ namespace qd {
 constexpr int kBatchThreads = 512;  // two CTAs per SM
 constexpr int kBatchMaxSteps = 256;
 constexpr int kChunk = 64;  // FP32 partial sums cover at most this many elements
-constexpr int kClusterCtasMax = 8;  // CTAs of a cluster that shares one large instance: 8, 4 or 2 per call
 constexpr int64_t kClusterMinDim = 32768;
 
+constexpr int kWTile = 4096;  // elements of w staged in shared memory for the Gram-Schmidt coefficients
+
 struct BlockScratch {
+  float wt[kWTile];
   double red[kBatchThreads / 32];
+  double red3[kBatchThreads / 32][3];
   double bcast;
+  double bcast3[3];
   double xp[2], bc[2];                    // this CTA's partial of a cluster sum, and the sum
+  double xp3[2][3], bc3[2][3];
   double hp[2][kBatchMaxSteps + 2];       // this CTA's partials of the Gram-Schmidt coefficients
   double alpha[kBatchMaxSteps + 2];
   double beta[kBatchMaxSteps + 2];
   double y[kBatchMaxSteps + 2];
   double h[kBatchMaxSteps + 2];
+  double c[kBatchMaxSteps + 2];           // update coefficients of the stored vectors
+  double scl[kBatchMaxSteps + 2];         // basis vector j is scl[j] * V[j] (V stored unnormalised)
   int stop;
   int idx;
 };
@@ -87,6 +94,30 @@ __device__ double block_sum_all(double v, BlockScratch& S) {
   }
   __syncthreads();
   return S.bcast;
+}
+
+// The same for three values at once.
+__device__ void block_sum_all3(double (&v)[3], BlockScratch& S) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 3; ++q) v[q] = warp_sum(v[q]);
+  __syncthreads();
+  if (lane == 0) {
+#pragma unroll
+    for (int q = 0; q < 3; ++q) S.red3[warp][q] = v[q];
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+      double t = (lane < (int)(blockDim.x >> 5)) ? S.red3[lane][q] : 0.0;
+      t = warp_sum(t);
+      if (lane == 0) S.bcast3[q] = t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int q = 0; q < 3; ++q) v[q] = S.bcast3[q];
 }
 
 // <a, b> over [lo, hi) with FP32 products and partials over <= kChunk
@@ -118,45 +149,92 @@ __device__ double block_dot(const float* __restrict__ a, const float* __restrict
   return block_sum_all(dacc, S);
 }
 
-// w -= c * v on [lo, hi)
-__device__ void block_axpy(float* __restrict__ w, float c, const float* __restrict__ v, int64_t lo, int64_t hi) {
-  const int64_t q0 = lo >> 2, q1 = hi >> 2;
-  float4* w4 = reinterpret_cast<float4*>(w);
-  const float4* v4 = reinterpret_cast<const float4*>(v);
-#pragma unroll 4
-  for (int64_t i = q0 + threadIdx.x; i < q1; i += blockDim.x) {
-    float4 x = w4[i];
-    const float4 y = v4[i];
-    x.x = fmaf(-c, y.x, x.x);
-    x.y = fmaf(-c, y.y, x.y);
-    x.z = fmaf(-c, y.z, x.z);
-    x.w = fmaf(-c, y.w, x.w);
-    w4[i] = x;
+// y = H x on rows [lo, hi) (FP32 values, FP32 accumulation), one thread per
+// row, two rows per thread at a time (r and r + blockDim.x: two independent
+// chains of four gathers), each summed in its entry order.  x is a basis
+// vector written earlier in the same launch (by this CTA or, for a cluster, by
+// all of its CTAs), so it is read with ordinary loads, not the read-only path.
+__device__ __forceinline__ float row_f32(const BatchInst& I, const float* x, int64_t b, int64_t e) {
+  float acc = 0.f;
+  int64_t k = b;
+  for (; k + 4 <= e; k += 4) {
+    const int32_t c0 = I.colidx[k], c1 = I.colidx[k + 1], c2 = I.colidx[k + 2], c3 = I.colidx[k + 3];
+    const float v0 = I.vals_f[k], v1 = I.vals_f[k + 1], v2 = I.vals_f[k + 2], v3 = I.vals_f[k + 3];
+    const float x0 = x[c0], x1 = x[c1], x2 = x[c2], x3 = x[c3];
+    acc = fmaf(v0, x0, acc);
+    acc = fmaf(v1, x1, acc);
+    acc = fmaf(v2, x2, acc);
+    acc = fmaf(v3, x3, acc);
   }
-  for (int64_t i = (q1 << 2) + threadIdx.x; i < hi; i += blockDim.x) w[i] = fmaf(-c, v[i], w[i]);
+  for (; k < e; ++k) acc = fmaf(I.vals_f[k], x[I.colidx[k]], acc);
+  return acc;
 }
 
-// y = H x on rows [lo, hi) (FP32 values, FP32 accumulation), one thread per
-// row.  x is a basis vector written earlier in the same launch (by this CTA
-// or, for a cluster, by all of its CTAs), so it is read with ordinary loads,
-// not the read-only path.
-__device__ void block_spmv_f32(const BatchInst& I, const float* x, float* __restrict__ y, int64_t lo, int64_t hi) {
-  for (int64_t r = lo + threadIdx.x; r < hi; r += blockDim.x) {
-    const int64_t b = I.rowptr[r], e = I.rowptr[r + 1];
-    float acc = 0.f;
-    int64_t k = b;
-    for (; k + 4 <= e; k += 4) {
-      const int32_t c0 = I.colidx[k], c1 = I.colidx[k + 1], c2 = I.colidx[k + 2], c3 = I.colidx[k + 3];
-      const float v0 = I.vals_f[k], v1 = I.vals_f[k + 1], v2 = I.vals_f[k + 2], v3 = I.vals_f[k + 3];
-      const float x0 = x[c0], x1 = x[c1], x2 = x[c2], x3 = x[c3];
-      acc = fmaf(v0, x0, acc);
-      acc = fmaf(v1, x1, acc);
-      acc = fmaf(v2, x2, acc);
-      acc = fmaf(v3, x3, acc);
+// The product of the step and, row by row as it is formed, this thread's
+// shares of <V2, y>, <V1, y> and <V1, V2> (FP32 over at most kChunk rows, FP64
+// beyond; V2 null on the first step).
+struct ProdDots {
+  float fa = 0.f, fb = 0.f, fc = 0.f;
+  double da = 0.0, db = 0.0, dc = 0.0;
+  int cnt = 0;
+  __device__ __forceinline__ void add(const float* x, const float* v2, int64_t r, float yr) {
+    const float x1 = x[r];
+    fb = fmaf(x1, yr, fb);
+    if (v2) {
+      const float x2 = v2[r];
+      fa = fmaf(x2, yr, fa);
+      fc = fmaf(x1, x2, fc);
     }
-    for (; k < e; ++k) acc = fmaf(I.vals_f[k], x[I.colidx[k]], acc);
-    y[r] = acc;
+    if (++cnt == kChunk) flush();
   }
+  __device__ __forceinline__ void flush() {
+    da += (double)fa;
+    db += (double)fb;
+    dc += (double)fc;
+    fa = fb = fc = 0.f;
+    cnt = 0;
+  }
+};
+
+__device__ void block_spmv_f32(const BatchInst& I, const float* x, const float* v2, float* __restrict__ y, int64_t lo,
+                               int64_t hi, ProdDots& pd) {
+  const int64_t bs = blockDim.x;
+  int64_t r = lo + threadIdx.x;
+  for (; r + bs < hi; r += 2 * bs) {
+    const int64_t b0 = I.rowptr[r], e0 = I.rowptr[r + 1], b1 = I.rowptr[r + bs], e1 = I.rowptr[r + bs + 1];
+    // the two rows' groups of four interleaved: eight gathers in flight
+    float a0 = 0.f, a1 = 0.f;
+    int64_t k0 = b0, k1 = b1;
+    for (; k0 + 4 <= e0 && k1 + 4 <= e1; k0 += 4, k1 += 4) {
+      const int32_t c0 = I.colidx[k0], c1 = I.colidx[k0 + 1], c2 = I.colidx[k0 + 2], c3 = I.colidx[k0 + 3];
+      const int32_t d0 = I.colidx[k1], d1 = I.colidx[k1 + 1], d2 = I.colidx[k1 + 2], d3 = I.colidx[k1 + 3];
+      const float v0 = I.vals_f[k0], v1 = I.vals_f[k0 + 1], w2 = I.vals_f[k0 + 2], v3 = I.vals_f[k0 + 3];
+      const float u0 = I.vals_f[k1], u1 = I.vals_f[k1 + 1], u2 = I.vals_f[k1 + 2], u3 = I.vals_f[k1 + 3];
+      const float x0 = x[c0], x1 = x[c1], x2 = x[c2], x3 = x[c3];
+      const float z0 = x[d0], z1 = x[d1], z2 = x[d2], z3 = x[d3];
+      a0 = fmaf(v0, x0, a0);
+      a0 = fmaf(v1, x1, a0);
+      a0 = fmaf(w2, x2, a0);
+      a0 = fmaf(v3, x3, a0);
+      a1 = fmaf(u0, z0, a1);
+      a1 = fmaf(u1, z1, a1);
+      a1 = fmaf(u2, z2, a1);
+      a1 = fmaf(u3, z3, a1);
+    }
+    // the rest of each row, continuing its sum in entry order
+    for (; k0 < e0; ++k0) a0 = fmaf(I.vals_f[k0], x[I.colidx[k0]], a0);
+    for (; k1 < e1; ++k1) a1 = fmaf(I.vals_f[k1], x[I.colidx[k1]], a1);
+    y[r] = a0;
+    y[r + bs] = a1;
+    pd.add(x, v2, r, a0);
+    pd.add(x, v2, r + bs, a1);
+  }
+  if (r < hi) {
+    const float a0 = row_f32(I, x, I.rowptr[r], I.rowptr[r + 1]);
+    y[r] = a0;
+    pd.add(x, v2, r, a0);
+  }
+  pd.flush();
 }
 
 // ---------------------------------------------------------------- cluster sums
@@ -187,6 +265,28 @@ __device__ double inst_sum(double block_total, BlockScratch& S, int& buf) {
     const double t = S.bc[buf];
     buf ^= 1;
     return t;
+  }
+}
+
+// The instance totals of three block totals (one cluster barrier).
+template <int C>
+__device__ void inst_sum3(double (&v)[3], BlockScratch& S, int& buf) {
+  if constexpr (C > 1) {
+    cg::cluster_group cl = cg::this_cluster();
+    if (threadIdx.x == 0) {
+#pragma unroll
+      for (int q = 0; q < 3; ++q) S.xp3[buf][q] = v[q];
+    }
+    cl.sync();
+    if (threadIdx.x < 3) {
+      double t = 0.0;
+      for (int r = 0; r < C; ++r) t += cl.map_shared_rank(&S.xp3[buf][0], r)[threadIdx.x];
+      S.bc3[buf][threadIdx.x] = t;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 3; ++q) v[q] = S.bc3[buf][q];
+    buf ^= 1;
   }
 }
 
@@ -292,83 +392,136 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const B
     const double nrm0 = sqrt(inst_sum<C>(block_dot(I.v0, I.v0, lo, hi, S), S, buf));
     const float inv0 = (float)(1.0 / nrm0);
     for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) V[i] = I.v0[i] * inv0;
-    if (threadIdx.x == 0) S.stop = 0;
+    if (threadIdx.x == 0) {
+      S.stop = 0;
+      S.scl[0] = 1.0;
+    }
     inst_sync<C>();
     int act = I.steps;
+    // The basis is stored unnormalised: vector j is scl[j] V[j].  A step forms y = H V[k-1]
+    // with the three inner products of the reference's local orthogonalisation, folds
+    // u = y - c2 V[k-2] - c1 V[k-1] into the first read of the Gram-Schmidt pass, and
+    // writes the orthogonalised u, times a power of two near 1 / ||u||, to V[k] itself.
     for (int k = 1; k <= I.steps; ++k) {
       const float* v1 = V + (int64_t)(k - 1) * I.ld;
       const float* v2 = (k >= 2) ? V + (int64_t)(k - 2) * I.ld : nullptr;
-      block_spmv_f32(I, v1, w, lo, hi);
-      __syncthreads();
-      double bp = 0.0;
-      if (v2) {
-        bp = inst_sum<C>(block_dot(v2, w, lo, hi, S), S, buf);
-        block_axpy(w, (float)bp, v2, lo, hi);
-        __syncthreads();
-      }
-      const double al = inst_sum<C>(block_dot(v1, w, lo, hi, S), S, buf);
-      block_axpy(w, (float)al, v1, lo, hi);
-      __syncthreads();
-      // one full Gram-Schmidt pass against v_0 .. v_{k-1}: a warp per basis vector
+      const double s1 = S.scl[k - 1], s2 = (k >= 2) ? S.scl[k - 2] : 0.0;
+      ProdDots pd;
+      block_spmv_f32(I, v1, v2, w, lo, hi, pd);
+      double d3[3] = {pd.da, pd.db, pd.dc};
+      block_sum_all3(d3, S);
+      inst_sum3<C>(d3, S, buf);
+      // bp = <v2, w>, al = <v1, w - bp v2> in the true (normalised) vectors
+      const double bp = v2 ? s2 * s1 * d3[0] : 0.0;
+      const double al = s1 * (s1 * d3[1] - bp * s2 * d3[2]);
+      const float c2 = v2 ? (float)(bp * s2 / s1) : 0.f, c1 = (float)al;
+      // one full Gram-Schmidt pass against v_0 .. v_{k-1}
+      double nacc = 0.0;  // this thread's share of the stored V[k]'s squared norm
+      float tk = 1.f;     // the power of two V[k] is stored with
       {
-        const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
         const int64_t q0 = lo >> 2, q1 = hi >> 2;
-        const float4* w4 = reinterpret_cast<const float4*>(w);
         double* part = (C > 1) ? S.hp[hbuf] : S.h;
-        for (int j = warp; j < k; j += nw) {
-          const float* vj = V + (int64_t)j * I.ld;
-          const float4* vj4 = reinterpret_cast<const float4*>(vj);
-          double dacc = 0.0;
-          float acc = 0.f;
-          int cnt = 0;
-          int64_t i = q0 + lane;
-          for (; i + 96 < q1; i += 128) {  // four float4 pairs in flight per lane
-            const float4 x0 = vj4[i], y0 = w4[i], x1 = vj4[i + 32], y1 = w4[i + 32];
-            const float4 x2 = vj4[i + 64], y2 = w4[i + 64], x3 = vj4[i + 96], y3 = w4[i + 96];
-            acc = fmaf(x0.x, y0.x, acc);
-            acc = fmaf(x0.y, y0.y, acc);
-            acc = fmaf(x0.z, y0.z, acc);
-            acc = fmaf(x0.w, y0.w, acc);
-            acc = fmaf(x1.x, y1.x, acc);
-            acc = fmaf(x1.y, y1.y, acc);
-            acc = fmaf(x1.z, y1.z, acc);
-            acc = fmaf(x1.w, y1.w, acc);
-            acc = fmaf(x2.x, y2.x, acc);
-            acc = fmaf(x2.y, y2.y, acc);
-            acc = fmaf(x2.z, y2.z, acc);
-            acc = fmaf(x2.w, y2.w, acc);
-            acc = fmaf(x3.x, y3.x, acc);
-            acc = fmaf(x3.y, y3.y, acc);
-            acc = fmaf(x3.z, y3.z, acc);
-            acc = fmaf(x3.w, y3.w, acc);
-            cnt += 4;
-            if (cnt >= kChunk / 4) {
+        // g_j = <V_j, u>, j < k, and ||u||^2 in part[k]: u formed tile by tile into shared
+        // memory (and written back for the update), a warp per basis vector within a
+        // tile, eight float4 of V_j in flight per lane
+        {
+          const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+          for (int j = threadIdx.x; j <= k; j += blockDim.x) part[j] = 0.0;
+          double uacc = 0.0;
+          for (int64_t t0 = lo; t0 < hi; t0 += kWTile) {
+            const int tn = (int)std::min<int64_t>(hi - t0, kWTile);
+            const int nq = tn >> 2;  // t0 is a multiple of 32: float4-aligned
+            __syncthreads();  // the previous tile's readers are done (and part is zeroed)
+            float uf = 0.f;
+            for (int i = threadIdx.x; i < nq; i += blockDim.x) {
+              float4 u = reinterpret_cast<const float4*>(w + t0)[i];
+              const float4 p1 = reinterpret_cast<const float4*>(v1 + t0)[i];
+              if (v2) {
+                const float4 p2 = reinterpret_cast<const float4*>(v2 + t0)[i];
+                u.x = fmaf(-c2, p2.x, u.x);
+                u.y = fmaf(-c2, p2.y, u.y);
+                u.z = fmaf(-c2, p2.z, u.z);
+                u.w = fmaf(-c2, p2.w, u.w);
+              }
+              u.x = fmaf(-c1, p1.x, u.x);
+              u.y = fmaf(-c1, p1.y, u.y);
+              u.z = fmaf(-c1, p1.z, u.z);
+              u.w = fmaf(-c1, p1.w, u.w);
+              reinterpret_cast<float4*>(S.wt)[i] = u;
+              reinterpret_cast<float4*>(w + t0)[i] = u;
+              uf = fmaf(u.x, u.x, uf);
+              uf = fmaf(u.y, u.y, uf);
+              uf = fmaf(u.z, u.z, uf);
+              uf = fmaf(u.w, u.w, uf);
+            }
+            for (int i = (nq << 2) + threadIdx.x; i < tn; i += blockDim.x) {
+              float u = w[t0 + i];
+              if (v2) u = fmaf(-c2, v2[t0 + i], u);
+              u = fmaf(-c1, v1[t0 + i], u);
+              S.wt[i] = u;
+              w[t0 + i] = u;
+              uf = fmaf(u, u, uf);
+            }
+            uacc += (double)uf;  // at most kWTile / blockDim.x = 8 elements per thread per tile
+            __syncthreads();
+            const float4* ws4 = reinterpret_cast<const float4*>(S.wt);
+            for (int j = warp; j < k; j += nw) {
+              const float* vj = V + (int64_t)j * I.ld + t0;
+              const float4* vj4 = reinterpret_cast<const float4*>(vj);
+              double dacc = 0.0;
+              float acc = 0.f;
+              int i = lane;
+              for (; i + 224 < nq; i += 256) {  // 8 float4 per lane: 128 elements in two FP32 chunks
+                float4 x[8];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) x[q] = vj4[i + 32 * q];
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                  const float4 y = ws4[i + 32 * q];
+                  acc = fmaf(x[q].x, y.x, acc);
+                  acc = fmaf(x[q].y, y.y, acc);
+                  acc = fmaf(x[q].z, y.z, acc);
+                  acc = fmaf(x[q].w, y.w, acc);
+                  if (q == 3 || q == 7) {
+                    dacc += (double)acc;
+                    acc = 0.f;
+                  }
+                }
+              }
+              int cnt = 0;
+              for (; i < nq; i += 32) {
+                const float4 x = vj4[i], y = ws4[i];
+                acc = fmaf(x.x, y.x, acc);
+                acc = fmaf(x.y, y.y, acc);
+                acc = fmaf(x.z, y.z, acc);
+                acc = fmaf(x.w, y.w, acc);
+                if (++cnt == kChunk / 4) {
+                  dacc += (double)acc;
+                  acc = 0.f;
+                  cnt = 0;
+                }
+              }
+              for (int ii = (nq << 2) + lane; ii < tn; ii += 32) acc = fmaf(vj[ii], S.wt[ii], acc);
               dacc += (double)acc;
-              acc = 0.f;
-              cnt = 0;
+              dacc = warp_sum(dacc);
+              if (lane == 0) part[j] += dacc;  // tile by tile, in order: the same bits in every run
             }
           }
-          for (; i < q1; i += 32) {
-            const float4 x = vj4[i], y = w4[i];
-            acc = fmaf(x.x, y.x, acc);
-            acc = fmaf(x.y, y.y, acc);
-            acc = fmaf(x.z, y.z, acc);
-            acc = fmaf(x.w, y.w, acc);
-            if (++cnt == kChunk / 4) {
-              dacc += (double)acc;
-              acc = 0.f;
-              cnt = 0;
-            }
+          // ||u||^2 of this CTA's rows into part[k]
+          uacc = warp_sum(uacc);
+          __syncthreads();
+          if (lane == 0) S.red[warp] = uacc;
+          __syncthreads();
+          if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int q = 0; q < nw; ++q) t += S.red[q];
+            part[k] = t;
           }
-          for (int64_t i = (q1 << 2) + lane; i < hi; i += 32) acc = fmaf(vj[i], w[i], acc);
-          dacc += (double)acc;
-          dacc = warp_sum(dacc);
-          if (lane == 0) part[j] = dacc;
         }
         if constexpr (C > 1) {  // the coefficients of the whole vector, the same bits in every CTA
           cg::cluster_group cl = cg::this_cluster();
           cl.sync();
-          for (int j = threadIdx.x; j < k; j += blockDim.x) {
+          for (int j = threadIdx.x; j <= k; j += blockDim.x) {
             double t = 0.0;
             for (int r = 0; r < C; ++r) t += *cl.map_shared_rank(&S.hp[hbuf][j], r);
             S.h[j] = t;
@@ -376,14 +529,29 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const B
           hbuf ^= 1;
         }
         __syncthreads();
-        float4* wm4 = reinterpret_cast<float4*>(w);
+        // update coefficients of the stored vectors: u' = u - sum_j scl[j]^2 g_j V[j]
+        for (int j = threadIdx.x; j < k; j += blockDim.x) S.c[j] = S.scl[j] * S.scl[j] * S.h[j];
+        {
+          int e2 = 0;
+          const double un = sqrt(S.h[k]);
+          if (un > 0.0 && std::isfinite(un)) {
+            frexp(un, &e2);
+            tk = ldexpf(1.f, -e2);  // tk ||u|| in [0.5, 1)
+          }
+        }
+        __syncthreads();
+        // V[k] = tk (u - sum_j c_j V[j]), and its squared norm (FP32 over at most kChunk elements)
+        const float4* wm4 = reinterpret_cast<const float4*>(w);
+        float4* vk4 = reinterpret_cast<float4*>(V + (int64_t)k * I.ld);
         const int64_t bs = blockDim.x;
+        float nf = 0.f;
+        int ncnt = 0;
         int64_t i = q0 + threadIdx.x;
-        for (; i + bs < q1; i += 2 * bs) {  // two float4 of w per thread: two independent chains
+        for (; i + bs < q1; i += 2 * bs) {  // two float4 of u per thread: two independent chains
           float4 x = wm4[i], u = wm4[i + bs];
 #pragma unroll 4
           for (int j = 0; j < k; ++j) {
-            const float c = -(float)S.h[j];
+            const float c = -(float)S.c[j];
             const float4* vj4 = reinterpret_cast<const float4*>(V + (int64_t)j * I.ld);
             const float4 y = vj4[i], z = vj4[i + bs];
             x.x = fmaf(c, y.x, x.x);
@@ -395,33 +563,66 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const B
             u.z = fmaf(c, z.z, u.z);
             u.w = fmaf(c, z.w, u.w);
           }
-          wm4[i] = x;
-          wm4[i + bs] = u;
+          x = make_float4(x.x * tk, x.y * tk, x.z * tk, x.w * tk);
+          u = make_float4(u.x * tk, u.y * tk, u.z * tk, u.w * tk);
+          vk4[i] = x;
+          vk4[i + bs] = u;
+          nf = fmaf(x.x, x.x, nf);
+          nf = fmaf(x.y, x.y, nf);
+          nf = fmaf(x.z, x.z, nf);
+          nf = fmaf(x.w, x.w, nf);
+          nf = fmaf(u.x, u.x, nf);
+          nf = fmaf(u.y, u.y, nf);
+          nf = fmaf(u.z, u.z, nf);
+          nf = fmaf(u.w, u.w, nf);
+          if (++ncnt == kChunk / 8) {
+            nacc += (double)nf;
+            nf = 0.f;
+            ncnt = 0;
+          }
         }
+        nacc += (double)nf;
+        nf = 0.f;
+        ncnt = 0;
         for (; i < q1; i += bs) {
           float4 x = wm4[i];
 #pragma unroll 4
           for (int j = 0; j < k; ++j) {
-            const float c = -(float)S.h[j];
+            const float c = -(float)S.c[j];
             const float4 y = reinterpret_cast<const float4*>(V + (int64_t)j * I.ld)[i];
             x.x = fmaf(c, y.x, x.x);
             x.y = fmaf(c, y.y, x.y);
             x.z = fmaf(c, y.z, x.z);
             x.w = fmaf(c, y.w, x.w);
           }
-          wm4[i] = x;
+          x = make_float4(x.x * tk, x.y * tk, x.z * tk, x.w * tk);
+          vk4[i] = x;
+          nf = fmaf(x.x, x.x, nf);
+          nf = fmaf(x.y, x.y, nf);
+          nf = fmaf(x.z, x.z, nf);
+          nf = fmaf(x.w, x.w, nf);
+          if (++ncnt == kChunk / 4) {
+            nacc += (double)nf;
+            nf = 0.f;
+            ncnt = 0;
+          }
         }
+        float* vk = V + (int64_t)k * I.ld;
         for (int64_t i = (q1 << 2) + threadIdx.x; i < hi; i += blockDim.x) {
           float wi = w[i];
-          for (int j = 0; j < k; ++j) wi = fmaf(-(float)S.h[j], V[(int64_t)j * I.ld + i], wi);
-          w[i] = wi;
+          for (int j = 0; j < k; ++j) wi = fmaf(-(float)S.c[j], V[(int64_t)j * I.ld + i], wi);
+          wi *= tk;
+          vk[i] = wi;
+          nf = fmaf(wi, wi, nf);
         }
-        __syncthreads();
+        nacc += (double)nf;
       }
-      const double nr = sqrt(inst_sum<C>(block_dot(w, w, lo, hi, S), S, buf));
+      const double nst = sqrt(inst_sum<C>(block_sum_all(nacc, S), S, buf));  // ||V[k]|| as stored
+      const double nr = s1 * nst / (double)tk;                               // beta_k
       if (threadIdx.x == 0) {
-        S.alpha[k] = al + S.h[k - 1];
+        S.alpha[k] = al + s1 * s1 * S.h[k - 1];  // al + <v_{k-1}, u> in the true vectors
         S.beta[k] = nr;
+        S.scl[k] = (nst > 0.0) ? 1.0 / nst : 0.0;
         // breakdown (sparse_algorithm.hpp:421): the reference's 1e-10, or the
         // FP32 resolution of the recurrence, or an exhausted space
         const double scale = fabs(al) + fabs(bp) + (k >= 2 ? S.beta[k - 1] : 0.0);
@@ -432,10 +633,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const B
         act = k;     // v_0 .. v_{k-1} span an invariant subspace: T_k is exact
         break;
       }
-      const float inv = (float)(1.0 / nr);
-      float* vk = V + (int64_t)k * I.ld;
-      for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) vk[i] = w[i] * inv;
-      inst_sync<C>();  // the next product reads all of v_k
+      inst_sync<C>();  // the next product reads all of V[k]
     }
     if (act < 1) act = 1;
     // lowest Ritz pair of tridiag(alpha_1..act, beta_1..act-1), the same in every CTA
@@ -452,7 +650,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const B
     // Ritz vector psi = sum_k y_k v_k (FP32 storage)
     for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
       float acc = 0.f;
-      for (int k = 0; k < act; ++k) acc = fmaf((float)S.y[k], V[(int64_t)k * I.ld + i], acc);
+      for (int k = 0; k < act; ++k) acc = fmaf((float)(S.y[k] * S.scl[k]), V[(int64_t)k * I.ld + i], acc);
       I.psi[i] = acc;
     }
     inst_sync<C>();  // the refinement reads all of psi
