@@ -34,7 +34,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 #include <cooperative_groups.h>
@@ -196,6 +198,43 @@ struct ProdDots {
   }
 };
 
+// The same product when every off-diagonal value is one c (uniform hopping, any
+// diagonal): y_r = c (sum of x over the row's stored columns) + e_r x_r with
+// e_r = d_r - c where the row stores its diagonal (else 0), the column indices
+// the only per-entry reads (no values).
+__device__ void block_spmv_f32_uniform(const BatchInst& I, const float* x, const float* v2, float* __restrict__ y,
+                                       int64_t lo, int64_t hi, ProdDots& pd) {
+  const float c = __ldg(I.coff);
+  const int64_t bs = blockDim.x;
+  int64_t r = lo + threadIdx.x;
+  auto finish = [&](int64_t row, float sum) {
+    const float yr = fmaf(c, sum, __ldg(I.diag_f + row) * x[row]);
+    y[row] = yr;
+    pd.add(x, v2, row, yr);
+  };
+  for (; r + bs < hi; r += 2 * bs) {
+    const int64_t b0 = I.rowptr[r], e0 = I.rowptr[r + 1], b1 = I.rowptr[r + bs], e1 = I.rowptr[r + bs + 1];
+    float a0 = 0.f, a1 = 0.f;
+    int64_t k0 = b0, k1 = b1;
+    for (; k0 + 4 <= e0 && k1 + 4 <= e1; k0 += 4, k1 += 4) {  // eight gathers in flight
+      const int32_t c0 = I.colidx[k0], c1 = I.colidx[k0 + 1], c2 = I.colidx[k0 + 2], c3 = I.colidx[k0 + 3];
+      const int32_t d0 = I.colidx[k1], d1 = I.colidx[k1 + 1], d2 = I.colidx[k1 + 2], d3 = I.colidx[k1 + 3];
+      a0 += (x[c0] + x[c1]) + (x[c2] + x[c3]);
+      a1 += (x[d0] + x[d1]) + (x[d2] + x[d3]);
+    }
+    for (; k0 < e0; ++k0) a0 += x[I.colidx[k0]];
+    for (; k1 < e1; ++k1) a1 += x[I.colidx[k1]];
+    finish(r, a0);
+    finish(r + bs, a1);
+  }
+  if (r < hi) {
+    float a0 = 0.f;
+    for (int64_t k = I.rowptr[r]; k < I.rowptr[r + 1]; ++k) a0 += x[I.colidx[k]];
+    finish(r, a0);
+  }
+  pd.flush();
+}
+
 __device__ void block_spmv_f32(const BatchInst& I, const float* x, const float* v2, float* __restrict__ y, int64_t lo,
                                int64_t hi, ProdDots& pd) {
   const int64_t bs = blockDim.x;
@@ -235,6 +274,79 @@ __device__ void block_spmv_f32(const BatchInst& I, const float* x, const float* 
     pd.add(x, v2, r, a0);
   }
   pd.flush();
+}
+
+// ---------------------------------------------------------------- uniform check
+struct BunJob {
+  int64_t n;
+  const int64_t* rowptr;
+  const int32_t* colidx;
+  const float* vals;
+  int* flag;
+  float* c;
+  float* d;
+};
+
+// One CTA per Hamiltonian: c = the first off-diagonal value (rows in order), then flag = 1
+// if every off-diagonal value equals c and c is not 0 (an explicit zero off the diagonal
+// fails: the uniform form would add it as c), and d_r = diagonal - c where the row stores
+// its diagonal, else 0.
+__global__ void __launch_bounds__(512) bun_check_kernel(const BunJob* jobs) {
+  const BunJob J = jobs[blockIdx.x];
+  __shared__ float sc;
+  __shared__ int found, bad;
+  if (threadIdx.x == 0) {
+    found = 0;
+    bad = 0;
+    for (int64_t r = 0; r < J.n && !found; ++r)
+      for (int64_t k = J.rowptr[r]; k < J.rowptr[r + 1]; ++k)
+        if (J.colidx[k] != (int32_t)r) {
+          sc = J.vals[k];
+          found = 1;
+          break;
+        }
+  }
+  __syncthreads();
+  const float c = found ? sc : 0.f;
+  for (int64_t r = threadIdx.x; r < J.n; r += blockDim.x) {
+    float d = 0.f;  // d_r - c where the row stores its diagonal (its x_r is in the column sum), else 0
+    for (int64_t k = J.rowptr[r]; k < J.rowptr[r + 1]; ++k) {
+      if (J.colidx[k] == (int32_t)r) d = J.vals[k] - c;
+      else if (J.vals[k] != c || c == 0.f) bad = 1;
+    }
+    J.d[r] = d;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    *J.flag = (found && !bad) ? 1 : 0;
+    *J.c = c;
+  }
+}
+
+// The check for the Hamiltonians of a call that have not had it, in one launch.
+static void check_uniform(Ctx* ctx, qd_ham* const* hams, int ninst) {
+  std::vector<BunJob> jobs;
+  std::vector<qd_ham*> done;
+  for (int i = 0; i < ninst; ++i) {
+    qd_ham* H = hams[i];
+    if (H->bun_checked || std::find(done.begin(), done.end(), H) != done.end()) continue;
+    H->bun_d.alloc(H->dim + 4);  // e_r, then c at [dim], the flag's bits at [dim + 1]
+    float* c = H->bun_d.p + H->dim;
+    jobs.push_back(BunJob{H->dim, H->rowptr.p, H->colidx.p, H->vals_f.p, reinterpret_cast<int*>(c + 1), c,
+                          H->bun_d.p});
+    done.push_back(H);
+  }
+  if (jobs.empty()) return;
+  DBuf<BunJob> dj(jobs.size());
+  QD_CUDA(cudaMemcpyAsync(dj.p, jobs.data(), jobs.size() * sizeof(BunJob), cudaMemcpyHostToDevice, ctx->stream));
+  for (size_t j0 = 0; j0 < jobs.size(); j0 += 65535) {
+    const unsigned cnt = (unsigned)std::min<size_t>(65535, jobs.size() - j0);
+    bun_check_kernel<<<cnt, 512, 0, ctx->stream>>>(dj.p + j0);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+  }
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));  // dj is freed on return
+  for (qd_ham* H : done) H->bun_checked = true;
 }
 
 // ---------------------------------------------------------------- cluster sums
@@ -388,6 +500,7 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const B
     const int64_t lo = std::min<int64_t>(n, (int64_t)rank * per), hi = std::min<int64_t>(n, lo + per);
     float* V = I.V;
     float* w = I.w;
+    const bool uni = I.uniform && __ldg(I.uniform) == 1;
     // v_0 = v0 / ||v0||
     const double nrm0 = sqrt(inst_sum<C>(block_dot(I.v0, I.v0, lo, hi, S), S, buf));
     const float inv0 = (float)(1.0 / nrm0);
@@ -407,7 +520,8 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const B
       const float* v2 = (k >= 2) ? V + (int64_t)(k - 2) * I.ld : nullptr;
       const double s1 = S.scl[k - 1], s2 = (k >= 2) ? S.scl[k - 2] : 0.0;
       ProdDots pd;
-      block_spmv_f32(I, v1, v2, w, lo, hi, pd);
+      if (uni) block_spmv_f32_uniform(I, v1, v2, w, lo, hi, pd);
+      else block_spmv_f32(I, v1, v2, w, lo, hi, pd);
       double d3[3] = {pd.da, pd.db, pd.dc};
       block_sum_all3(d3, S);
       inst_sum3<C>(d3, S, buf);
@@ -738,6 +852,10 @@ void batch_lanczos(Ctx* ctx, qd_ham* const* hams, const double* const* v0s, int 
                "instance %d: the batched mixed-precision solver needs a real Hamiltonian", i);
     QD_REQUIRE(hams[i]->ctx == ctx, QD_ERR_INVALID, "instance %d: Hamiltonian of another context", i);
   }
+  // QD_BATCH_UNIFORM=0 keeps the valued product for every instance
+  const char* uenv = std::getenv("QD_BATCH_UNIFORM");
+  const bool uniform_ok = !(uenv && std::strcmp(uenv, "0") == 0);
+  if (uniform_ok) check_uniform(ctx, hams, ninst);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return hams[a]->nnz > hams[b]->nnz; });
   // large instances (a cluster each) first, each class longest first
   std::stable_partition(order.begin(), order.end(), [&](int a) { return hams[a]->dim >= kClusterMinDim; });
@@ -759,14 +877,29 @@ void batch_lanczos(Ctx* ctx, qd_ham* const* hams, const double* const* v0s, int 
   // the start vectors, in FP32, in one copy
   int64_t v0_total = 0;
   for (int i = 0; i < ninst; ++i) v0_total += (hams[i]->dim + 31) / 32 * 32;
-  std::vector<float> h32((size_t)v0_total, 0.f);
+  std::unique_ptr<float[]> h32(new float[(size_t)std::max<int64_t>(v0_total, 1)]);
   DBuf<float> v0buf(v0_total);
   std::vector<int64_t> off_h(ninst);
-  for (int i = 0; i < ninst; ++i) {
-    off_h[i] = (i == 0) ? 0 : off_h[i - 1] + (hams[i - 1]->dim + 31) / 32 * 32;
-    for (int64_t q = 0; q < hams[i]->dim; ++q) h32[(size_t)(off_h[i] + q)] = (float)v0s[i][q];
+  for (int i = 0; i < ninst; ++i) off_h[i] = (i == 0) ? 0 : off_h[i - 1] + (hams[i - 1]->dim + 31) / 32 * 32;
+  {
+    // FP64 -> FP32 on up to eight host threads, instances dealt round-robin (padding zeroed)
+    const int nt = (int)std::max<int64_t>(1, std::min<int64_t>(8, v0_total >> 20));
+    auto convert = [&](int t) {
+      for (int i = t; i < ninst; i += nt) {
+        const int64_t d = hams[i]->dim, ld = (d + 31) / 32 * 32;
+        float* o = h32.get() + off_h[i];
+        const double* v = v0s[i];
+        for (int64_t q = 0; q < d; ++q) o[q] = (float)v[q];
+        for (int64_t q = d; q < ld; ++q) o[q] = 0.f;
+      }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(convert, t);
+    convert(0);
+    for (auto& th : pool) th.join();
   }
-  QD_CUDA(cudaMemcpyAsync(v0buf.p, h32.data(), h32.size() * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(v0buf.p, h32.get(), (size_t)v0_total * sizeof(float), cudaMemcpyHostToDevice,
+                          ctx->stream));
   // the work list: large instances, then small ones
   std::vector<BatchInst> list(ninst);
   int nlarge = 0;
@@ -792,6 +925,9 @@ void batch_lanczos(Ctx* ctx, qd_ham* const* hams, const double* const* v0s, int 
     I.rowptr = H->rowptr.p;
     I.colidx = H->colidx.p;
     I.vals_f = H->vals_f.p;
+    I.uniform = uniform_ok ? reinterpret_cast<const int*>(H->bun_d.p + H->dim + 1) : nullptr;
+    I.coff = H->bun_d.p + H->dim;
+    I.diag_f = H->bun_d.p;
     I.vals_d = H->vals_r.p;
     I.v0 = v0buf.p + off_h[i];
     I.V = arena.p + off_V[i];

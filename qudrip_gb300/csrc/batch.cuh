@@ -13,6 +13,9 @@ struct BatchInst {
   const int64_t* rowptr;
   const int32_t* colidx;
   const float* vals_f;   // FP32 copy of the values
+  const int* uniform;    // device flag: every off-diagonal value is *coff (the product reads no values)
+  const float* coff;
+  const float* diag_f;   // uniform form: d_r - c where row r stores its diagonal, else 0
   const double* vals_d;  // FP64 values (refinement)
   const float* v0;       // start vector
   float* V;              // (steps + 1) x ld Krylov basis

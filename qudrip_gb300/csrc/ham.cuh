@@ -89,6 +89,11 @@ struct qd_ham {
   qd::DBuf<double> vals_r;
   qd::DBuf<float> vals_f;  // fp32 copy of vals_r for the mixed-precision SpMV
   qd::DBuf<int32_t> row_order;  // rows by decreasing length inside 256-row windows (kernel 111)
+  // the batched solver's check for one common off-diagonal FP32 value (batch.cu): run once,
+  // dropped when the matrix changes; bun_d holds d_r - c per row (0 where the row stores no
+  // diagonal), then c, then the flag (1 when the value is common) as an int
+  bool bun_checked = false;
+  qd::DBuf<float> bun_d;
   // uniform-coupling form with exact fixed-point sums (fxsum.cuh)
   int fx_state = 0;          // 0 not tried, 1 built, -1 not applicable
   bool fx_allowed = true;    // the Lanczos product uses it when built (kernel code 120)

@@ -398,6 +398,8 @@ void ham_finish(qd_ham* H) {
   const int64_t nnz = H->nnz;
   H->vals_r = DBuf<double>();
   H->vals_f = DBuf<float>();
+  H->bun_checked = false;  // the batched solver's uniform-value check follows the values
+  H->bun_d = DBuf<float>();
   if (H->flags & QD_HAM_REAL) {
     H->vals_r.alloc(nnz + 16);
     H->vals_f.alloc(nnz + 16);

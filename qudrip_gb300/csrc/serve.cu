@@ -135,7 +135,7 @@ static int64_t held_bytes(const qd_sector* S, const qd_ham* H) {
   if (S) b += dbytes(S->basis) + dbytes(S->binom) + dbytes(S->dir);
   if (H) {
     b += dbytes(H->rowptr) + dbytes(H->colidx) + dbytes(H->vals_c) + dbytes(H->vals_r) + dbytes(H->vals_f) +
-         dbytes(H->row_order) + dbytes(H->diag_r);
+         dbytes(H->row_order) + dbytes(H->diag_r) + dbytes(H->bun_d);
     if (H->ws) {
       const Workspace& W = *H->ws;
       b += dbytes(W.partials_d) + dbytes(W.gpart_d) + dbytes(W.partials_c) + dbytes(W.gpart_c) +

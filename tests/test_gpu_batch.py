@@ -112,3 +112,55 @@ def test_batch_many_large_instances_take_small_clusters(ctx):
         assert out[i, 3] == 80 and out[i, 4] == 0
     for i in (0, 1):
         assert abs(out[i, 1] - few[i, 1]) <= DE_TOL * abs(few[i, 1])
+
+
+def bond_disorder_xxz(L, seed):
+    """XXZ ring with bond-dependent hopping: no common off-diagonal value."""
+    from qudrip_gb300.operators import (II, SectorSpec, getBoseGate, getEmptyOperator, getNset, getQbits,
+                                        pauli_x, pauli_y, pauli_z)
+    rng = np.random.default_rng(seed)
+    pre = getQbits(L)
+    gc, ga, gz = getBoseGate(pre), getBoseGate(pre), getBoseGate(pre)
+    gc << 0.5 * (pauli_x + II * pauli_y)
+    ga << 0.5 * (pauli_x - II * pauli_y)
+    gz << 0.5 * pauli_z
+    ham = getEmptyOperator()
+    for i in range(L):
+        j = (i + 1) % L
+        t = float(rng.uniform(0.5, 1.5))
+        ham = ham + (0.5 * t) * (gc(i) * ga(j)) + (0.5 * t) * (gc(j) * ga(i)) + gz(i) * gz(j)
+    return SectorSpec(pre, [getNset(pre) == L // 2]), ham
+
+
+def test_batch_uniform_and_valued_products_in_one_call(ctx):
+    """One call mixing the two FP32 products: uniform hopping with a diagonal (random-field
+    XXZ), uniform hopping without stored diagonal entries (open XY chain: the column sum must
+    not count x_r), and bond disorder (the valued product).  Each refined energy is within
+    DE_TOL of the FP64 oracle; out[:, 5:8] hold each instance's device start and end (ns) and
+    the CTAs that computed it."""
+    cases = [chains.xxz_chain(14, 1.0, 1.0, True, np.random.default_rng(7).uniform(-2, 2, 14)),
+             chains.xy_chain(14),
+             bond_disorder_xxz(14, 8),
+             bond_disorder_xxz(18, 9)]  # a cluster instance (dim 48,620) on the valued product
+    hams, v0s, refs = [], [], []
+    for spec, ham in cases:
+        sec = q.Sector(spec.index, spec.constraints)
+        H = sec.lower(ham)
+        H._keep = sec
+        hams.append(H)
+        v0 = q.start_vector(sec.dim, 40 + len(hams))
+        v0s.append(v0)
+        refs.append(O.Ham(O.Sector(spec), ham).lanczos_ground(v0, 60)["ritz"])
+    out = q.batch_lanczos(hams, v0s, 60)
+    for i, ref in enumerate(refs):
+        assert abs(out[i, 1] - ref) <= DE_TOL * abs(ref), (i, out[i, 1], ref)
+    assert np.all(out[:, 6] > out[:, 5]) and np.all(out[:, 5] > 0)
+    assert out[3, 7] >= 2 and out[0, 7] == 1
+    # the same energies when every instance takes the valued product
+    import os
+    os.environ["QD_BATCH_UNIFORM"] = "0"
+    try:
+        out2 = q.batch_lanczos(hams, v0s, 60)
+    finally:
+        del os.environ["QD_BATCH_UNIFORM"]
+    assert np.allclose(out2[:, 1], out[:, 1], rtol=DE_TOL, atol=0)
