@@ -300,29 +300,6 @@ __global__ void __launch_bounds__(kVecThreads) ritz_kernel(int64_t n, const VV* 
   }
 }
 
-// The real basis two elements per thread (16-byte loads, two independent
-// chains); each element still sums in k order, so psi carries the same bits.
-// ld is a multiple of 32, so the pair (i, i + 1) stays inside the basis.
-__global__ void __launch_bounds__(kVecThreads) ritz_pair_kernel(int64_t n, const double* V, int64_t ld,
-                                                                const double* y, int act, cplx* psi) {
-  const int64_t np = (n + 1) / 2;
-  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < np; p += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = 2 * p;
-    const double y0 = __ldg(y);
-    double2 v = __ldcs(reinterpret_cast<const double2*>(V + i));
-    double a0 = y0 * v.x, a1 = y0 * v.y;
-#pragma unroll 4
-    for (int k = 1; k < act; ++k) {
-      const double yk = __ldg(y + k);
-      v = __ldcs(reinterpret_cast<const double2*>(V + (int64_t)k * ld + i));
-      a0 = fma(yk, v.x, a0);
-      a1 = fma(yk, v.y, a1);
-    }
-    psi[i] = mkc(a0, 0.0);
-    if (i + 1 < n) psi[i + 1] = mkc(a1, 0.0);
-  }
-}
-
 // <a, b> over complex columns (a^dagger b).
 __global__ void __launch_bounds__(kVecThreads) cdot_kernel(int64_t n, const cplx* a, const cplx* b, cplx* out,
                                                            GridRed<cplx> red) {
@@ -860,10 +837,7 @@ static void lanczos_finish(qd_ham* H, cplx* psi, const double* psi_nrm2, const q
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
   for (int i = 0; i < act; ++i) yk[i] = z[i] * scl[i];
   QD_CUDA(cudaMemcpyAsync(B.y.p, yk.data(), act * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
-  if constexpr (std::is_same<VV, double>::value)
-    ritz_pair_kernel<<<vec_grid(ctx, (n + 1) / 2), kVecThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, B.y.p, act, psi);
-  else
-    ritz_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, B.y.p, act, psi);
+  ritz_kernel<VV><<<vg, kVecThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, B.y.p, act, psi);
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
