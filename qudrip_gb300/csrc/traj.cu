@@ -270,49 +270,66 @@ __global__ void __launch_bounds__(kTrajMaxWarps * 32, 1) traj_resident_kernel(Tr
             const float f = A.tau / (float)k * ((sub == 0 && k == 1) ? sc : 1.f);
             const float2* __restrict__ src = M.tb[rb];
             float2* __restrict__ dst = M.tb[rb ^ 1];
+            // Two slices at a time (i and i + 1): their entry loads and gathers interleave, so a
+            // lane has four independent gathers in flight; each row keeps its own sums in entry
+            // order (even entries in s, odd ones in u).
+            auto gather = [&](uint32_t pr, float& sx, float& sy, float& ux, float& uy) {
+              const uint32_t ev = pr & 0xffffu, fv = pr >> 16;
+              if (kSigned) {
+                const float2 x = src[ev & 0x7fffu], y = src[fv & 0x7fffu];
+                const float sg = __uint_as_float(0x3f800000u | ((ev & 0x8000u) << 16));
+                const float tg = __uint_as_float(0x3f800000u | ((fv & 0x8000u) << 16));
+                sx = fmaf(sg, x.x, sx);
+                sy = fmaf(sg, x.y, sy);
+                ux = fmaf(tg, y.x, ux);
+                uy = fmaf(tg, y.y, uy);
+              } else {  // every entry carries +c: plain sums
+                const float2 x = src[ev], y = src[fv];
+                sx += x.x;
+                sy += x.y;
+                ux += y.x;
+                uy += y.y;
+              }
+            };
+            auto finish = [&](int i, int r, float sx, float sy) {
+              if (r < A.n) {
+                const float2 o = src[r];
+                // v = c * sum + dg * own
+                const float vx = fmaf(A.coff.x, sx, fmaf(-A.coff.y, sy, fmaf(dg[i].x, o.x, -dg[i].y * o.y)));
+                const float vy = fmaf(A.coff.x, sy, fmaf(A.coff.y, sx, fmaf(dg[i].x, o.y, dg[i].y * o.x)));
+                // t = (-i f) v = (f vy, -f vx)
+                const float2 t = make_float2(f * vy, -f * vx);
+                dst[r] = t;
+                acc[i].x += t.x;
+                acc[i].y += t.y;
+              }
+            };
 #pragma unroll
-            for (int i = 0; i < kTrajRpt; ++i) {
-              const int s = warp + i * A.nwarps;
-              if (s < A.nsl) {
-                const int slot = 32 * s + lane;
-                const int r = M.rid[slot];
-                const int2 sd = M.sd[s];
-                // a lane's entries 2j and 2j+1 share one 32-bit word (sd.y is even)
-                const uint32_t* e2 = reinterpret_cast<const uint32_t*>(M.ent + sd.x) + lane;
-                float sx = 0.f, sy = 0.f, ux = 0.f, uy = 0.f;
-#pragma unroll 2
-                for (int q = 0; q < (sd.y >> 1); ++q) {  // two independent gathers in flight
-                  const uint32_t pr = e2[32 * q];
-                  const uint32_t ev = pr & 0xffffu, fv = pr >> 16;
-                  if (kSigned) {
-                    const float2 x = src[ev & 0x7fffu], y = src[fv & 0x7fffu];
-                    const float sg = __uint_as_float(0x3f800000u | ((ev & 0x8000u) << 16));
-                    const float tg = __uint_as_float(0x3f800000u | ((fv & 0x8000u) << 16));
-                    sx = fmaf(sg, x.x, sx);
-                    sy = fmaf(sg, x.y, sy);
-                    ux = fmaf(tg, y.x, ux);
-                    uy = fmaf(tg, y.y, uy);
-                  } else {  // every entry carries +c: plain sums
-                    const float2 x = src[ev], y = src[fv];
-                    sx += x.x;
-                    sy += x.y;
-                    ux += y.x;
-                    uy += y.y;
-                  }
+            for (int i = 0; i < kTrajRpt; i += 2) {
+              const int s0 = warp + i * A.nwarps, s1 = s0 + A.nwarps;
+              if (s0 < A.nsl) {
+                const bool has1 = s1 < A.nsl;
+                const int2 d0 = M.sd[s0];
+                const int2 d1 = has1 ? M.sd[s1] : make_int2(0, 0);
+                const int r0 = M.rid[32 * s0 + lane];
+                const int r1 = has1 ? (int)M.rid[32 * s1 + lane] : A.n;
+                // a lane's entries 2j and 2j+1 share one 32-bit word (widths are even)
+                const uint32_t* e0 = reinterpret_cast<const uint32_t*>(M.ent + d0.x) + lane;
+                const uint32_t* e1 = reinterpret_cast<const uint32_t*>(M.ent + d1.x) + lane;
+                const int w0 = d0.y >> 1, w1 = d1.y >> 1;
+                float sx0 = 0.f, sy0 = 0.f, ux0 = 0.f, uy0 = 0.f;
+                float sx1 = 0.f, sy1 = 0.f, ux1 = 0.f, uy1 = 0.f;
+                const int wm = min(w0, w1);
+                int q = 0;
+                for (; q < wm; ++q) {
+                  const uint32_t p0 = e0[32 * q], p1 = e1[32 * q];
+                  gather(p0, sx0, sy0, ux0, uy0);
+                  gather(p1, sx1, sy1, ux1, uy1);
                 }
-                sx += ux;
-                sy += uy;
-                if (r < A.n) {
-                  const float2 o = src[r];
-                  // v = c * sum + dg * own
-                  const float vx = fmaf(A.coff.x, sx, fmaf(-A.coff.y, sy, fmaf(dg[i].x, o.x, -dg[i].y * o.y)));
-                  const float vy = fmaf(A.coff.x, sy, fmaf(A.coff.y, sx, fmaf(dg[i].x, o.y, dg[i].y * o.x)));
-                  // t = (-i f) v = (f vy, -f vx)
-                  const float2 t = make_float2(f * vy, -f * vx);
-                  dst[r] = t;
-                  acc[i].x += t.x;
-                  acc[i].y += t.y;
-                }
+                for (int q0 = q; q0 < w0; ++q0) gather(e0[32 * q0], sx0, sy0, ux0, uy0);
+                for (int q1 = q; q1 < w1; ++q1) gather(e1[32 * q1], sx1, sy1, ux1, uy1);
+                finish(i, r0, sx0 + ux0, sy0 + uy0);
+                if (has1) finish(i + 1, r1, sx1 + ux1, sy1 + uy1);
               }
             }
             __syncthreads();
