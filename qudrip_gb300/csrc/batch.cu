@@ -295,16 +295,30 @@ __global__ void __launch_bounds__(512) bun_check_kernel(const BunJob* jobs) {
   const BunJob J = jobs[blockIdx.x];
   __shared__ float sc;
   __shared__ int found, bad;
+  __shared__ unsigned long long first;  // the first row with an off-diagonal entry
   if (threadIdx.x == 0) {
     found = 0;
     bad = 0;
-    for (int64_t r = 0; r < J.n && !found; ++r)
-      for (int64_t k = J.rowptr[r]; k < J.rowptr[r + 1]; ++k)
-        if (J.colidx[k] != (int32_t)r) {
-          sc = J.vals[k];
-          found = 1;
-          break;
-        }
+    first = ~0ull;
+  }
+  __syncthreads();
+  for (int64_t r = threadIdx.x; r < J.n; r += blockDim.x) {
+    bool off = false;
+    for (int64_t k = J.rowptr[r]; k < J.rowptr[r + 1] && !off; ++k) off = J.colidx[k] != (int32_t)r;
+    if (off) {
+      atomicMin(&first, (unsigned long long)r);
+      break;  // this thread's later rows are larger
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0 && first != ~0ull) {
+    const int64_t r = (int64_t)first;
+    for (int64_t k = J.rowptr[r]; k < J.rowptr[r + 1]; ++k)
+      if (J.colidx[k] != (int32_t)r) {
+        sc = J.vals[k];
+        found = 1;
+        break;
+      }
   }
   __syncthreads();
   const float c = found ? sc : 0.f;

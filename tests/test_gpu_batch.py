@@ -135,13 +135,15 @@ def bond_disorder_xxz(L, seed):
 def test_batch_uniform_and_valued_products_in_one_call(ctx):
     """One call mixing the two FP32 products: uniform hopping with a diagonal (random-field
     XXZ), uniform hopping without stored diagonal entries (open XY chain: the column sum must
-    not count x_r), and bond disorder (the valued product).  Each refined energy is within
+    not count x_r), bond disorder (the valued product) and a diagonal matrix (no off-diagonal
+    value: the valued product).  Each refined energy is within
     DE_TOL of the FP64 oracle; out[:, 5:8] hold each instance's device start and end (ns) and
     the CTAs that computed it."""
     cases = [chains.xxz_chain(14, 1.0, 1.0, True, np.random.default_rng(7).uniform(-2, 2, 14)),
              chains.xy_chain(14),
              bond_disorder_xxz(14, 8),
-             bond_disorder_xxz(18, 9)]  # a cluster instance (dim 48,620) on the valued product
+             bond_disorder_xxz(18, 9),  # a cluster instance (dim 48,620) on the valued product
+             chains.xxz_chain(12, 0.0, 1.0, True, np.linspace(-1, 1, 12))]  # no off-diagonal entry at all
     hams, v0s, refs = [], [], []
     for spec, ham in cases:
         sec = q.Sector(spec.index, spec.constraints)
