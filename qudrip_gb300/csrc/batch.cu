@@ -865,6 +865,7 @@ void batch_lanczos(Ctx* ctx, qd_ham* const* hams, const double* const* v0s, int 
     QD_REQUIRE(hams[i]->flags & QD_HAM_REAL, QD_ERR_UNSUPPORTED,
                "instance %d: the batched mixed-precision solver needs a real Hamiltonian", i);
     QD_REQUIRE(hams[i]->ctx == ctx, QD_ERR_INVALID, "instance %d: Hamiltonian of another context", i);
+    QD_REQUIRE(hams[i]->dim >= 1, QD_ERR_INVALID, "instance %d: the sector has no state", i);
   }
   // QD_BATCH_UNIFORM=0 keeps the valued product for every instance
   const char* uenv = std::getenv("QD_BATCH_UNIFORM");

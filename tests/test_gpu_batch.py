@@ -166,3 +166,31 @@ def test_batch_uniform_and_valued_products_in_one_call(ctx):
     finally:
         del os.environ["QD_BATCH_UNIFORM"]
     assert np.allclose(out2[:, 1], out[:, 1], rtol=DE_TOL, atol=0)
+
+
+def test_batch_one_state_and_empty_instances(ctx):
+    """A one-state sector (no particle) batched beside a normal instance gives its diagonal
+    value exactly; a sector without states is refused before any device work."""
+    from qudrip_gb300 import _capi as A
+    spec1, ham1 = chains.xxz_chain(6, 1.0, 1.0, True, np.linspace(-1, 1, 6))
+    vac = q.SectorSpec(spec1.index, [q.getNset(spec1.index) == 0])
+    sec0 = q.Sector(vac.index, vac.constraints)
+    H0 = sec0.lower(ham1)
+    H0._keep = sec0
+    assert sec0.dim == 1
+    spec2, ham2 = chains.xxz_chain(10, 1.0, 1.0, True, np.linspace(-1, 1, 10))
+    sec2 = q.Sector(spec2.index, spec2.constraints)
+    H2 = sec2.lower(ham2)
+    H2._keep = sec2
+    out = q.batch_lanczos([H0, H2], [np.ones(1), q.start_vector(sec2.dim, 3)], 40)
+    d = H0.scipy().toarray()[0, 0].real
+    assert abs(out[0, 1] - d) <= 1e-12 * max(1.0, abs(d)) and out[0, 3] == 1
+    ref = O.Ham(O.Sector(spec2), ham2).lanczos_ground(q.start_vector(sec2.dim, 3), 40)["ritz"]
+    assert abs(out[1, 1] - ref) <= DE_TOL * abs(ref)
+    empty = q.SectorSpec(spec1.index, [q.getNset(spec1.index) == 7])
+    sec_e = q.Sector(empty.index, empty.constraints)
+    He = sec_e.lower(ham1)
+    He._keep = sec_e
+    with pytest.raises(A.QDError) as e:
+        q.batch_lanczos([He], [np.ones(0)], 10)
+    assert e.value.code == A.QD_ERR_INVALID
