@@ -27,9 +27,16 @@ namespace qd {
 
 constexpr int kEvThreads = 256;
 
+// Grid of the multi-dot kernels (their per-thread accumulators allow two blocks per SM).
 static int ev_grid(Ctx* ctx, int64_t n) {
   const int64_t want = ceil_div(n, kEvThreads * 4);
   return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->num_sms * 2));
+}
+
+// Grid of the streaming kernels (update, norm, scale, combination): eight blocks per SM.
+static int ev_stream_grid(Ctx* ctx, int64_t n) {
+  const int64_t want = ceil_div(n, kEvThreads);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->num_sms * 8));
 }
 
 __device__ __forceinline__ bool ev_stopped(const int* stop, int step) {
@@ -93,7 +100,16 @@ __global__ void __launch_bounds__(kEvThreads) gs_update_kernel(int64_t n, const 
     hcol[threadIdx.x] = first_pass ? s_c[threadIdx.x] : vadd(hcol[threadIdx.x], s_c[threadIdx.x]);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     cplx wi = w[i];
-    for (int j = 0; j < J; ++j) wi = vsubmul(wi, s_c[j], V[(int64_t)j * ld + i]);
+    int j = 0;
+    for (; j + 4 <= J; j += 4) {  // four loads in flight, the updates still in j order
+      const cplx v0 = V[(int64_t)j * ld + i], v1 = V[(int64_t)(j + 1) * ld + i];
+      const cplx v2 = V[(int64_t)(j + 2) * ld + i], v3 = V[(int64_t)(j + 3) * ld + i];
+      wi = vsubmul(wi, s_c[j], v0);
+      wi = vsubmul(wi, s_c[j + 1], v1);
+      wi = vsubmul(wi, s_c[j + 2], v2);
+      wi = vsubmul(wi, s_c[j + 3], v3);
+    }
+    for (; j < J; ++j) wi = vsubmul(wi, s_c[j], V[(int64_t)j * ld + i]);
     w[i] = wi;
   }
 }
@@ -143,13 +159,31 @@ __global__ void __launch_bounds__(kEvThreads) ev_combine_kernel(int64_t n, const
   __syncthreads();
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     cplx acc = mkc(0.0, 0.0);
-    for (int j = 0; j < a; ++j) acc = vfma(s_e[j], V[(int64_t)j * ld + i], acc);
+    int j = 0;
+    for (; j + 4 <= a; j += 4) {  // four loads in flight, the sum still in j order
+      const cplx v0 = V[(int64_t)j * ld + i], v1 = V[(int64_t)(j + 1) * ld + i];
+      const cplx v2 = V[(int64_t)(j + 2) * ld + i], v3 = V[(int64_t)(j + 3) * ld + i];
+      acc = vfma(s_e[j], v0, acc);
+      acc = vfma(s_e[j + 1], v1, acc);
+      acc = vfma(s_e[j + 2], v2, acc);
+      acc = vfma(s_e[j + 3], v3, acc);
+    }
+    for (; j < a; ++j) acc = vfma(s_e[j], V[(int64_t)j * ld + i], acc);
     out[i] = acc;
   }
 }
 
+void ArnoldiBuffers::drop_graph() {
+  if (steps_exec) cudaGraphExecDestroy(steps_exec);
+  steps_exec = nullptr;
+  steps_m = steps_kind = 0;
+  steps_variant = -1;
+  steps_seen = -1;
+}
+
 void ArnoldiBuffers::ensure(int64_t n_, int m_, int grid, cudaStream_t stream) {
   if (n_ == n && m_ == m && grid <= grid_cap) return;
+  drop_graph();  // the buffers move
   n = n_;
   m = m_;
   ld = (n + 31) / 32 * 32;
@@ -173,7 +207,7 @@ static void arnoldi_steps(qd_ham* H, const MV* vals, ArnoldiBuffers& B, int step
   Ctx* ctx = H->ctx;
   Workspace& W = ham_workspace(H);
   const int64_t n = B.n;
-  const int g = ev_grid(ctx, n);
+  const int g = ev_grid(ctx, n), gs = ev_stream_grid(ctx, n);
   for (int idx = 1; idx <= steps; ++idx) {
     const cplx* vprev = B.V.p + (int64_t)(idx - 1) * B.ld;
     launch_spmv<MV, cplx>(ctx, H, vals, vprev, B.w.p, 1.0, nullptr, W.red_c(0), nullptr, B.stop.p, idx, -1);
@@ -190,17 +224,17 @@ static void arnoldi_steps(qd_ham* H, const MV* vals, ArnoldiBuffers& B, int step
                                                                 B.tickets.p, B.proj.p, B.stop.p, idx);
       QD_CHECK_LAUNCH();
       QD_LAUNCHED(ctx);
-      gs_update_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, idx, B.proj.p, B.w.p, hcol, pass == 0,
-                                                           B.stop.p, idx);
+      gs_update_kernel<<<gs, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, idx, B.proj.p, B.w.p, hcol, pass == 0,
+                                                            B.stop.p, idx);
       QD_CHECK_LAUNCH();
       QD_LAUNCHED(ctx);
     }
-    ev_norm_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, B.w.p, B.nrm2.p + idx, B.nrm.p + idx,
-                                                       GridRed<double>{B.rpart.p, B.tickets.p + 1}, B.stop.p, idx);
+    ev_norm_kernel<<<gs, kEvThreads, 0, ctx->stream>>>(n, B.w.p, B.nrm2.p + idx, B.nrm.p + idx,
+                                                        GridRed<double>{B.rpart.p, B.tickets.p + 1}, B.stop.p, idx);
     QD_CHECK_LAUNCH();
     QD_LAUNCHED(ctx);
-    ev_scale_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, B.w.p, B.nrm.p + idx, B.V.p + (int64_t)idx * B.ld,
-                                                        B.stop.p, idx);
+    ev_scale_kernel<<<gs, kEvThreads, 0, ctx->stream>>>(n, B.w.p, B.nrm.p + idx, B.V.p + (int64_t)idx * B.ld,
+                                                         B.stop.p, idx);
     QD_CHECK_LAUNCH();
     QD_LAUNCHED(ctx);
   }
@@ -223,10 +257,50 @@ void arnoldi_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int 
   QD_LAUNCHED(ctx);
   QD_CUDA(cudaMemsetAsync(B.stop.p, 0, sizeof(int), ctx->stream));
   const int steps = m - 1;  // updateKrylovRepr(H, kry_dim_rt - 1)
-  if (H->flags & QD_HAM_REAL)
-    arnoldi_steps<double>(H, H->vals_r.p, B, steps);
-  else
-    arnoldi_steps<cplx>(H, H->vals_c.p, B, steps);
+  const bool real = (H->flags & QD_HAM_REAL) != 0;
+  auto run_steps = [&]() {
+    if (real) arnoldi_steps<double>(H, H->vals_r.p, B, steps);
+    else arnoldi_steps<cplx>(H, H->vals_c.p, B, steps);
+  };
+  const int kind = real ? 1 : 2;
+  // one uncaptured run per (m, value type, product kernel) first: the product's workspace and
+  // tables are allocated on first use, which a capture does not allow
+  const long long key = ((long long)H->spmv_variant << 16) | ((long long)kind << 8) | (long long)m;
+  if (H->one_shot || B.steps_seen != key) {  // a served request is solved once: no capture
+    run_steps();
+    B.steps_seen = key;
+  } else {
+    const void* vals = real ? (const void*)H->vals_r.p : (const void*)H->vals_c.p;
+    if (!B.steps_exec || B.steps_m != m || B.steps_kind != kind || B.steps_variant != H->spmv_variant ||
+        B.steps_vals != vals || B.steps_rowptr != (const void*)H->rowptr.p) {
+      if (B.steps_exec) cudaGraphExecDestroy(B.steps_exec);
+      B.steps_exec = nullptr;
+      cudaGraph_t gr = nullptr;
+      const int64_t before = ctx->launches;
+      QD_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      try {
+        run_steps();
+      } catch (...) {
+        cudaStreamEndCapture(ctx->stream, &gr);
+        if (gr) cudaGraphDestroy(gr);
+        ctx->launches = before;
+        throw;
+      }
+      QD_CUDA(cudaStreamEndCapture(ctx->stream, &gr));
+      B.steps_kernels = ctx->launches - before;
+      ctx->launches = before;
+      const cudaError_t e = cudaGraphInstantiate(&B.steps_exec, gr, 0);
+      cudaGraphDestroy(gr);
+      QD_CUDA(e);
+      B.steps_m = m;
+      B.steps_kind = kind;
+      B.steps_variant = H->spmv_variant;
+      B.steps_vals = vals;
+      B.steps_rowptr = H->rowptr.p;
+    }
+    QD_CUDA(cudaGraphLaunch(B.steps_exec, ctx->stream));
+    ctx->launches += B.steps_kernels;
+  }
   std::vector<cplx> hc((size_t)(m + 1) * 64);
   std::vector<double> nrm(m + 2);
   int stop = 0;
@@ -250,7 +324,7 @@ void arnoldi_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int 
   std::vector<cplx> e(act);
   for (int j = 0; j < act; ++j) e[j] = mkc(E[j].real(), E[j].imag());
   QD_CUDA(cudaMemcpyAsync(B.e.p, e.data(), act * sizeof(cplx), cudaMemcpyHostToDevice, ctx->stream));
-  ev_combine_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, act, B.e.p, psi_out);
+  ev_combine_kernel<<<ev_stream_grid(ctx, n), kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, act, B.e.p, psi_out);
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
   QD_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -20,7 +20,17 @@ struct ArnoldiBuffers {
   DBuf<cplx> partials;  // grid x 32 multi-dot partials
   DBuf<double> rpart;
   DBuf<unsigned> tickets;
+  // the m - 1 Arnoldi steps captured once and replayed (they read and write only these
+  // buffers and the Hamiltonian's arrays, so the graph stays valid while neither changes)
+  cudaGraphExec_t steps_exec = nullptr;
+  int steps_m = 0, steps_kind = 0, steps_variant = -1;
+  const void* steps_vals = nullptr;  // the matrix arrays the graph reads
+  const void* steps_rowptr = nullptr;
+  long long steps_seen = -1;  // key of the last uncaptured run (its lazy allocations are done)
+  int64_t steps_kernels = 0;
   void ensure(int64_t n_, int m_, int grid, cudaStream_t stream);
+  void drop_graph();
+  ~ArnoldiBuffers() { drop_graph(); }
 };
 
 void arnoldi_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int m, int* act_out);
