@@ -88,6 +88,67 @@ __global__ void __launch_bounds__(kEvThreads) multidot_kernel(int64_t n, const c
   if (threadIdx.x == 0) *ticket = 0u;
 }
 
+// The same inner products with w staged in shared memory tile by tile and a
+// warp per basis vector inside a tile (two accumulators per lane, four loads of
+// V_j in flight): one complex accumulator pair per thread instead of J, so the
+// kernel runs many more warps per SM than multidot_kernel.  Each tile's warp
+// sums are added to the block's partial in tile order and the blocks' partials
+// in block order: deterministic.
+constexpr int kDotTile = 2048;  // complex elements of w per tile (32 KB)
+
+__global__ void __launch_bounds__(kEvThreads) multidot_tile_kernel(int64_t n, const cplx* __restrict__ V, int64_t ld,
+                                                                   int J, const cplx* __restrict__ w,
+                                                                   cplx* partials, unsigned* ticket, cplx* out,
+                                                                   const int* stop, int step) {
+  if (ev_stopped(stop, step)) return;
+  __shared__ cplx ws[kDotTile];
+  __shared__ cplx part[32];
+  __shared__ bool last;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = kEvThreads / 32;
+  if (threadIdx.x < 32) part[threadIdx.x] = mkc(0.0, 0.0);
+  for (int64_t t0 = (int64_t)blockIdx.x * kDotTile; t0 < n; t0 += (int64_t)gridDim.x * kDotTile) {
+    const int tn = (int)std::min<int64_t>(kDotTile, n - t0);
+    __syncthreads();  // the previous tile's readers are done (and part is zeroed)
+    for (int i = threadIdx.x; i < tn; i += kEvThreads) ws[i] = w[t0 + i];
+    __syncthreads();
+    for (int j = warp; j < J; j += nw) {
+      const cplx* vj = V + (int64_t)j * ld + t0;
+      cplx a0 = mkc(0.0, 0.0), a1 = mkc(0.0, 0.0);
+      int i = lane;
+      for (; i + 96 < tn; i += 128) {
+        const cplx x0 = vj[i], x1 = vj[i + 32], x2 = vj[i + 64], x3 = vj[i + 96];
+        a0 = vdotfma(x0, ws[i], a0);
+        a1 = vdotfma(x1, ws[i + 32], a1);
+        a0 = vdotfma(x2, ws[i + 64], a0);
+        a1 = vdotfma(x3, ws[i + 96], a1);
+      }
+      for (; i < tn; i += 32) a0 = vdotfma(vj[i], ws[i], a0);
+      const cplx t = warp_sum(vadd(a0, a1));
+      if (lane == 0) part[j] = vadd(part[j], t);  // one warp owns vector j: no race
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) partials[(int64_t)blockIdx.x * 32 + threadIdx.x] = part[threadIdx.x];
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (threadIdx.x < J) {
+    cplx t = mkc(0.0, 0.0);
+    for (unsigned b = 0; b < gridDim.x; ++b) t = vadd(t, ld_cg(partials + (int64_t)b * 32 + threadIdx.x));
+    out[threadIdx.x] = t;
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
+}
+
+// Grid of multidot_tile_kernel: one tile per block at most, up to six blocks per SM.
+static int ev_tile_grid(Ctx* ctx, int64_t n) {
+  const int64_t want = ceil_div(n, kDotTile);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)ctx->num_sms * 6));
+}
+
 // w -= sum_{j<J} c_j V_j;  acc_h[j] += c_j (the Hessenberg column gathers both passes)
 __global__ void __launch_bounds__(kEvThreads) gs_update_kernel(int64_t n, const cplx* __restrict__ V, int64_t ld,
                                                                int J, const cplx* c, cplx* __restrict__ w,
@@ -207,21 +268,14 @@ static void arnoldi_steps(qd_ham* H, const MV* vals, ArnoldiBuffers& B, int step
   Ctx* ctx = H->ctx;
   Workspace& W = ham_workspace(H);
   const int64_t n = B.n;
-  const int g = ev_grid(ctx, n), gs = ev_stream_grid(ctx, n);
+  const int gs = ev_stream_grid(ctx, n), gt = ev_tile_grid(ctx, n);
   for (int idx = 1; idx <= steps; ++idx) {
     const cplx* vprev = B.V.p + (int64_t)(idx - 1) * B.ld;
     launch_spmv<MV, cplx>(ctx, H, vals, vprev, B.w.p, 1.0, nullptr, W.red_c(0), nullptr, B.stop.p, idx, -1);
     cplx* hcol = B.hcol.p + (int64_t)(idx - 1) * 64;
     for (int pass = 0; pass < 2; ++pass) {
-      if (idx <= 8)
-        multidot_kernel<8><<<g, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, idx, B.w.p, B.partials.p,
+      multidot_tile_kernel<<<gt, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, idx, B.w.p, B.partials.p,
                                                                B.tickets.p, B.proj.p, B.stop.p, idx);
-      else if (idx <= 16)
-        multidot_kernel<16><<<g, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, idx, B.w.p, B.partials.p,
-                                                                B.tickets.p, B.proj.p, B.stop.p, idx);
-      else
-        multidot_kernel<32><<<g, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, idx, B.w.p, B.partials.p,
-                                                                B.tickets.p, B.proj.p, B.stop.p, idx);
       QD_CHECK_LAUNCH();
       QD_LAUNCHED(ctx);
       gs_update_kernel<<<gs, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, idx, B.proj.p, B.w.p, hcol, pass == 0,
@@ -247,7 +301,7 @@ void arnoldi_evolve(qd_ham* H, const cplx* psi_in, cplx* psi_out, double h, int 
   if (!H->arnoldi) H->arnoldi.reset(new ArnoldiBuffers());
   ArnoldiBuffers& B = *H->arnoldi;
   const int g = ev_grid(ctx, n);
-  B.ensure(n, m, g, ctx->stream);
+  B.ensure(n, m, std::max(g, ev_tile_grid(ctx, n)), ctx->stream);
   // v_0 = psi / ||psi||
   ev_norm_only_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, psi_in, B.nrm2.p, GridRed<double>{B.rpart.p, B.tickets.p + 1});
   QD_CHECK_LAUNCH();
