@@ -44,56 +44,11 @@ __device__ __forceinline__ bool ev_stopped(const int* stop, int step) {
   return st != 0 && st < step;
 }
 
-// out[j] = <V_j, w> for j < J (J <= JB); deterministic grid reduction.
-template <int JB>
-__global__ void __launch_bounds__(kEvThreads) multidot_kernel(int64_t n, const cplx* __restrict__ V, int64_t ld,
-                                                              int J, const cplx* __restrict__ w, cplx* partials,
-                                                              unsigned* ticket, cplx* out, const int* stop,
-                                                              int step) {
-  if (ev_stopped(stop, step)) return;
-  __shared__ cplx s_part[kEvThreads / 32][JB];
-  __shared__ bool last;
-  cplx acc[JB];
-#pragma unroll
-  for (int j = 0; j < JB; ++j) acc[j] = mkc(0.0, 0.0);
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const cplx wi = w[i];
-#pragma unroll
-    for (int j = 0; j < JB; ++j)
-      if (j < J) acc[j] = vdotfma(V[(int64_t)j * ld + i], wi, acc[j]);
-  }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int j = 0; j < JB; ++j) {
-    const cplx v = warp_sum(acc[j]);
-    if (lane == 0) s_part[warp][j] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < JB) {
-    cplx b = mkc(0.0, 0.0);
-    for (int q = 0; q < kEvThreads / 32; ++q) b = vadd(b, s_part[q][threadIdx.x]);
-    partials[(int64_t)blockIdx.x * JB + threadIdx.x] = b;
-  }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  if (threadIdx.x < J) {
-    cplx t = mkc(0.0, 0.0);
-    for (unsigned b = 0; b < gridDim.x; ++b) t = vadd(t, ld_cg(partials + (int64_t)b * JB + threadIdx.x));
-    out[threadIdx.x] = t;
-  }
-  if (threadIdx.x == 0) *ticket = 0u;
-}
-
-// The same inner products with w staged in shared memory tile by tile and a
-// warp per basis vector inside a tile (two accumulators per lane, four loads of
-// V_j in flight): one complex accumulator pair per thread instead of J, so the
-// kernel runs many more warps per SM than multidot_kernel.  Each tile's warp
-// sums are added to the block's partial in tile order and the blocks' partials
-// in block order: deterministic.
+// out[j] = <V_j, w> for j < J (J <= 32): w staged in shared memory tile by tile
+// and a warp per basis vector inside a tile (two accumulators per lane, four
+// loads of V_j in flight), so a thread holds one complex accumulator pair, not
+// J, and six blocks fit an SM.  Each tile's warp sums are added to the block's
+// partial in tile order and the blocks' partials in block order: deterministic.
 constexpr int kDotTile = 2048;  // complex elements of w per tile (32 KB)
 
 __global__ void __launch_bounds__(kEvThreads) multidot_tile_kernel(int64_t n, const cplx* __restrict__ V, int64_t ld,
@@ -462,16 +417,16 @@ static void arnoldi_ground_steps(qd_ham* H, const MV* vals, ArnoldiGround& B, in
   Ctx* ctx = H->ctx;
   Workspace& W = ham_workspace(H);
   const int64_t n = B.n;
-  const int g = ev_grid(ctx, n);
+  const int g = ev_grid(ctx, n), gt = ev_tile_grid(ctx, n);
   for (int idx = first; idx <= last; ++idx) {
     const cplx* vprev = B.V.p + (int64_t)(idx - 1) * B.ld;
     launch_spmv<MV, cplx>(ctx, H, vals, vprev, B.w.p, 1.0, nullptr, W.red_c(0), nullptr, B.stop.p, idx, -1);
     cplx* hcol = B.hcol.p + (int64_t)(idx - 1) * B.ldh;
     for (int pass = 0; pass < 2; ++pass) {
       for (int j0 = 0; j0 < idx; j0 += 32) {
-        multidot_kernel<32><<<g, kEvThreads, 0, ctx->stream>>>(n, B.V.p + (int64_t)j0 * B.ld, B.ld,
-                                                                std::min(32, idx - j0), B.w.p, B.partials.p,
-                                                                B.tickets.p, B.proj.p + j0, B.stop.p, idx);
+        multidot_tile_kernel<<<gt, kEvThreads, 0, ctx->stream>>>(n, B.V.p + (int64_t)j0 * B.ld, B.ld,
+                                                                 std::min(32, idx - j0), B.w.p, B.partials.p,
+                                                                 B.tickets.p, B.proj.p + j0, B.stop.p, idx);
         QD_CHECK_LAUNCH();
         QD_LAUNCHED(ctx);
       }
@@ -504,7 +459,7 @@ void arnoldi_ground(qd_ham* H, cplx* psi, int kdim, int add_dim, bool extend, do
   } else {
     if (!H->arnoldi_gs) H->arnoldi_gs.reset(new ArnoldiGround());
     ArnoldiGround& B = *H->arnoldi_gs;
-    B.ensure(n, kdim, g, ctx->stream);
+    B.ensure(n, kdim, std::max(g, ev_tile_grid(ctx, n)), ctx->stream);
     B.act = 0;
     B.open = true;
     B.broke = false;
