@@ -368,7 +368,17 @@ __global__ void __launch_bounds__(kEvThreads) gs_update_long_kernel(int64_t n, c
     __syncthreads();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
       cplx wi = w[i];
-      for (int j = 0; j < jc; ++j) wi = vsubmul(wi, s_c[j], V[(int64_t)(j0 + j) * ld + i]);
+      const cplx* vp = V + (int64_t)j0 * ld + i;
+      int j = 0;
+      for (; j + 4 <= jc; j += 4) {  // four loads in flight, the updates still in j order
+        const cplx v0 = vp[(int64_t)j * ld], v1 = vp[(int64_t)(j + 1) * ld];
+        const cplx v2 = vp[(int64_t)(j + 2) * ld], v3 = vp[(int64_t)(j + 3) * ld];
+        wi = vsubmul(wi, s_c[j], v0);
+        wi = vsubmul(wi, s_c[j + 1], v1);
+        wi = vsubmul(wi, s_c[j + 2], v2);
+        wi = vsubmul(wi, s_c[j + 3], v3);
+      }
+      for (; j < jc; ++j) wi = vsubmul(wi, s_c[j], vp[(int64_t)j * ld]);
       w[i] = wi;
     }
   }
@@ -385,7 +395,17 @@ __global__ void __launch_bounds__(kEvThreads) ev_combine_long_kernel(int64_t n, 
     __syncthreads();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
       cplx acc = (j0 == 0) ? mkc(0.0, 0.0) : out[i];
-      for (int j = 0; j < jc; ++j) acc = vfma(s_e[j], V[(int64_t)(j0 + j) * ld + i], acc);
+      const cplx* vp = V + (int64_t)j0 * ld + i;
+      int j = 0;
+      for (; j + 4 <= jc; j += 4) {  // four loads in flight, the sum still in j order
+        const cplx v0 = vp[(int64_t)j * ld], v1 = vp[(int64_t)(j + 1) * ld];
+        const cplx v2 = vp[(int64_t)(j + 2) * ld], v3 = vp[(int64_t)(j + 3) * ld];
+        acc = vfma(s_e[j], v0, acc);
+        acc = vfma(s_e[j + 1], v1, acc);
+        acc = vfma(s_e[j + 2], v2, acc);
+        acc = vfma(s_e[j + 3], v3, acc);
+      }
+      for (; j < jc; ++j) acc = vfma(s_e[j], vp[(int64_t)j * ld], acc);
       out[i] = acc;
     }
   }
@@ -417,7 +437,7 @@ static void arnoldi_ground_steps(qd_ham* H, const MV* vals, ArnoldiGround& B, in
   Ctx* ctx = H->ctx;
   Workspace& W = ham_workspace(H);
   const int64_t n = B.n;
-  const int g = ev_grid(ctx, n), gt = ev_tile_grid(ctx, n);
+  const int gs = ev_stream_grid(ctx, n), gt = ev_tile_grid(ctx, n);
   for (int idx = first; idx <= last; ++idx) {
     const cplx* vprev = B.V.p + (int64_t)(idx - 1) * B.ld;
     launch_spmv<MV, cplx>(ctx, H, vals, vprev, B.w.p, 1.0, nullptr, W.red_c(0), nullptr, B.stop.p, idx, -1);
@@ -430,17 +450,17 @@ static void arnoldi_ground_steps(qd_ham* H, const MV* vals, ArnoldiGround& B, in
         QD_CHECK_LAUNCH();
         QD_LAUNCHED(ctx);
       }
-      gs_update_long_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, idx, B.proj.p, B.w.p, hcol, pass == 0,
-                                                                B.stop.p, idx);
+      gs_update_long_kernel<<<gs, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, idx, B.proj.p, B.w.p, hcol,
+                                                                 pass == 0, B.stop.p, idx);
       QD_CHECK_LAUNCH();
       QD_LAUNCHED(ctx);
     }
-    ev_norm_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, B.w.p, B.nrm2.p + idx, B.nrm.p + idx,
-                                                       GridRed<double>{B.rpart.p, B.tickets.p + 1}, B.stop.p, idx);
+    ev_norm_kernel<<<gs, kEvThreads, 0, ctx->stream>>>(n, B.w.p, B.nrm2.p + idx, B.nrm.p + idx,
+                                                        GridRed<double>{B.rpart.p, B.tickets.p + 1}, B.stop.p, idx);
     QD_CHECK_LAUNCH();
     QD_LAUNCHED(ctx);
-    ev_scale_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, B.w.p, B.nrm.p + idx, B.V.p + (int64_t)idx * B.ld,
-                                                        B.stop.p, idx);
+    ev_scale_kernel<<<gs, kEvThreads, 0, ctx->stream>>>(n, B.w.p, B.nrm.p + idx, B.V.p + (int64_t)idx * B.ld,
+                                                         B.stop.p, idx);
     QD_CHECK_LAUNCH();
     QD_LAUNCHED(ctx);
   }
@@ -513,7 +533,7 @@ void arnoldi_ground(qd_ham* H, cplx* psi, int kdim, int add_dim, bool extend, do
   std::vector<cplx> yc(act);
   for (int j = 0; j < act; ++j) yc[j] = mkc(y[j], 0.0);
   QD_CUDA(cudaMemcpyAsync(B.e.p, yc.data(), act * sizeof(cplx), cudaMemcpyHostToDevice, ctx->stream));
-  ev_combine_long_kernel<<<g, kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, act, B.e.p, psi);
+  ev_combine_long_kernel<<<ev_stream_grid(ctx, n), kEvThreads, 0, ctx->stream>>>(n, B.V.p, B.ld, act, B.e.p, psi);
   QD_CHECK_LAUNCH();
   QD_LAUNCHED(ctx);
   QD_CUDA(cudaStreamSynchronize(ctx->stream));
