@@ -533,9 +533,25 @@ def batched_sweep(ctx, n_inst=512, steps=80, seed=2024, chain_L=None):
     plain_s = time.perf_counter() - t0
     rel = np.abs(out[:, 1] - plain_e) / np.abs(plain_e)
     lset = "{14,16,18,20}" if chain_L is None else "{%d}" % chain_L
+    # the device's own span of the call (out[:, 5:7]: each instance's start and end, ns) and the
+    # reorthogonalisation's bytes: two passes over the stored FP32 basis, act (act + 1) / 2 vectors each
+    span_s = (out[:, 6].max() - out[:, 5].min()) * 1e-9
+    act = out[:, 3]
+    dimf = np.array(dims, dtype=float)
+    nnzf = np.array([float(h.nnz) for h in hams])
+    reorth_bytes = float(np.sum(act * (act + 1) * dimf * 4.0))
+    # per step k, as the kernel table counts it: the FP32 CSR product (nnz 8 B) and (2k + 3) vector
+    # passes of dim 4 B (the basis read twice, w, v1, v2)
+    step_bytes = float(np.sum(act * nnzf * 8.0 + (act * (act + 1) + 3 * act) * dimf * 4.0))
+    hbm_peak, _ = peaks()
     return {"workload": f"{n_inst} random-field XXZ chains L in {lset}, {steps} Lanczos steps",
             "mixed_solves_per_s": n_inst / mixed_s, "plain_fp64_solves_per_s": n_inst / plain_s,
             "speedup": plain_s / mixed_s, "max_rel_dE": float(rel.max()), "median_rel_dE": float(np.median(rel)),
+            "device_span_ms": span_s * 1e3, "algorithmic_step_bytes": step_bytes,
+            "step_bytes_frac_of_measured_hbm": step_bytes / span_s / 1e9 / hbm_peak,
+            "reorth_basis_bytes": reorth_bytes,
+            "reorth_GBps_over_device_span": reorth_bytes / span_s / 1e9,
+            "reorth_frac_of_measured_hbm": reorth_bytes / span_s / 1e9 / hbm_peak,
             "lowering_s_all_instances": lower_s, "mixed_form": "fp32 products/basis, fp64 accumulation, "
             "full reorthogonalisation, device tridiagonal, fp64 Rayleigh refinement; one persistent launch",
             "plain_form": "fp64 Lanczos (reference algorithm), one solve after another"}
