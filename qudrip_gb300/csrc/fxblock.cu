@@ -348,19 +348,34 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) lz_fx_blkstep_kerne
   // first half: w = s1 (d x + c 2^-F sum X) and the three dots
   const double sc = *a.s1;
   Tri<double> acc = vzero(Tri<double>{});
+  // per buffer: the parity of its next phase and whether a copy into it is in flight (the same
+  // values in every thread: each wait's outcome is agreed by the whole block)
   unsigned par0 = 0, par1 = 0;
+  bool out0 = g0 < g1, out1 = false;
   for (int g = g0; g < g1; ++g) {
     const int buf = (g - g0) & 1;
     __int128* xs = buf ? xs1 : xs0;
-    if (threadIdx.x == 0 && g + 1 < g1) {  // the other buffer's readers passed the barrier below
-      const int2 nx = P.groups[g + 1];
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      blk_issue_copy(buf ? xs0 : xs1, B.X + nx.x, nx.y - nx.x, &bar[buf ^ 1]);
+    if (g + 1 < g1) {  // the other buffer's readers passed the barrier below
+      if (threadIdx.x == 0) {
+        const int2 nx = P.groups[g + 1];
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        blk_issue_copy(buf ? xs0 : xs1, B.X + nx.x, nx.y - nx.x, &bar[buf ^ 1]);
+      }
+      if (buf) out0 = true;
+      else out1 = true;
     }
-    const bool ok = blk_wait(&bar[buf], buf ? par1 : par0);
-    if (buf) par1 ^= 1u;
-    else par0 ^= 1u;
-    if (!ok) copy_bad = 1;
+    if (!__syncthreads_and(blk_wait(&bar[buf], buf ? par1 : par0))) {
+      // a copy that did not land: flag the solve and stop issuing or reading copies
+      if (threadIdx.x == 0) copy_bad = 1;
+      break;
+    }
+    if (buf) {
+      par1 ^= 1u;
+      out1 = false;
+    } else {
+      par0 ^= 1u;
+      out0 = false;
+    }
     const int2 gr = P.groups[g];
     for (int r = gr.x + (int)threadIdx.x; r < gr.y; r += blockDim.x) {
       const __int128 s = B.row_sum_staged(r, xs, gr.x);
@@ -376,6 +391,11 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) lz_fx_blkstep_kerne
     }
     __syncthreads();
   }
+  // copies still in flight (only after a wait ran out) get one more bounded wait before the
+  // block moves on, so none lands after the block has left
+  if (out0) blk_wait(&bar[0], par0);
+  if (out1) blk_wait(&bar[1], par1);
+  __syncthreads();
   if (threadIdx.x == 0 && copy_bad) atomicExch(a.ovf + 1, 1);
   if (grid_sum(acc, a.red, a.dots) && threadIdx.x == 0) {
     const Tri<double> d = *a.dots;
