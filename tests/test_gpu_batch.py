@@ -194,3 +194,38 @@ def test_batch_one_state_and_empty_instances(ctx):
     with pytest.raises(A.QDError) as e:
         q.batch_lanczos([He], [np.ones(0)], 10)
     assert e.value.code == A.QD_ERR_INVALID
+
+
+def test_full_disorder_sweep_within_tolerance_of_fp64(ctx):
+    """The batched workload at its full size: 512 random-field XXZ chains (L drawn from
+    {14, 16, 18, 20}, h_i ~ U[-2, 2], periodic, Sz = 0), 80 steps each, in one call; every refined
+    energy within 1e-8 relative of the plain FP64 Lanczos solve of the same instance and start
+    vector, and the device clock columns consistent (every instance starts and ends inside the
+    call, on the CTAs its size asks for)."""
+    rng = np.random.Generator(np.random.PCG64(2024))
+    hams, v0s, dims = [], [], []
+    for i in range(512):
+        L = int(rng.choice([14, 16, 18, 20]))
+        h = rng.uniform(-2.0, 2.0, L)
+        spec, ham = chains.xxz_chain(L, 1.0, 1.0, True, h)
+        sec = q.Sector(spec.index, spec.constraints)
+        H = sec.lower(ham)
+        H._keep = sec
+        hams.append(H)
+        v0s.append(q.start_vector(sec.dim, 2024 + i))
+        dims.append(sec.dim)
+    out = q.batch_lanczos(hams, v0s, 80)
+    worst = 0.0
+    states = {}
+    for i, H in enumerate(hams):
+        st = states.get(dims[i])
+        if st is None:
+            st = states[dims[i]] = q.getState(H._keep, 1)
+        st.set(0, v0s[i])
+        e = q.Arnoldi.getLanczosSolver(H._keep, 80).getGroundState(H, st(0), 0).ritz_value
+        worst = max(worst, abs(out[i, 1] - e) / abs(e))
+    assert worst <= DE_TOL, worst
+    big = np.array(dims) >= 32768
+    assert np.all(out[big, 7] >= 2) and np.all(out[~big, 7] == 1)
+    assert np.all(out[:, 6] > out[:, 5])
+    assert out[:, 6].max() - out[:, 5].min() < 5e9  # the whole call inside five seconds of device time
