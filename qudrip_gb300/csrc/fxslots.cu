@@ -214,7 +214,7 @@ __global__ void __launch_bounds__(256, 6) spmv_fx_slots_dots_kernel(
       acc.c = fma(xr, v2, acc.c);
     }
   }
-  if (grid_sum(acc, red, dots) && threadIdx.x == 0) {
+  if (grid_sum_ordered(acc, red, dots) && threadIdx.x == 0) {
     const Tri<double> d = *dots;
     const double bt = kHas2 ? (*s2) * d.a : 0.0;
     double t = d.b;

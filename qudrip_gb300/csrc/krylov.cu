@@ -512,9 +512,9 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   const FxForm* step_form = mfx ? H->mfx.get() : ((fx && spmv == QD_SPMV_CSR) ? H->fx.get() : nullptr);
   if (!fx_one_launch_step()) step_form = nullptr;
   DBuf<__int128> X2(step_form ? n + 32 : 1);
-  DBuf<unsigned> ep(1);
+  DBuf<unsigned> ep(4);
   DBuf<int> flags(2);
-  QD_CUDA(cudaMemsetAsync(ep.p, 0, sizeof(unsigned), ctx->stream));
+  QD_CUDA(cudaMemsetAsync(ep.p, 0, 4 * sizeof(unsigned), ctx->stream));
   QD_CUDA(cudaMemsetAsync(flags.p, 0, 2 * sizeof(int), ctx->stream));
   bool stepped = false;
   auto launch = [&]() {
@@ -631,6 +631,8 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int k_
   // two-launch step
   const bool one_launch = fxk == 1 && fx_one_launch_step() && !H->one_shot;
   if (fxk == 1 && !one_launch) form->step_fused = -1;
+  // the step's barrier counters start every run at zero (each launch also leaves them so)
+  if (one_launch) QD_CUDA(cudaMemsetAsync(B.epoch.p, 0, 4 * sizeof(unsigned), ctx->stream));
   for (int k = k_first; k <= k_last; ++k) {
     const VV* V1 = B.V.p + (int64_t)(k - 1) * B.ld;
     const VV* V2 = (k >= 2) ? B.V.p + (int64_t)(k - 2) * B.ld : nullptr;

@@ -28,7 +28,7 @@ struct LanczosBuffers {
   DBuf<int> stop;
   DBuf<__int128> X;  // fixed-point copies of the two newest basis vectors (uniform-coupling product)
   DBuf<int> ovf;         // [0] a vector left the fixed-point range, [1] a bounded device wait ran out
-  DBuf<unsigned> epoch;  // barrier word of the one-launch step (fxstep.cuh)
+  DBuf<unsigned> epoch;  // barrier counters of the one-launch steps (fxstep.cuh, fxblock.cu)
   cudaGraphExec_t exec = nullptr;
   int kind = 0;  // product the captured graph launches (0 CSR, 1 matrix-free, 2 fixed-point, +4 one-launch step)
   int done = 0;  // Lanczos steps run on the stored basis (incremental solves continue from here)
@@ -36,8 +36,8 @@ struct LanczosBuffers {
     if (!X.p) {
       X.alloc((size_t)2 * ld);
       ovf.alloc(2);
-      epoch.alloc(1);
-      QD_CUDA(cudaMemsetAsync(epoch.p, 0, sizeof(unsigned), s));
+      epoch.alloc(4);
+      QD_CUDA(cudaMemsetAsync(epoch.p, 0, 4 * sizeof(unsigned), s));
     }
   }
   int64_t graph_kernels = 0;
