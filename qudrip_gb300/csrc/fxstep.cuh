@@ -7,10 +7,11 @@
 // ramp and tail.  Here one cooperative launch does both halves: every thread
 // keeps the w of its own rows in shared memory (rows r = gtid + i * stride,
 // slot i * 256 + tid), the last block to post its partials of the three dots
-// forms their total in one fixed order, publishes alpha and beta and bumps an
-// epoch word, every block waits for the epoch (a bounded wait), and then
-// updates the same rows it produced (in adjacent pairs, for 16-byte accesses): reads v1, v2, writes
-// v_k, its fixed-point copy for the next product, and its share of ||v_k||^2.
+// forms their total (one level: all its threads load the partials at once),
+// publishes alpha and beta and bumps an epoch word, every block waits for the
+// epoch (a bounded wait), and then updates the same rows it produced (in
+// adjacent pairs, for 16-byte accesses): reads v1, v2, writes v_k, its
+// fixed-point copy for the next product, and its share of ||v_k||^2.
 //
 // Per-element arithmetic is that of spmv_fx_dots_kernel + lz_update_kernel,
 // and the dots use the same grid, row order and reduction order
@@ -99,9 +100,9 @@ __global__ void __launch_bounds__(256, 6) lz_fx_step_kernel(Src src, FxStepArgs 
       acc.c = fma(xr, v2, acc.c);
     }
   }
-  // The three dots: every block posts its partial; the last to post forms the total in
-  // grid_sum_ordered's fixed order (one warp, no second level), stores alpha and beta and
-  // bumps the epoch word; every block waits for the epoch (a bounded wait).
+  // The three dots: every block posts its partial; the last to post forms the total (one
+  // level, all its threads loading the partials at once), stores alpha and beta and bumps
+  // the epoch word; every block waits for the epoch (a bounded wait).
   if (grid_sum_ordered(acc, a.red, a.dots) && threadIdx.x == 0) {
     const Tri<double> d = *a.dots;
     const double bt = kHas2 ? (*a.s2) * d.a : 0.0;

@@ -151,22 +151,12 @@ __device__ __forceinline__ bool grid_sum_flat(T v, GridRed<T> R, T* total) {
   return true;
 }
 
-// The total of G block partials in one fixed order: lane l of the calling warp
-// adds partials l, l + 32, ... in turn, then the warp's butterfly; lane 0's value
-// is the result.  Any block that calls it on the same partials gets the same bits.
-template <typename T>
-__device__ __forceinline__ T ordered_warp_total(const T* partials, int G) {
-  const int lane = threadIdx.x & 31;
-  T acc = vzero(T{});
-#pragma unroll 4
-  for (int i = lane; i < G; i += 32) acc = vadd(acc, ld_cg(partials + i));
-  return warp_sum(acc);
-}
-
-// A grid reduction whose total is ordered_warp_total of the block partials:
-// the last block to arrive forms it (warp 0) and returns true in all its threads;
-// thread 0 of it writes *total.  The one-launch Lanczos step forms the same total
-// in every block, so both forms of the step carry the same bits.
+// A one-level grid reduction for the Lanczos step's inner products: every block
+// posts its block total; the last block to arrive loads all the partials at once
+// (thread t takes partials t, t + blockDim, ... in turn) and forms the total with
+// one block sum, returning true in all its threads; thread 0 of it writes *total.
+// The one-launch step and the two-launch products both reduce their dots this
+// way, so both forms of the step carry the same bits.
 template <typename T>
 __device__ __forceinline__ bool grid_sum_ordered(T v, GridRed<T> R, T* total) {
   __shared__ T smem_o[32];
@@ -180,12 +170,12 @@ __device__ __forceinline__ bool grid_sum_ordered(T v, GridRed<T> R, T* total) {
   __syncthreads();
   if (!last_o) return false;
   __threadfence();
-  if (threadIdx.x < 32) {
-    const T tot = ordered_warp_total(R.partials, (int)gridDim.x);
-    if (threadIdx.x == 0) {
-      *total = tot;
-      *R.ticket = 0u;
-    }
+  T acc = vzero(v);
+  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) acc = vadd(acc, ld_cg(R.partials + i));
+  const T tot = block_sum(acc, smem_o);
+  if (threadIdx.x == 0) {
+    *total = tot;
+    *R.ticket = 0u;
   }
   return true;
 }
