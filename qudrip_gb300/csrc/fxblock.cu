@@ -404,8 +404,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) lz_fx_blkstep_kerne
     if (kHas2) t = fma(-(bt * (*a.s2)), d.c, t);
     *a.beta = bt;
     *a.alpha = (*a.s1) * t;
-    __threadfence();
-    if (!a.hold_epoch) atomicAdd(a.epoch, 1u);
+    if (!a.hold_epoch) epoch_release_add(a.epoch);
   }
   if (threadIdx.x == 0) {
     const unsigned limit = a.spin_limit ? a.spin_limit : kStepSpinLimit;
@@ -418,7 +417,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) lz_fx_blkstep_kerne
       }
       __nanosleep(200);
     }
-    __threadfence();
+    fence_acq_rel_gpu();
     ab[0] = __ldcg(a.alpha);
     ab[1] = __ldcg(a.beta);
   }

@@ -72,9 +72,11 @@ __global__ void __launch_bounds__(256, 6) lz_fx_step_kernel(Src src, FxStepArgs 
   __shared__ unsigned e0;
   __shared__ int waited_out;
   __shared__ double ab[2];
+  __shared__ double s2s;  // s2, read once (the publishing thread and the update need it)
   if (threadIdx.x == 0) {
     e0 = *reinterpret_cast<volatile unsigned*>(a.epoch);
     waited_out = 0;
+    s2s = kHas2 ? *a.s2 : 0.0;
   }
   const auto& rows = src.bind(fx_step_smem + (size_t)a.rows * 256 * sizeof(double));
   __syncthreads();
@@ -103,15 +105,14 @@ __global__ void __launch_bounds__(256, 6) lz_fx_step_kernel(Src src, FxStepArgs 
   // The three dots: every block posts its partial; the last to post forms the total (one
   // level, all its threads loading the partials at once), stores alpha and beta and bumps
   // the epoch word; every block waits for the epoch (a bounded wait).
-  if (grid_sum_ordered(acc, a.red, a.dots) && threadIdx.x == 0) {
-    const Tri<double> d = *a.dots;
-    const double bt = kHas2 ? (*a.s2) * d.a : 0.0;
+  Tri<double> d;
+  if (grid_sum_ordered(acc, a.red, a.dots, &d) && threadIdx.x == 0) {
+    const double bt = kHas2 ? s2s * d.a : 0.0;
     double t = d.b;
-    if (kHas2) t = fma(-(bt * (*a.s2)), d.c, t);
+    if (kHas2) t = fma(-(bt * s2s), d.c, t);
     *a.beta = bt;
-    *a.alpha = (*a.s1) * t;
-    __threadfence();
-    if (!a.hold_epoch) atomicAdd(a.epoch, 1u);
+    *a.alpha = sc * t;
+    if (!a.hold_epoch) epoch_release_add(a.epoch);  // alpha and beta are visible before the new epoch
   }
   if (threadIdx.x == 0) {
     const unsigned limit = a.spin_limit ? a.spin_limit : kStepSpinLimit;
@@ -124,7 +125,7 @@ __global__ void __launch_bounds__(256, 6) lz_fx_step_kernel(Src src, FxStepArgs 
       }
       __nanosleep(32);
     }
-    __threadfence();
+    fence_acq_rel_gpu();  // with the read of the new epoch: acquire of the published alpha and beta
     ab[0] = __ldcg(a.alpha);
     ab[1] = __ldcg(a.beta);
   }
@@ -134,8 +135,8 @@ __global__ void __launch_bounds__(256, 6) lz_fx_step_kernel(Src src, FxStepArgs 
   double acc0 = 0.0;
   int out = 0;
   if (!waited_out) {
-    const double al = (*a.s1) * ab[0];
-    const double bt = kHas2 ? (*a.s2) * ab[1] : 0.0;
+    const double al = sc * ab[0];
+    const double bt = kHas2 ? s2s * ab[1] : 0.0;
     // The block's rows of pass i are 256 consecutive rows; here thread t takes
     // the adjacent pair 2 (t % 128) + {0, 1} of the passes i = t / 128 (mod 2),
     // with 16-byte loads and stores, two passes per iteration.

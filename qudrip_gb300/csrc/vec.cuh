@@ -125,6 +125,47 @@ struct GridRed {
   T* gpart = nullptr;
 };
 
+// Ticket of a grid reduction: one atomic increment at device scope with
+// acquire-release order.  Its release half publishes the caller's earlier
+// writes (the block's partial, and through the preceding block barrier those
+// of its other threads); its acquire half, in the thread that draws the last
+// ticket, makes every partial released before it visible to that thread and,
+// through the block barrier that follows, to the rest of its block.  This
+// replaces a full fence before the increment and a fence in every thread of
+// the last block after it.
+__device__ __forceinline__ unsigned ticket_add(unsigned int* p) {
+  unsigned old;
+  asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+  return old;
+}
+
+// Bump an epoch word with release order: the caller's earlier writes are
+// visible to a thread that reads the new value and then fences (acquire).
+__device__ __forceinline__ void epoch_release_add(unsigned int* p) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], 1;" : : "l"(p) : "memory");
+}
+__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" : : : "memory"); }
+
+// Thread t's share of a block's sum over p[0, count): p[t] + p[t + blockDim] +
+// ... added in that order, with kInFlight loads issued before their additions
+// (one round trip to L2 per kInFlight terms instead of one per term).
+template <int kInFlight, typename T>
+__device__ __forceinline__ T strided_sum(const T* p, int count, T zero) {
+  T acc = zero;
+  for (int i0 = threadIdx.x; i0 < count; i0 += kInFlight * (int)blockDim.x) {
+    T x[kInFlight];
+#pragma unroll
+    for (int u = 0; u < kInFlight; ++u) {
+      const int i = i0 + u * (int)blockDim.x;
+      x[u] = i < count ? ld_cg(p + i) : zero;
+    }
+#pragma unroll
+    for (int u = 0; u < kInFlight; ++u)
+      if (i0 + u * (int)blockDim.x < count) acc = vadd(acc, x[u]);
+  }
+  return acc;
+}
+
 // Every thread of every block calls this with its value; the last block to
 // arrive returns true in all its threads and thread 0 of it writes *total.
 template <typename T>
@@ -134,15 +175,11 @@ __device__ __forceinline__ bool grid_sum_flat(T v, GridRed<T> R, T* total) {
   const T b = block_sum(v, smem);
   if (threadIdx.x == 0) {
     R.partials[blockIdx.x] = b;
-    __threadfence();
-    const unsigned t = atomicAdd(R.ticket, 1u);
-    last = (t == gridDim.x - 1);
+    last = (ticket_add(R.ticket) == gridDim.x - 1);
   }
   __syncthreads();
   if (!last) return false;
-  __threadfence();
-  T acc = vzero(v);
-  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) acc = vadd(acc, ld_cg(R.partials + i));
+  const T acc = strided_sum<4>(R.partials, (int)gridDim.x, vzero(v));
   const T tot = block_sum(acc, smem);
   if (threadIdx.x == 0) {
     *total = tot;
@@ -156,26 +193,26 @@ __device__ __forceinline__ bool grid_sum_flat(T v, GridRed<T> R, T* total) {
 // (thread t takes partials t, t + blockDim, ... in turn) and forms the total with
 // one block sum, returning true in all its threads; thread 0 of it writes *total.
 // The one-launch step and the two-launch products both reduce their dots this
-// way, so both forms of the step carry the same bits.
+// way, so both forms of the step carry the same bits.  With `held` set, thread
+// 0 of the last block also keeps the total there (no reload of *total).
 template <typename T>
-__device__ __forceinline__ bool grid_sum_ordered(T v, GridRed<T> R, T* total) {
+__device__ __forceinline__ bool grid_sum_ordered(T v, GridRed<T> R, T* total, T* held = nullptr) {
   __shared__ T smem_o[32];
   __shared__ bool last_o;
   const T b = block_sum(v, smem_o);
   if (threadIdx.x == 0) {
     R.partials[blockIdx.x] = b;
-    __threadfence();
-    last_o = (atomicAdd(R.ticket, 1u) == gridDim.x - 1);
+    last_o = (ticket_add(R.ticket) == gridDim.x - 1);
   }
   __syncthreads();
   if (!last_o) return false;
-  __threadfence();
-  T acc = vzero(v);
-  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x) acc = vadd(acc, ld_cg(R.partials + i));
+  // two triples in flight keep the one-launch step within its 40 registers
+  const T acc = strided_sum<sizeof(T) <= 16 ? 4 : 2>(R.partials, (int)gridDim.x, vzero(v));
   const T tot = block_sum(acc, smem_o);
   if (threadIdx.x == 0) {
     *total = tot;
     *R.ticket = 0u;
+    if (held) *held = tot;
   }
   return true;
 }
@@ -191,26 +228,20 @@ __device__ __forceinline__ bool grid_sum(T v, GridRed<T> R, T* total) {
   const unsigned ngroups = (gridDim.x + kRedGroup - 1) / kRedGroup;
   if (threadIdx.x == 0) {
     R.partials[blockIdx.x] = b;
-    __threadfence();
-    last2 = (atomicAdd(R.ticket + 1 + group, 1u) == gsize - 1);
+    last2 = (ticket_add(R.ticket + 1 + group) == gsize - 1);
   }
   __syncthreads();
   if (!last2) return false;
-  __threadfence();
-  T acc = vzero(v);
-  for (unsigned i = threadIdx.x; i < gsize; i += blockDim.x) acc = vadd(acc, ld_cg(R.partials + group * kRedGroup + i));
+  const T acc = strided_sum<4>(R.partials + group * kRedGroup, (int)gsize, vzero(v));
   const T gs = block_sum(acc, smem2);
   if (threadIdx.x == 0) {
     R.gpart[group] = gs;
     R.ticket[1 + group] = 0u;
-    __threadfence();
-    last2 = (atomicAdd(R.ticket, 1u) == ngroups - 1);
+    last2 = (ticket_add(R.ticket) == ngroups - 1);
   }
   __syncthreads();
   if (!last2) return false;
-  __threadfence();
-  T acc2 = vzero(v);
-  for (unsigned i = threadIdx.x; i < ngroups; i += blockDim.x) acc2 = vadd(acc2, ld_cg(R.gpart + i));
+  const T acc2 = strided_sum<4>(R.gpart, (int)ngroups, vzero(v));
   const T tot = block_sum(acc2, smem2);
   if (threadIdx.x == 0) {
     *total = tot;
