@@ -397,29 +397,27 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) lz_fx_blkstep_kerne
   if (out1) blk_wait(&bar[1], par1);
   __syncthreads();
   if (threadIdx.x == 0 && copy_bad) atomicExch(a.ovf + 1, 1);
-  if (grid_sum(acc, a.red, a.dots) && threadIdx.x == 0) {
-    const Tri<double> d = *a.dots;
-    const double bt = kHas2 ? (*a.s2) * d.a : 0.0;
-    double t = d.b;
-    if (kHas2) t = fma(-(bt * (*a.s2)), d.c, t);
-    *a.beta = bt;
-    *a.alpha = (*a.s1) * t;
-    if (!a.hold_epoch) epoch_release_add(a.epoch);
+  if (grid_sum(acc, a.red, a.dots) && threadIdx.x < 32) {
+    double bt = 0.0, al = 0.0;
+    if (threadIdx.x == 0) {
+      const Tri<double> d = *a.dots;
+      bt = kHas2 ? (*a.s2) * d.a : 0.0;
+      double t = d.b;
+      if (kHas2) t = fma(-(bt * (*a.s2)), d.c, t);
+      al = (*a.s1) * t;
+      *a.beta = bt;
+      *a.alpha = al;
+    }
+    if (!a.hold_epoch) mbox_publish(a.mbox, a.epoch, e0, al, bt);
   }
   if (threadIdx.x == 0) {
-    const unsigned limit = a.spin_limit ? a.spin_limit : kStepSpinLimit;
-    unsigned polls = 0;
-    while (*reinterpret_cast<volatile unsigned*>(a.epoch) == e0) {
-      if (++polls > limit) {
-        waited_out = 1;
-        atomicExch(a.ovf + 1, 1);
-        break;
-      }
-      __nanosleep(200);
+    double al, bt;
+    if (!mbox_wait(a.mbox, e0, a.spin_limit ? a.spin_limit : kStepSpinLimit, 200, &al, &bt)) {
+      waited_out = 1;
+      atomicExch(a.ovf + 1, 1);
     }
-    fence_acq_rel_gpu();
-    ab[0] = __ldcg(a.alpha);
-    ab[1] = __ldcg(a.beta);
+    ab[0] = al;
+    ab[1] = bt;
   }
   __syncthreads();
   // second half: v_k = (w - (beta s2) V2) - (alpha s1) V1 on the CTA's rows

@@ -8,8 +8,8 @@
 // keeps the w of its own rows in shared memory (rows r = gtid + i * stride,
 // slot i * 256 + tid), the last block to post its partials of the three dots
 // forms their total (one level: all its threads load the partials at once),
-// publishes alpha and beta and bumps an epoch word, every block waits for the
-// epoch (a bounded wait), and then updates the same rows it produced (in
+// publishes alpha and beta in a mailbox, every block waits for them (a bounded
+// wait), and then updates the same rows it produced (in
 // adjacent pairs, for 16-byte accesses): reads v1, v2, writes v_k, its
 // fixed-point copy for the next product, and its share of ||v_k||^2.
 //
@@ -24,9 +24,64 @@
 
 namespace qd {
 
-// Polls of the epoch word before a block gives up on the others (with the
+// Polls of the mailbox before a block gives up on the others (with the
 // back-off below, about a second; a healthy step waits a few microseconds).
 constexpr unsigned kStepSpinLimit = 1u << 22;
+
+// The mailbox through which the block that forms alpha and beta hands them to
+// every block: two sets, used by alternate launches (the parity of an epoch
+// word that every launch bumps), of 16 copies on separate 128-byte lines; block
+// b reads copy b mod 16, so the polls spread over 16 lines.  Every entry is
+// written once per launch from kMboxEmpty, a signalling NaN that no arithmetic
+// produces: a block that reads two entries other than kMboxEmpty holds the
+// final alpha and beta, with no fence and no second read.  The publisher also
+// empties the other set for the next launch; the kernel boundary orders that
+// before the next launch's reads.  A launch that publishes nothing (a step
+// past a breakdown, or the test hold below) leaves both sets and the epoch as
+// they were, so every launch starts with the set of its parity empty.
+constexpr int kMboxCopies = 16;
+constexpr int kMboxStride = 16;  // doubles from one copy to the next (128 bytes)
+constexpr int kMboxDoubles = 2 * kMboxCopies * kMboxStride;
+constexpr long long kMboxEmpty = 0x7ff0000000000001LL;
+
+__device__ __forceinline__ double ld_relaxed_f64(const double* p) {
+  double v;
+  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_f64(double* p, double v) {
+  asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" : : "l"(p), "d"(v) : "memory");
+}
+
+// Called by warp 0 of the publishing block (all 32 lanes, al and bt valid in
+// lane 0): lanes 0-15 write the copies of this launch's set, lanes 16-31 empty
+// the other set, lane 0 bumps the epoch.
+__device__ __forceinline__ void mbox_publish(double* mbox, unsigned* epoch, unsigned e0, double al, double bt) {
+  const int lane = threadIdx.x & 31;
+  al = __shfl_sync(0xffffffffu, al, 0);
+  bt = __shfl_sync(0xffffffffu, bt, 0);
+  const bool pub = lane < kMboxCopies;
+  const int set = (int)((e0 & 1u) ^ (pub ? 0u : 1u));
+  double* m = mbox + (set * kMboxCopies + (lane & (kMboxCopies - 1))) * kMboxStride;
+  const double empty = __longlong_as_double(kMboxEmpty);
+  st_relaxed_f64(m, pub ? al : empty);
+  st_relaxed_f64(m + 1, pub ? bt : empty);
+  if (lane == 0) atomicAdd(epoch, 1u);
+}
+
+// Thread 0 of every block: wait (at most `limit` polls) for this launch's
+// alpha and beta.  Returns false when the wait ran out.
+__device__ __forceinline__ bool mbox_wait(const double* mbox, unsigned e0, unsigned limit, int backoff_ns,
+                                          double* al, double* bt) {
+  const double* m = mbox + ((int)(e0 & 1u) * kMboxCopies + (int)(blockIdx.x & (kMboxCopies - 1))) * kMboxStride;
+  for (unsigned polls = 0;; ++polls) {
+    *al = ld_relaxed_f64(m);
+    *bt = ld_relaxed_f64(m + 1);
+    if (__double_as_longlong(*al) != kMboxEmpty && __double_as_longlong(*bt) != kMboxEmpty) return true;
+    if (polls >= limit) return false;
+    __nanosleep(backoff_ns);
+  }
+}
 
 struct FxStepArgs {
   int64_t n;
@@ -44,6 +99,7 @@ struct FxStepArgs {
   Tri<double>* dots;
   GridRed<Tri<double>> red;
   unsigned* epoch;      // bumped once per launch by the block that publishes alpha and beta
+  double* mbox;         // kMboxDoubles entries: alpha and beta for every block
   double* Vk;
   double* nrm2;
   double* nrm;
@@ -54,7 +110,7 @@ struct FxStepArgs {
   int* ovf;             // ovf[0]: an element left the fixed-point range; ovf[1]: a wait ran out
   int rows;             // rows per thread: the length of each thread's w column in shared memory
   unsigned spin_limit;  // polls before a block gives up (0: kStepSpinLimit)
-  int hold_epoch;       // test control: the publishing block does not bump the epoch, so every
+  int hold_epoch;       // test control: the publishing block publishes nothing, so every
                         // block's wait runs out after spin_limit polls
 };
 
@@ -103,31 +159,29 @@ __global__ void __launch_bounds__(256, 6) lz_fx_step_kernel(Src src, FxStepArgs 
     }
   }
   // The three dots: every block posts its partial; the last to post forms the total (one
-  // level, all its threads loading the partials at once), stores alpha and beta and bumps
-  // the epoch word; every block waits for the epoch (a bounded wait).
+  // level, all its threads loading the partials at once), stores alpha and beta and
+  // publishes them in the mailbox; every block waits for them (a bounded wait).
   Tri<double> d;
-  if (grid_sum_ordered(acc, a.red, a.dots, &d) && threadIdx.x == 0) {
-    const double bt = kHas2 ? s2s * d.a : 0.0;
-    double t = d.b;
-    if (kHas2) t = fma(-(bt * s2s), d.c, t);
-    *a.beta = bt;
-    *a.alpha = sc * t;
-    if (!a.hold_epoch) epoch_release_add(a.epoch);  // alpha and beta are visible before the new epoch
+  if (grid_sum_ordered(acc, a.red, a.dots, &d) && threadIdx.x < 32) {
+    double bt = 0.0, al = 0.0;
+    if (threadIdx.x == 0) {
+      bt = kHas2 ? s2s * d.a : 0.0;
+      double t = d.b;
+      if (kHas2) t = fma(-(bt * s2s), d.c, t);
+      al = sc * t;
+      *a.beta = bt;
+      *a.alpha = al;
+    }
+    if (!a.hold_epoch) mbox_publish(a.mbox, a.epoch, e0, al, bt);
   }
   if (threadIdx.x == 0) {
-    const unsigned limit = a.spin_limit ? a.spin_limit : kStepSpinLimit;
-    unsigned polls = 0;
-    while (*reinterpret_cast<volatile unsigned*>(a.epoch) == e0) {
-      if (++polls > limit) {
-        waited_out = 1;
-        atomicExch(a.ovf + 1, 1);
-        break;
-      }
-      __nanosleep(32);
+    double al, bt;
+    if (!mbox_wait(a.mbox, e0, a.spin_limit ? a.spin_limit : kStepSpinLimit, 32, &al, &bt)) {
+      waited_out = 1;
+      atomicExch(a.ovf + 1, 1);
     }
-    fence_acq_rel_gpu();  // with the read of the new epoch: acquire of the published alpha and beta
-    ab[0] = __ldcg(a.alpha);
-    ab[1] = __ldcg(a.beta);
+    ab[0] = al;
+    ab[1] = bt;
   }
   __syncthreads();
 

@@ -437,8 +437,8 @@ static bool fx_one_launch_step() {
 }
 
 // Test control of the one-launch step's bounded grid barrier:
-// QD_STEP_WAIT_OUT=<polls> (1 .. 2^20) keeps the publishing block from bumping
-// the epoch and lets every block give up after <polls> polls, so each step's
+// QD_STEP_WAIT_OUT=<polls> (1 .. 2^20) keeps the publishing block from
+// publishing alpha and beta and lets every block give up after <polls> polls, so each step's
 // wait runs out and the solve returns QD_ERR_TIMEOUT with the kernel finished.
 // Read per solve; 0 when unset.
 static unsigned step_wait_out_polls() {
@@ -446,6 +446,13 @@ static unsigned step_wait_out_polls() {
   if (!e) return 0;
   const long v = std::strtol(e, nullptr, 10);
   return v > 0 ? (unsigned)std::min<long>(v, 1L << 20) : 0u;
+}
+
+// The epoch to 0 and every mailbox entry to kMboxEmpty (once per Lanczos run,
+// so that a run does not depend on what earlier runs left).
+__global__ void step_mbox_reset_kernel(unsigned* epoch, double* mbox) {
+  for (int i = threadIdx.x; i < kMboxDoubles; i += blockDim.x) mbox[i] = __longlong_as_double(kMboxEmpty);
+  if (threadIdx.x == 0) *epoch = 0u;
 }
 
 // Overflow flag of a fixed-point run (nonzero: rerun on the FP64 product);
@@ -513,8 +520,10 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
   if (!fx_one_launch_step()) step_form = nullptr;
   DBuf<__int128> X2(step_form ? n + 32 : 1);
   DBuf<unsigned> ep(4);
+  DBuf<double> mb(kMboxDoubles);
   DBuf<int> flags(2);
-  QD_CUDA(cudaMemsetAsync(ep.p, 0, 4 * sizeof(unsigned), ctx->stream));
+  step_mbox_reset_kernel<<<1, 128, 0, ctx->stream>>>(ep.p, mb.p);
+  QD_CHECK_LAUNCH();
   QD_CUDA(cudaMemsetAsync(flags.p, 0, 2 * sizeof(int), ctx->stream));
   bool stepped = false;
   auto launch = [&]() {
@@ -531,6 +540,7 @@ void time_spmv(qd_ham* H, int spmv, int iters, double* avg_ms, double* bytes_per
       a.dots = reinterpret_cast<Tri<double>*>(d + 6);
       a.red = W.red_tri<double>(2);
       a.epoch = ep.p;
+      a.mbox = mb.p;
       a.Vk = (double*)t.p;
       a.nrm2 = d + 3;
       a.nrm = d + 4;
@@ -631,8 +641,12 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int k_
   // two-launch step
   const bool one_launch = fxk == 1 && fx_one_launch_step() && !H->one_shot;
   if (fxk == 1 && !one_launch) form->step_fused = -1;
-  // the step's barrier counters start every run at zero (each launch also leaves them so)
-  if (one_launch) QD_CUDA(cudaMemsetAsync(B.epoch.p, 0, 4 * sizeof(unsigned), ctx->stream));
+  // the step's epoch and mailbox start every run empty
+  if (one_launch) {
+    step_mbox_reset_kernel<<<1, 128, 0, ctx->stream>>>(B.epoch.p, B.mbox.p);
+    QD_CHECK_LAUNCH();
+    QD_LAUNCHED(ctx);
+  }
   for (int k = k_first; k <= k_last; ++k) {
     const VV* V1 = B.V.p + (int64_t)(k - 1) * B.ld;
     const VV* V2 = (k >= 2) ? B.V.p + (int64_t)(k - 2) * B.ld : nullptr;
@@ -657,6 +671,7 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int k_
         a.dots = B.dots.p + k;
         a.red = W.red_tri<double>(2);
         a.epoch = B.epoch.p;
+        a.mbox = B.mbox.p;
         a.Vk = Vk;
         a.nrm2 = B.nrm2.p + k;
         a.nrm = B.nrm.p + k;

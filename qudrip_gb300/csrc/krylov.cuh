@@ -3,6 +3,7 @@
 
 #include <type_traits>
 
+#include "fxstep.cuh"
 #include "ham.cuh"
 #include "spmv.cuh"
 #include "vec.cuh"
@@ -28,7 +29,8 @@ struct LanczosBuffers {
   DBuf<int> stop;
   DBuf<__int128> X;  // fixed-point copies of the two newest basis vectors (uniform-coupling product)
   DBuf<int> ovf;         // [0] a vector left the fixed-point range, [1] a bounded device wait ran out
-  DBuf<unsigned> epoch;  // barrier counters of the one-launch steps (fxstep.cuh, fxblock.cu)
+  DBuf<unsigned> epoch;  // launch parity of the one-launch steps (fxstep.cuh, fxblock.cu)
+  DBuf<double> mbox;     // their alpha and beta mailbox (kMboxDoubles entries)
   cudaGraphExec_t exec = nullptr;
   int kind = 0;  // product the captured graph launches (0 CSR, 1 matrix-free, 2 fixed-point, +4 one-launch step)
   int done = 0;  // Lanczos steps run on the stored basis (incremental solves continue from here)
@@ -37,7 +39,7 @@ struct LanczosBuffers {
       X.alloc((size_t)2 * ld);
       ovf.alloc(2);
       epoch.alloc(4);
-      QD_CUDA(cudaMemsetAsync(epoch.p, 0, 4 * sizeof(unsigned), s));
+      mbox.alloc(kMboxDoubles);  // both set empty by each run's first launch
     }
   }
   int64_t graph_kernels = 0;

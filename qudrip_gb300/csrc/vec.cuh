@@ -139,13 +139,6 @@ __device__ __forceinline__ unsigned ticket_add(unsigned int* p) {
   return old;
 }
 
-// Bump an epoch word with release order: the caller's earlier writes are
-// visible to a thread that reads the new value and then fences (acquire).
-__device__ __forceinline__ void epoch_release_add(unsigned int* p) {
-  asm volatile("red.release.gpu.global.add.u32 [%0], 1;" : : "l"(p) : "memory");
-}
-__device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" : : : "memory"); }
-
 // Thread t's share of a block's sum over p[0, count): p[t] + p[t + blockDim] +
 // ... added in that order, with kInFlight loads issued before their additions
 // (one round trip to L2 per kInFlight terms instead of one per term).

@@ -95,7 +95,7 @@ def test_argument_limits(ctx):
 
 def test_step_barrier_wait_runs_out_and_next_solve_is_unchanged(ctx, monkeypatch):
     """The one-launch Lanczos step's grid barrier is a bounded wait.  With the
-    test control QD_STEP_WAIT_OUT the publishing block holds the epoch back, so
+    test control QD_STEP_WAIT_OUT the publishing block publishes no alpha and beta, so
     every block gives up after a few polls, skips its update and still joins the
     norm's reduction: the kernel returns and the solve reports QD_ERR_TIMEOUT.
     The next solve on the same operator carries the bits of one on a fresh
