@@ -45,6 +45,10 @@ __device__ __forceinline__ cplx vsubmul(cplx x, cplx a, cplx y) {
 }
 
 __device__ __forceinline__ double shfl_xor(double v, int o) { return __shfl_xor_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ double shfl_down(double v, int o) { return __shfl_down_sync(0xffffffffu, v, o); }
+__device__ __forceinline__ cplx shfl_down(cplx v, int o) {
+  return mkc(__shfl_down_sync(0xffffffffu, v.re, o), __shfl_down_sync(0xffffffffu, v.im, o));
+}
 __device__ __forceinline__ cplx shfl_xor(cplx v, int o) {
   return mkc(__shfl_xor_sync(0xffffffffu, v.re, o), __shfl_xor_sync(0xffffffffu, v.im, o));
 }
@@ -81,6 +85,10 @@ __device__ __forceinline__ Tri<T> shfl_xor(Tri<T> v, int o) {
   return Tri<T>{shfl_xor(v.a, o), shfl_xor(v.b, o), shfl_xor(v.c, o)};
 }
 template <typename T>
+__device__ __forceinline__ Tri<T> shfl_down(Tri<T> v, int o) {
+  return Tri<T>{shfl_down(v.a, o), shfl_down(v.b, o), shfl_down(v.c, o)};
+}
+template <typename T>
 __device__ __forceinline__ Tri<T> ld_cg(const Tri<T>* p) {
   return Tri<T>{ld_cg(&p->a), ld_cg(&p->b), ld_cg(&p->c)};
 }
@@ -93,18 +101,31 @@ __device__ __forceinline__ T warp_sum(T v) {
 }
 
 // Sum over the block; the result is valid in thread 0.  smem >= 32 entries.
+// Each level of the trees adds only in the lanes whose sum is still needed
+// (lane < offset) and the warp totals take log2(warps) levels, not five: lane
+// 0 pairs its operands exactly as the butterfly of warp_sum does, with less
+// work for GB300's narrow FP64 pipe.
 template <typename T>
 __device__ __forceinline__ T block_sum(T v, T* smem) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nw = (blockDim.x + 31) >> 5;
-  v = warp_sum(v);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const T t = shfl_down(v, o);
+    if (lane < o) v = vadd(v, t);
+  }
   __syncthreads();
   if (lane == 0) smem[warp] = v;
   __syncthreads();
   T r = vzero(v);
   if (warp == 0) {
     r = (lane < nw) ? smem[lane] : vzero(v);
-    r = warp_sum(r);
+    int top = 1;
+    while (top < nw) top <<= 1;
+    for (int o = top >> 1; o > 0; o >>= 1) {
+      const T t = shfl_down(r, o);
+      if (lane < o) r = vadd(r, t);
+    }
   }
   return r;
 }
