@@ -84,14 +84,14 @@ __device__ __forceinline__ unsigned long long batch_clock_ns() {
 
 // FP64 sum over the block of per-thread values; every thread gets the result.
 __device__ double block_sum_all(double v, BlockScratch& S) {
-  v = warp_sum(v);
+  v = warp_sum0(v);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   __syncthreads();
   if (lane == 0) S.red[warp] = v;
   __syncthreads();
   if (warp == 0) {
     double t = (lane < (int)(blockDim.x >> 5)) ? S.red[lane] : 0.0;
-    t = warp_sum(t);
+    t = warp_sum0(t);
     if (lane == 0) S.bcast = t;
   }
   __syncthreads();
@@ -102,7 +102,7 @@ __device__ double block_sum_all(double v, BlockScratch& S) {
 __device__ void block_sum_all3(double (&v)[3], BlockScratch& S) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int q = 0; q < 3; ++q) v[q] = warp_sum(v[q]);
+  for (int q = 0; q < 3; ++q) v[q] = warp_sum0(v[q]);
   __syncthreads();
   if (lane == 0) {
 #pragma unroll
@@ -113,7 +113,7 @@ __device__ void block_sum_all3(double (&v)[3], BlockScratch& S) {
 #pragma unroll
     for (int q = 0; q < 3; ++q) {
       double t = (lane < (int)(blockDim.x >> 5)) ? S.red3[lane][q] : 0.0;
-      t = warp_sum(t);
+      t = warp_sum0(t);
       if (lane == 0) S.bcast3[q] = t;
     }
   }
@@ -631,12 +631,12 @@ __global__ void __launch_bounds__(kBatchThreads, 2) batch_lanczos_kernel(const B
               }
               for (int ii = (nq << 2) + lane; ii < tn; ii += 32) acc = fmaf(vj[ii], S.wt[ii], acc);
               dacc += (double)acc;
-              dacc = warp_sum(dacc);
+              dacc = warp_sum0(dacc);
               if (lane == 0) part[j] += dacc;  // tile by tile, in order: the same bits in every run
             }
           }
           // ||u||^2 of this CTA's rows into part[k]
-          uacc = warp_sum(uacc);
+          uacc = warp_sum0(uacc);
           __syncthreads();
           if (lane == 0) S.red[warp] = uacc;
           __syncthreads();

@@ -78,7 +78,7 @@ __global__ void __launch_bounds__(kEvThreads) multidot_tile_kernel(int64_t n, co
         a1 = vdotfma(x3, ws[i + 96], a1);
       }
       for (; i < tn; i += 32) a0 = vdotfma(vj[i], ws[i], a0);
-      const cplx t = warp_sum(vadd(a0, a1));
+      const cplx t = warp_sum0(vadd(a0, a1));
       if (lane == 0) part[j] = vadd(part[j], t);  // one warp owns vector j: no race
     }
   }

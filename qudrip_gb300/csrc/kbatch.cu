@@ -33,7 +33,7 @@ struct KbScratch {
 };
 
 __device__ cplx kb_block_sum(cplx v, KbScratch& S) {
-  double re = warp_sum(v.re), im = warp_sum(v.im);
+  double re = warp_sum0(v.re), im = warp_sum0(v.im);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   __syncthreads();
   if (lane == 0) {
@@ -44,8 +44,8 @@ __device__ cplx kb_block_sum(cplx v, KbScratch& S) {
   if (warp == 0) {
     double a = (lane < kKbThreads / 32) ? S.red[lane] : 0.0;
     double b = (lane < kKbThreads / 32) ? S.redi[lane] : 0.0;
-    a = warp_sum(a);
-    b = warp_sum(b);
+    a = warp_sum0(a);
+    b = warp_sum0(b);
     if (lane == 0) {
       S.bcast = a;
       S.bcasti = b;
@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(kKbThreads) kbatch_kernel(KbArgs A, const MV* 
           const cplx* vj = V + (size_t)j * A.ld;
           cplx acc = mkc(0.0, 0.0);
           for (int64_t i = lane; i < n; i += 32) acc = vdotfma(vj[i], w[i], acc);
-          acc = warp_sum(acc);
+          acc = warp_sum0(acc);
           if (lane == 0) S.h[j] = acc;
         }
         __syncthreads();

@@ -100,6 +100,20 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
+// The warp's sum in lane 0 only (the other lanes hold partial sums): the same
+// operand pairs as warp_sum's lane 0, so the same bits, with adds only in the
+// lanes still needed at each level (a fifth of warp_sum's FP64 work).
+template <typename T>
+__device__ __forceinline__ T warp_sum0(T v) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const T t = shfl_down(v, o);
+    if (lane < o) v = vadd(v, t);
+  }
+  return v;
+}
+
 // Sum over the block; the result is valid in thread 0.  smem >= 32 entries.
 // Each level of the trees adds only in the lanes whose sum is still needed
 // (lane < offset) and the warp totals take log2(warps) levels, not five: lane
@@ -109,11 +123,7 @@ template <typename T>
 __device__ __forceinline__ T block_sum(T v, T* smem) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nw = (blockDim.x + 31) >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const T t = shfl_down(v, o);
-    if (lane < o) v = vadd(v, t);
-  }
+  v = warp_sum0(v);
   __syncthreads();
   if (lane == 0) smem[warp] = v;
   __syncthreads();
