@@ -125,3 +125,33 @@ def test_step_barrier_wait_runs_out_and_next_solve_is_unchanged(ctx, monkeypatch
     r2, p2 = solve(sec.lower(ham))
     assert r1.ritz_value == r0.ritz_value == r2.ritz_value
     assert np.array_equal(p1, p0) and np.array_equal(p2, p0)
+
+
+def test_step_mailbox_across_runs_and_forms(ctx, monkeypatch):
+    """The one-launch step hands alpha and beta to every block through a
+    mailbox whose set alternates with the launch parity.  Solves of different
+    lengths and solves in the two-launch form, interleaved on one operator,
+    each carry the bits of the same solve in the same form on a fresh
+    operator."""
+    spec, ham = chains.xxz_chain(14)
+    sec = sector(spec)
+    v0 = q.start_vector(sec.dim, 11)
+
+    def solve(H, kdim, split):
+        if split:
+            monkeypatch.setenv("QD_LANCZOS_STEP", "split")
+        else:
+            monkeypatch.delenv("QD_LANCZOS_STEP", raising=False)
+        psi = q.getState(sec, 1)
+        psi.set(0, v0)
+        r = q.Arnoldi.getLanczosSolver(sec, kdim).getGroundState(H, psi(0), 0)
+        return r.ritz_value, psi.get(0)
+
+    plan = ((17, False), (30, False), (17, True), (30, False), (17, False), (30, True), (17, False))
+    fresh = {key: solve(sec.lower(ham), *key) for key in set(plan)}
+    H = sec.lower(ham)
+    for key in plan:
+        e, p = solve(H, *key)
+        assert e == fresh[key][0]
+        assert np.array_equal(p, fresh[key][1])
+    monkeypatch.delenv("QD_LANCZOS_STEP", raising=False)
