@@ -140,7 +140,6 @@ __device__ __forceinline__ T block_sum(T v, T* smem) {
   return r;
 }
 
-// Grid reduction slot: per-block partials and a ticket counter (zero at rest).
 // Grid reduction slot: per-block partials and ticket counters (zero at rest).
 // With `gpart` set the reduction is two-level: blocks are grouped by
 // kRedGroup, the last block of each group sums the group (ticket[1 + group]),
