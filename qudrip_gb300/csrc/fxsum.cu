@@ -381,6 +381,65 @@ bool launch_fx_step(Ctx* ctx, const qd_ham* H, const FxForm& f, FxStepArgs a) {
   return ok;
 }
 
+// <psi|H psi> for a psi whose imaginary part is 0 (State::eval, state.hpp:33-43, on a
+// real ground state): (H psi)_r = c sum_k psi_k + d_r psi_r over the row's
+// sliced columns, the gathered values summed in FP64 in the row's column order,
+// and psi_r (H psi)_r summed over the grid in one pass.  Only the real halves of
+// the gathered entries are read.  A row whose own psi_r carries an imaginary
+// part sets *has_imag; the caller then takes the complex CSR product, so every
+// entry is checked (each is some row's own).
+__global__ void __launch_bounds__(256) fx_eval_real_kernel(int64_t n, const int64_t* __restrict__ soff,
+                                                           const int32_t* __restrict__ scol,
+                                                           const uint8_t* __restrict__ slen,
+                                                           const double* __restrict__ diag, double c,
+                                                           const cplx* __restrict__ psi, GridRed<double> red,
+                                                           double* out, int* has_imag) {
+  const double* pre = reinterpret_cast<const double*>(psi);  // psi[k].re at pre[2 k]
+  double acc = 0.0;
+  bool im = false;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+    const int4* c4 = sell_row(soff, scol, r);
+    const int e = __ldcs(slen + r);
+    double s = 0.0;
+    int4 cc = __ldcs(c4);
+#pragma unroll 1
+    for (int k = 0; k < e; k += 4) {
+      int4 nc = cc;
+      if (k + 4 < e) nc = __ldcs(c4 + 8 * (k + 4));
+      double x0 = __ldg(pre + 2 * (int64_t)cc.x), x1 = 0.0, x2 = 0.0, x3 = 0.0;
+      if (k + 1 < e) x1 = __ldg(pre + 2 * (int64_t)cc.y);
+      if (k + 2 < e) x2 = __ldg(pre + 2 * (int64_t)cc.z);
+      if (k + 3 < e) x3 = __ldg(pre + 2 * (int64_t)cc.w);
+      s += (x0 + x1) + (x2 + x3);
+      cc = nc;
+    }
+    const double2 p = __ldcs(reinterpret_cast<const double2*>(psi + r));
+    im |= (p.y != 0.0);
+    acc = fma(p.x, fma(c, s, __ldcs(diag + r) * p.x), acc);
+  }
+  if (im) *has_imag = 1;
+  grid_sum(acc, red, out);
+}
+
+bool fx_eval_real(Ctx* ctx, const qd_ham* H, const FxForm& f, const cplx* psi, GridRed<double> red, double* out_dev,
+                  int* flag_dev, double* value) {
+  QD_CUDA(cudaMemsetAsync(flag_dev, 0, sizeof(int), ctx->stream));
+  fx_eval_real_kernel<<<fx_dots_grid(ctx, H->dim), 256, 0, ctx->stream>>>(
+      H->dim, f.sell_off.p, f.sell_col.p, f.sell_len.p, f.diag.p, f.c, psi, red, out_dev, flag_dev);
+  QD_CHECK_LAUNCH();
+  QD_LAUNCHED(ctx);
+  struct {
+    double v;
+    int flag;
+  } h{};
+  QD_CUDA(cudaMemcpyAsync(&h.v, out_dev, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaMemcpyAsync(&h.flag, flag_dev, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  QD_CUDA(cudaStreamSynchronize(ctx->stream));
+  *value = h.v;
+  return h.flag == 0;
+}
+
 // X = fixed-point copy of x (v_0 of a Lanczos run).
 __global__ void fx_shadow_kernel(int64_t n, const double* x, __int128* X, int F, int* ovf) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)

@@ -351,6 +351,14 @@ void ham_apply_c(qd_ham* H, const cplx* x, cplx* y) {
 cplx state_eval(qd_ham* H, const cplx* psi) {
   Ctx* ctx = H->ctx;
   Workspace& W = ham_workspace(H);
+  // a real state on an operator whose uniform-coupling form is built (by a solve
+  // on it): the sliced columns, no stored values read
+  if ((H->flags & QD_HAM_REAL) && H->fx_allowed && H->fx_state > 0 && H->fx) {
+    if (!W.eval_real.p) W.eval_real.alloc(1);
+    if (!W.eval_flag.p) W.eval_flag.alloc(1);
+    double v = 0.0;
+    if (fx_eval_real(ctx, H, *H->fx, psi, W.red_d(0), W.eval_real.p, W.eval_flag.p, &v)) return mkc(v, 0.0);
+  }
   if (W.eval_y.n < (size_t)H->dim + 1) W.eval_y.alloc(H->dim + 1);
   if (!W.eval_out.p) W.eval_out.alloc(1);
   // psi^dagger (H psi): the product and the dot in one pass

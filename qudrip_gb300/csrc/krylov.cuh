@@ -114,6 +114,8 @@ struct Workspace {
   // H psi and the result of state_eval, kept between calls (a device allocation
   // and free per call would wait for the whole device)
   DBuf<cplx> eval_y, eval_out;
+  DBuf<double> eval_real;  // the uniform-coupling form's value and its imaginary-part flag
+  DBuf<int> eval_flag;
   DBuf<double> start_nrm2;  // ||v0||^2 of the last ground-state solve (read by its first kernels)
   DBuf<int> start_has_im;
 
@@ -158,6 +160,10 @@ struct FxStepArgs;
 // One Lanczos step of the uniform-coupling form in one cooperative launch
 // (fxstep.cuh); false when it does not fit on the device at once.
 bool launch_fx_step(Ctx* ctx, const qd_ham* H, const FxForm& f, FxStepArgs a);
+// <psi|H psi> on the uniform-coupling form when psi's imaginary part is 0 (false, with *value
+// undefined, when it is not)
+bool fx_eval_real(Ctx* ctx, const qd_ham* H, const FxForm& f, const cplx* psi, GridRed<double> red, double* out_dev,
+                  int* flag_dev, double* value);
 bool launch_fx_slots_step(Ctx* ctx, const qd_ham* H, const FxForm& f, const FxStepArgs& a, int grid);
 bool launch_fx_block_step(Ctx* ctx, const qd_ham* H, const FxForm& f, FxStepArgs a, int grid);
 void launch_fx_block_dots(Ctx* ctx, const qd_ham* H, const FxForm& f, const double* x, const __int128* X,

@@ -243,3 +243,37 @@ def test_large_sector_takes_the_two_launch_step(ctx):
     assert abs(r_fx.ritz_value - r_csr.ritz_value) <= 1e-12 * abs(r_csr.ritz_value)
     ov = abs(np.vdot(psi_fx, psi_csr)) / (np.linalg.norm(psi_fx) * np.linalg.norm(psi_csr))
     assert ov >= 1 - 1e-10
+
+
+@pytest.mark.parametrize("L,fields", [(16, None), (14, "random")])
+def test_real_state_expectation_on_the_uniform_form(ctx, L, fields):
+    """psi.eval of a real state on an operator whose uniform-coupling form a solve has built reads the
+    sliced columns (fx_eval_real_kernel): within 1e-13 of the complex CSR product and of a host FP64 sum.
+    A state with an imaginary part takes the complex CSR product, whose bits the forced CSR path gives."""
+    h = np.random.default_rng(L).uniform(-1, 1, L) if fields else None
+    spec, ham = chains.xxz_chain(L, 1.0, 0.7, periodic=True, fields=h)
+    sec, H = gpu_objects(spec, ham)
+    v0 = q.start_vector(sec.dim, 21)
+    r, psi = solve(sec, H, v0, 60)  # builds the uniform-coupling form
+    rng = np.random.default_rng(L + 1)
+    real = rng.uniform(-1, 1, sec.dim).astype(np.complex128)
+    cplx = real + 1j * rng.uniform(-1, 1, sec.dim)
+    Hs = H.scipy()
+    st = q.getState(sec, 2)
+    got = {}
+    for name, x in (("ground", psi), ("real", real), ("cplx", cplx)):
+        st.set(0, x)
+        got[name] = st.eval(0, H)
+        ref = np.vdot(x, Hs @ x)
+        scale = np.abs(np.conj(x) * (Hs @ x)).sum()
+        assert abs(got[name] - ref) <= 1e-13 * scale, (name, got[name], ref)
+        if name != "cplx":
+            assert got[name].imag == 0.0
+    A.call("qd_ham_set_spmv_kernel", H.handle, 110)  # the FP64 CSR path for every product, eval included
+    for name, x in (("ground", psi), ("real", real), ("cplx", cplx)):
+        st.set(0, x)
+        e_csr = st.eval(0, H)
+        scale = np.abs(np.conj(x) * (Hs @ x)).sum()
+        assert abs(got[name] - e_csr) <= 1e-13 * scale, (name, got[name], e_csr)
+        if name == "cplx":
+            assert got[name] == e_csr  # the complex state took the CSR product in both
