@@ -408,7 +408,7 @@ __global__ void __launch_bounds__(kThreads, 1024 / kThreads) lz_fx_blkstep_kerne
       *a.beta = bt;
       *a.alpha = al;
     }
-    if (!a.hold_epoch) mbox_publish(a.mbox, a.epoch, e0, al, bt);
+    if (!a.hold_publish) mbox_publish(a.mbox, a.epoch, e0, al, bt);
   }
   if (threadIdx.x == 0) {
     double al, bt;

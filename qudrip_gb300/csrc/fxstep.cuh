@@ -110,7 +110,7 @@ struct FxStepArgs {
   int* ovf;             // ovf[0]: an element left the fixed-point range; ovf[1]: a wait ran out
   int rows;             // rows per thread: the length of each thread's w column in shared memory
   unsigned spin_limit;  // polls before a block gives up (0: kStepSpinLimit)
-  int hold_epoch;       // test control: the publishing block publishes nothing, so every
+  int hold_publish;     // test control: the publishing block publishes nothing, so every
                         // block's wait runs out after spin_limit polls
 };
 
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(256, 6) lz_fx_step_kernel(Src src, FxStepArgs 
       *a.beta = bt;
       *a.alpha = al;
     }
-    if (!a.hold_epoch) mbox_publish(a.mbox, a.epoch, e0, al, bt);
+    if (!a.hold_publish) mbox_publish(a.mbox, a.epoch, e0, al, bt);
   }
   if (threadIdx.x == 0) {
     double al, bt;

@@ -688,7 +688,7 @@ static void lanczos_run(qd_ham* H, const MV* vals, LanczosBuffers<VV>& B, int k_
         a.Xk = Xnext;
         a.ovf = B.ovf.p;
         a.spin_limit = step_wait_out_polls();
-        a.hold_epoch = a.spin_limit != 0;
+        a.hold_publish = a.spin_limit != 0;
         if (launch_fx_step(ctx, H, *form, a)) continue;
       }
       if (fxk == 1)  // product fused with the step's inner products, then the update
