@@ -136,8 +136,9 @@ __global__ void __launch_bounds__(kEvThreads) ev_norm_kernel(int64_t n, const cp
   double acc = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     acc += vnorm2(w[i]);
-  if (grid_sum(acc, red, nrm2) && threadIdx.x == 0) {
-    const double nr = sqrt(*nrm2);
+  double n2 = 0.0;
+  if (grid_sum(acc, red, nrm2, &n2) && threadIdx.x == 0) {
+    const double nr = sqrt(n2);
     *nrm = nr;
     if (nr < 1e-10 && *stop == 0) *stop = step;  // sparse_algorithm.hpp:387
   }

@@ -237,8 +237,9 @@ __global__ void __launch_bounds__(256, 6) lz_fx_step_kernel(Src src, FxStepArgs 
   }
   if (out) a.ovf[0] = 1;
   // every block arrives here, waited out or not, so the ticket counts stay whole
-  if (grid_sum(acc0, a.rd, a.nrm2) && threadIdx.x == 0) {
-    const double nr = sqrt(*a.nrm2);
+  double n2 = 0.0;
+  if (grid_sum(acc0, a.rd, a.nrm2, &n2) && threadIdx.x == 0) {
+    const double nr = sqrt(n2);
     *a.nrm = nr;
     *a.sk = 1.0 / nr;
     if (nr < 1e-10 && a.stop && *a.stop == 0) *a.stop = a.step;  // sparse_algorithm.hpp:421

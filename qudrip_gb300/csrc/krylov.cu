@@ -211,8 +211,9 @@ __global__ void __launch_bounds__(kLzThreads, kLzBlocksPerSm)
     acc0 += vnorm2(o);
   }
   if (kShadow && out) *ovf = 1;
-  if (grid_sum(acc0 + acc1, red, nrm2) && threadIdx.x == 0) {
-    const double nr = sqrt(*nrm2);
+  double n2 = 0.0;
+  if (grid_sum(acc0 + acc1, red, nrm2, &n2) && threadIdx.x == 0) {
+    const double nr = sqrt(n2);
     *nrm = nr;
     *sk = 1.0 / nr;
     if (nr < 1e-10 && stop && *stop == 0) *stop = step;  // sparse_algorithm.hpp:421

@@ -190,9 +190,10 @@ __device__ __forceinline__ T strided_sum(const T* p, int count, T zero) {
 }
 
 // Every thread of every block calls this with its value; the last block to
-// arrive returns true in all its threads and thread 0 of it writes *total.
+// arrive returns true in all its threads and thread 0 of it writes *total
+// (and, with `held` set, keeps the total there: no reload of *total).
 template <typename T>
-__device__ __forceinline__ bool grid_sum_flat(T v, GridRed<T> R, T* total) {
+__device__ __forceinline__ bool grid_sum_flat(T v, GridRed<T> R, T* total, T* held = nullptr) {
   __shared__ T smem[32];
   __shared__ bool last;
   const T b = block_sum(v, smem);
@@ -207,6 +208,7 @@ __device__ __forceinline__ bool grid_sum_flat(T v, GridRed<T> R, T* total) {
   if (threadIdx.x == 0) {
     *total = tot;
     *R.ticket = 0u;
+    if (held) *held = tot;
   }
   return true;
 }
@@ -241,8 +243,8 @@ __device__ __forceinline__ bool grid_sum_ordered(T v, GridRed<T> R, T* total, T*
 }
 
 template <typename T>
-__device__ __forceinline__ bool grid_sum(T v, GridRed<T> R, T* total) {
-  if (!R.gpart) return grid_sum_flat(v, R, total);
+__device__ __forceinline__ bool grid_sum(T v, GridRed<T> R, T* total, T* held = nullptr) {
+  if (!R.gpart) return grid_sum_flat(v, R, total, held);
   __shared__ T smem2[32];
   __shared__ bool last2;
   const T b = block_sum(v, smem2);
@@ -269,6 +271,7 @@ __device__ __forceinline__ bool grid_sum(T v, GridRed<T> R, T* total) {
   if (threadIdx.x == 0) {
     *total = tot;
     *R.ticket = 0u;
+    if (held) *held = tot;
   }
   return true;
 }
