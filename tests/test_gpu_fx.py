@@ -258,22 +258,24 @@ def test_real_state_expectation_on_the_uniform_form(ctx, L, fields):
     rng = np.random.default_rng(L + 1)
     real = rng.uniform(-1, 1, sec.dim).astype(np.complex128)
     cplx = real + 1j * rng.uniform(-1, 1, sec.dim)
+    one = real.copy()
+    one[sec.dim // 3] += 0.25j  # a single entry with an imaginary part still takes the complex product
     Hs = H.scipy()
     st = q.getState(sec, 2)
     got = {}
-    for name, x in (("ground", psi), ("real", real), ("cplx", cplx)):
+    for name, x in (("ground", psi), ("real", real), ("cplx", cplx), ("one", one)):
         st.set(0, x)
         got[name] = st.eval(0, H)
         ref = np.vdot(x, Hs @ x)
         scale = np.abs(np.conj(x) * (Hs @ x)).sum()
         assert abs(got[name] - ref) <= 1e-13 * scale, (name, got[name], ref)
-        if name != "cplx":
+        if name in ("ground", "real"):
             assert got[name].imag == 0.0
     A.call("qd_ham_set_spmv_kernel", H.handle, 110)  # the FP64 CSR path for every product, eval included
-    for name, x in (("ground", psi), ("real", real), ("cplx", cplx)):
+    for name, x in (("ground", psi), ("real", real), ("cplx", cplx), ("one", one)):
         st.set(0, x)
         e_csr = st.eval(0, H)
         scale = np.abs(np.conj(x) * (Hs @ x)).sum()
         assert abs(got[name] - e_csr) <= 1e-13 * scale, (name, got[name], e_csr)
-        if name == "cplx":
-            assert got[name] == e_csr  # the complex state took the CSR product in both
+        if name in ("cplx", "one"):
+            assert got[name] == e_csr  # a state with an imaginary part took the CSR product in both
